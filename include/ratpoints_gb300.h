@@ -1,0 +1,159 @@
+/*
+ * ratpoints_gb300.h - C ABI of the GB300 rational-point search library (librpgpu).
+ *
+ * Plain C types only: pointers, sizes, fixed-width integers.  Errors cross the
+ * ABI as rpg_status codes; rpg_last_error() returns the message of the last
+ * failing call on the calling thread (the reference throws C++ exceptions
+ * carrying the same messages: include/cuda_support.hpp:14-19,
+ * src/point_search.cpp:17-26, src/sieve_plan.cpp:110-113).
+ *
+ * Threading: calls may run on any thread; each call binds the device it is
+ * given (or the calling thread's current device) before any CUDA work, and all
+ * callbacks run synchronously on the calling thread.
+ */
+#ifndef RATPOINTS_GB300_H
+#define RATPOINTS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RPG_ABI_VERSION 1
+
+typedef enum rpg_status {
+    RPG_OK = 0,
+    RPG_E_ARG = 1,            /* invalid argument or option */
+    RPG_E_CUDA = 2,           /* CUDA runtime failure */
+    RPG_E_OOM = 3,            /* device or host allocation failed */
+    RPG_E_TIMEOUT = 4,        /* a bounded device wait expired */
+    RPG_E_INTERNAL = 5,       /* broken internal invariant or counter overflow */
+    RPG_E_NOT_SQUAREFREE = 6  /* the polynomial is not squarefree */
+} rpg_status;
+
+/* Sieve flags. */
+#define RPG_SIEVE_SQUARE_DENOMINATORS 1u /* parameters k give denominators k*k */
+#define RPG_SIEVE_FAST_PLAN 2u           /* this project's plan; default is the reference plan */
+
+/* Sieve plans for rpg_search_options.plan. */
+#define RPG_PLAN_REFERENCE 0
+#define RPG_PLAN_FAST 1
+
+/* Timing and counters of one sieve or search run.  Field meanings follow the
+ * reference's SieveMetrics / SearchMetrics (include/sieve.hpp:13-24,
+ * include/point_search.hpp:41-60). */
+typedef struct rpg_sieve_stats {
+    uint64_t survivor_count;   /* modular survivors emitted */
+    uint64_t word_count;       /* 32-site words per denominator row (reference metric) */
+    uint64_t denominator_count;
+    uint64_t launches;         /* sieve kernel launches */
+    double basis_ms;           /* device table build, CUDA events */
+    double sieve_ms;           /* sieve launches, CUDA events */
+    double plan_ms;
+    double workspace_ms;
+    double basis_wall_ms;
+    double survivor_setup_ms;
+    double verification_ms;
+    double sieve_wall_ms;
+    double initial_mask_bytes;
+    uint64_t h2d_bytes;        /* host-to-device bytes copied */
+    uint64_t d2h_bytes;        /* device-to-host bytes copied */
+} rpg_sieve_stats;
+
+/* Receives one batch of modular survivors (structure of arrays).  The arrays
+ * are valid only during the call.  Return 0 to continue, nonzero to stop the
+ * sieve early (rpg_sieve_run then returns RPG_OK). */
+typedef int (*rpg_candidate_cb)(const int64_t *numerators, const int32_t *denominators,
+                                size_t count, void *user);
+
+/*
+ * Modular sieve over numerators [-numerator_bound, numerator_bound] and
+ * parameters [first, last] (denominators d = k, or k*k with
+ * RPG_SIEVE_SQUARE_DENOMINATORS).  Every site whose F(a, d) is a square modulo
+ * each sieve modulus is delivered exactly once; order is unspecified.
+ * With the reference plan the delivered set is exactly the reference's
+ * survivor set (unreduced pairs included).
+ *
+ * Replaces: ratpoints_gpu::run_modular_sieve (include/sieve.hpp:41-47 of the
+ * reference; driver at src/sieve.cu:503-580).
+ */
+rpg_status rpg_sieve_run(const char *const *coefficients, int32_t coefficient_count,
+                         int64_t numerator_bound, int32_t first, int32_t last, uint32_t flags,
+                         int32_t device, rpg_candidate_cb callback, void *user,
+                         rpg_sieve_stats *stats);
+
+/* A closed x interval; a NULL bound is unbounded.  Bounds use the -l/-u
+ * syntax: [+-]digits[.digits][e[+-]digits]. */
+typedef struct rpg_interval {
+    const char *lower;
+    const char *upper;
+} rpg_interval;
+
+typedef struct rpg_search_options {
+    const char *const *coefficients;  /* c0 .. cn as decimal text */
+    int32_t coefficient_count;
+    int64_t numerator_bound;          /* H */
+    int32_t first;                    /* parameter range (denominators, or k) */
+    int32_t last;
+    const rpg_interval *intervals;    /* ascending, disjoint; may be NULL */
+    int32_t interval_count;
+    int32_t include_infinity;         /* nonzero: report points at infinity first */
+    int32_t batch_size;               /* denominators per batch, 1..65536 */
+    int32_t square_denominators;
+    int32_t plan;                     /* RPG_PLAN_REFERENCE or RPG_PLAN_FAST */
+    int32_t device;                   /* CUDA device ordinal, -1: current */
+    int32_t verify_threads;           /* host verification threads, 0: all cores */
+} rpg_search_options;
+
+/* One verified point (numerator : ordinate : denominator); the ordinate is
+ * the non-negative root in decimal, valid only during the call.  Return
+ * nonzero to continue, 0 to stop the search. */
+typedef int (*rpg_point_cb)(int64_t numerator, const char *ordinate, int64_t denominator,
+                            void *user);
+
+/*
+ * Full search: infinity first (if requested and present), then verified
+ * points with gcd(a, d) = 1 in batch order, (d, a) ascending within a batch,
+ * filtered by the intervals.  Fails with RPG_E_NOT_SQUAREFREE before any
+ * callback if f is not squarefree.
+ *
+ * Replaces: ratpoints_gpu::PointSearch / PointSearch::run
+ * (include/point_search.hpp:62-78, src/point_search.cpp:155-240).
+ */
+rpg_status rpg_point_search(const rpg_search_options *options, rpg_point_cb callback, void *user,
+                            rpg_sieve_stats *stats);
+
+/* Exact predicates.  Replace ExactPolynomial::is_squarefree and
+ * ExactPolynomial::square_root (src/exact_polynomial.cpp:25-71). */
+rpg_status rpg_is_squarefree(const char *const *coefficients, int32_t coefficient_count,
+                             int32_t *is_squarefree);
+rpg_status rpg_square_root(const char *const *coefficients, int32_t coefficient_count,
+                           int64_t numerator, int64_t denominator, char *ordinate,
+                           size_t ordinate_capacity, int32_t *is_point);
+
+/* The ratpoints_gpu command line in-process (src/main.cpp:48-85): writes to
+ * stdout/stderr and returns the exit status. */
+int32_t rpg_cli_main(int32_t argc, char **argv);
+
+/* Benchmark session: tables resident on the device, survivors counted on the
+ * device only.  rpg_session_count reports the CUDA-event time of the sieve
+ * launches it issues. */
+typedef struct rpg_session rpg_session;
+rpg_status rpg_session_create(const char *const *coefficients, int32_t coefficient_count,
+                              int64_t numerator_bound, uint32_t flags, int32_t device,
+                              rpg_session **session);
+rpg_status rpg_session_count(rpg_session *session, int32_t first, int32_t last,
+                             int32_t batch_size, uint64_t *survivors, double *device_ms);
+void rpg_session_destroy(rpg_session *session);
+
+int32_t rpg_device_count(void);
+int32_t rpg_abi_version(void);
+const char *rpg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RATPOINTS_GB300_H */

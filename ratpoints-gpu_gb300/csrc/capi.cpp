@@ -1,0 +1,293 @@
+// extern "C" entry points of librpgpu (include/ratpoints_gb300.h).
+#include "ratpoints_gb300.h"
+
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "cli.hpp"
+#include "exact.hpp"
+#include "plan.hpp"
+#include "search.hpp"
+#include "sieve.hpp"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+rpg_status fail(rpg_status status, const std::string &message) {
+    g_last_error = message;
+    return status;
+}
+
+template <typename F>
+rpg_status guarded(F &&body) {
+    try {
+        g_last_error.clear();
+        return body();
+    } catch (const rpg::CudaError &e) {
+        const std::string what = e.what();
+        if (what.find("out of memory") != std::string::npos) return fail(RPG_E_OOM, what);
+        return fail(RPG_E_CUDA, what);
+    } catch (const std::bad_alloc &e) {
+        return fail(RPG_E_OOM, e.what());
+    } catch (const std::invalid_argument &e) {
+        const std::string what = e.what();
+        if (what == "polynomial is not squarefree") return fail(RPG_E_NOT_SQUAREFREE, what);
+        return fail(RPG_E_ARG, what);
+    } catch (const std::exception &e) {
+        return fail(RPG_E_INTERNAL, e.what());
+    }
+}
+
+bool coefficients_from(const char *const *c, int32_t n, std::vector<std::string> &out,
+                       std::string &error) {
+    if (!c || n < 2 || n > 101) {
+        error = "supported polynomial degrees are 1 through 100";
+        return false;
+    }
+    out.clear();
+    for (int32_t i = 0; i < n; ++i) {
+        if (!c[i]) {
+            error = "coefficients must be decimal integers";
+            return false;
+        }
+        std::string s(c[i]);
+        if (!s.empty() && s.front() == '+') s.erase(0, 1);
+        rpg::BigInt probe;
+        if (!rpg::BigInt::parse(s, probe)) {
+            error = "coefficients must be decimal integers";
+            return false;
+        }
+        out.push_back(s);
+    }
+    rpg::BigInt lead;
+    rpg::BigInt::parse(out.back(), lead);
+    if (lead.is_zero()) {
+        error = "leading coefficient must be nonzero";
+        return false;
+    }
+    return true;
+}
+
+void fill_stats(rpg_sieve_stats *stats, const rpg::SearchMetrics &m) {
+    if (!stats) return;
+    std::memset(stats, 0, sizeof *stats);
+    stats->survivor_count = m.modular_survivors;
+    stats->word_count = m.word_count;
+    stats->denominator_count = m.denominator_count;
+    stats->launches = m.launches;
+    stats->basis_ms = m.basis_ms;
+    stats->sieve_ms = m.sieve_ms;
+    stats->plan_ms = m.plan_ms;
+    stats->workspace_ms = m.workspace_ms;
+    stats->basis_wall_ms = m.basis_wall_ms;
+    stats->survivor_setup_ms = m.survivor_setup_ms;
+    stats->verification_ms = m.verification_ms;
+    stats->sieve_wall_ms = m.sieve_wall_ms;
+    stats->initial_mask_bytes = double(m.initial_mask_bytes);
+    stats->h2d_bytes = m.h2d_bytes;
+    stats->d2h_bytes = m.d2h_bytes;
+}
+
+}  // namespace
+
+struct rpg_session {
+    std::unique_ptr<rpg::Sieve> sieve;
+    cudaEvent_t begin = nullptr, end = nullptr;
+    ~rpg_session() {
+        if (begin) cudaEventDestroy(begin);
+        if (end) cudaEventDestroy(end);
+    }
+};
+
+extern "C" {
+
+rpg_status rpg_sieve_run(const char *const *coefficients, int32_t coefficient_count,
+                         int64_t numerator_bound, int32_t first, int32_t last, uint32_t flags,
+                         int32_t device, rpg_candidate_cb callback, void *user,
+                         rpg_sieve_stats *stats) {
+    return guarded([&]() -> rpg_status {
+        std::vector<std::string> coeffs;
+        std::string error;
+        if (!coefficients_from(coefficients, coefficient_count, coeffs, error))
+            return fail(RPG_E_ARG, error);
+        if (numerator_bound < 1) return fail(RPG_E_ARG, "maximum height must be positive");
+        if (first < 1 || first > last) return fail(RPG_E_ARG, "invalid denominator range");
+        if (!callback) return fail(RPG_E_ARG, "callback must not be NULL");
+        rpg::SieveOptions so;
+        so.plan = (flags & RPG_SIEVE_FAST_PLAN) ? rpg::PlanKind::fast : rpg::PlanKind::reference;
+        so.square = (flags & RPG_SIEVE_SQUARE_DENOMINATORS) != 0;
+        so.device = device;
+        if (so.square && last > 46340) return fail(RPG_E_ARG, "invalid denominator range");
+        rpg::Sieve sieve(coeffs, numerator_bound, so);
+        sieve.start(first, last, 1 << 16);
+        rpg::BatchView view;
+        unsigned long long total = 0, denominators = 0;
+        std::vector<int64_t> a64;
+        std::vector<int32_t> d32;
+        bool stopped = false;
+        while (!stopped && sieve.next(view)) {
+            total += view.count;
+            if (view.complete) denominators += (unsigned long long)(view.last - view.first + 1);
+            if (!view.count) continue;
+            a64.assign(view.a, view.a + view.count);
+            d32.assign(view.d, view.d + view.count);
+            if (callback(a64.data(), d32.data(), view.count, user) != 0) stopped = true;
+        }
+        if (stopped) sieve.cancel();
+        if (stats) {
+            std::memset(stats, 0, sizeof *stats);
+            const auto &t = sieve.timings();
+            stats->survivor_count = total;
+            stats->word_count = (uint64_t)rpg::word_count32(numerator_bound);
+            stats->denominator_count = denominators;
+            stats->launches = t.launches;
+            stats->basis_ms = t.table_ms;
+            stats->sieve_ms = t.sieve_ms;
+            stats->plan_ms = t.plan_ms;
+            stats->workspace_ms = t.workspace_ms;
+            stats->basis_wall_ms = t.table_wall_ms;
+            stats->h2d_bytes = t.h2d_bytes;
+            stats->d2h_bytes = t.d2h_bytes;
+        }
+        return RPG_OK;
+    });
+}
+
+rpg_status rpg_point_search(const rpg_search_options *o, rpg_point_cb callback, void *user,
+                            rpg_sieve_stats *stats) {
+    return guarded([&]() -> rpg_status {
+        if (!o || !callback) return fail(RPG_E_ARG, "options and callback must not be NULL");
+        rpg::SearchOptions s;
+        std::string error;
+        if (!coefficients_from(o->coefficients, o->coefficient_count, s.coefficients, error))
+            return fail(RPG_E_ARG, error);
+        if (o->numerator_bound < 1) return fail(RPG_E_ARG, "maximum height must be positive");
+        if (o->first < 1 || o->first > o->last) return fail(RPG_E_ARG, "empty denominator range");
+        s.numerator_bound = o->numerator_bound;
+        s.first = o->first;
+        s.last = o->last;
+        if (o->square_denominators && s.last > 46340) s.last = 46340;
+        for (int32_t i = 0; i < o->interval_count; ++i) {
+            rpg::SearchInterval iv;
+            const rpg_interval &src = o->intervals[i];
+            iv.lower_infinite = src.lower == nullptr;
+            iv.upper_infinite = src.upper == nullptr;
+            if (src.lower && !rpg::parse_real(src.lower, "interval lower bound", iv.lower, error))
+                return fail(RPG_E_ARG, error);
+            if (src.upper && !rpg::parse_real(src.upper, "interval upper bound", iv.upper, error))
+                return fail(RPG_E_ARG, error);
+            s.intervals.push_back(iv);
+        }
+        s.include_infinity = o->include_infinity != 0;
+        s.batch_size = o->batch_size;
+        s.square = o->square_denominators != 0;
+        s.plan = o->plan == RPG_PLAN_REFERENCE ? rpg::PlanKind::reference : rpg::PlanKind::fast;
+        if (o->device >= 0) s.devices = {o->device};
+        s.verify_threads = o->verify_threads;
+        rpg::PointSearch search(s);
+        rpg::SearchMetrics m = search.run([&](const rpg::PointPair &p) {
+            return callback(p.numerator, p.ordinate.c_str(), p.denominator, user) != 0;
+        });
+        fill_stats(stats, m);
+        return RPG_OK;
+    });
+}
+
+rpg_status rpg_is_squarefree(const char *const *coefficients, int32_t coefficient_count,
+                             int32_t *is_squarefree) {
+    return guarded([&]() -> rpg_status {
+        std::vector<std::string> coeffs;
+        std::string error;
+        if (!coefficients_from(coefficients, coefficient_count, coeffs, error))
+            return fail(RPG_E_ARG, error);
+        if (!is_squarefree) return fail(RPG_E_ARG, "output must not be NULL");
+        *is_squarefree = rpg::ExactPolynomial(coeffs).is_squarefree() ? 1 : 0;
+        return RPG_OK;
+    });
+}
+
+rpg_status rpg_square_root(const char *const *coefficients, int32_t coefficient_count,
+                           int64_t numerator, int64_t denominator, char *ordinate,
+                           size_t ordinate_capacity, int32_t *is_point) {
+    return guarded([&]() -> rpg_status {
+        std::vector<std::string> coeffs;
+        std::string error;
+        if (!coefficients_from(coefficients, coefficient_count, coeffs, error))
+            return fail(RPG_E_ARG, error);
+        if (!is_point) return fail(RPG_E_ARG, "output must not be NULL");
+        std::string root;
+        const bool point = rpg::ExactPolynomial(coeffs).square_root(numerator, denominator, root);
+        *is_point = point ? 1 : 0;
+        if (point && ordinate) {
+            if (root.size() + 1 > ordinate_capacity)
+                return fail(RPG_E_ARG, "ordinate buffer too small");
+            std::memcpy(ordinate, root.c_str(), root.size() + 1);
+        }
+        return RPG_OK;
+    });
+}
+
+int32_t rpg_cli_main(int32_t argc, char **argv) { return rpg::run_cli(argc, argv); }
+
+rpg_status rpg_session_create(const char *const *coefficients, int32_t coefficient_count,
+                              int64_t numerator_bound, uint32_t flags, int32_t device,
+                              rpg_session **session) {
+    return guarded([&]() -> rpg_status {
+        if (!session) return fail(RPG_E_ARG, "session must not be NULL");
+        *session = nullptr;
+        std::vector<std::string> coeffs;
+        std::string error;
+        if (!coefficients_from(coefficients, coefficient_count, coeffs, error))
+            return fail(RPG_E_ARG, error);
+        if (numerator_bound < 1) return fail(RPG_E_ARG, "maximum height must be positive");
+        rpg::SieveOptions so;
+        so.plan = (flags & RPG_SIEVE_FAST_PLAN) ? rpg::PlanKind::fast : rpg::PlanKind::reference;
+        so.square = (flags & RPG_SIEVE_SQUARE_DENOMINATORS) != 0;
+        so.device = device;
+        std::unique_ptr<rpg_session> s(new rpg_session);
+        s->sieve.reset(new rpg::Sieve(coeffs, numerator_bound, so));
+        rpg::check_cuda(cudaEventCreate(&s->begin), "cudaEventCreate");
+        rpg::check_cuda(cudaEventCreate(&s->end), "cudaEventCreate");
+        *session = s.release();
+        return RPG_OK;
+    });
+}
+
+rpg_status rpg_session_count(rpg_session *session, int32_t first, int32_t last, int32_t batch_size,
+                             uint64_t *survivors, double *device_ms) {
+    return guarded([&]() -> rpg_status {
+        if (!session) return fail(RPG_E_ARG, "session must not be NULL");
+        if (first < 1 || first > last || batch_size < 1)
+            return fail(RPG_E_ARG, "invalid denominator range");
+        cudaStream_t st = session->sieve->stream();
+        rpg::check_cuda(cudaEventRecord(session->begin, st), "cudaEventRecord");
+        const unsigned long long n = session->sieve->count_only(first, last, batch_size);
+        rpg::check_cuda(cudaEventRecord(session->end, st), "cudaEventRecord");
+        rpg::check_cuda(cudaEventSynchronize(session->end), "cudaEventSynchronize");
+        float ms = 0;
+        rpg::check_cuda(cudaEventElapsedTime(&ms, session->begin, session->end),
+                        "cudaEventElapsedTime");
+        if (survivors) *survivors = n;
+        if (device_ms) *device_ms = ms;
+        return RPG_OK;
+    });
+}
+
+void rpg_session_destroy(rpg_session *session) { delete session; }
+
+int32_t rpg_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+int32_t rpg_abi_version(void) { return RPG_ABI_VERSION; }
+
+const char *rpg_last_error(void) { return g_last_error.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,49 @@
+// Sieve plans: which moduli reject which (a, d) sites, and the host-side
+// tables the device kernels are built from.
+//
+// The reference plan restates the reference's SievePlan (src/sieve_plan.hpp:27-46,
+// src/sieve_plan.cpp:83-151, 153-193): candidate primes are the 36 largest
+// primes below 512; a denominator d uses the 32 largest that do not divide d;
+// a site survives iff f(a/d) mod p is a square (0 included) for all 32.  Its
+// survivor set is the reference's, unreduced pairs included.
+//
+// The fast plan (this project's) keeps every reference test and adds filters
+// that no point can fail, so its survivors are a subset of the reference's
+// that still holds every point:
+//   - gcd(a, d) = 1 for the primes 2, 3, 5, 7 and every other small prime q | d;
+//   - F(a, d) is a square modulo 64;
+//   - f(a/d) mod q is a square for the small primes q in the wheel and the
+//     composite moduli (or, when q | d, c_n is a square mod q for even n).
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace rpg {
+
+constexpr int kCandidatePrimes = 36;   // sieve_plan.hpp:29 (NUM_PRIMES + 4)
+constexpr int kSelectedPrimes = 32;    // sieve_plan.hpp:11 (NUM_PRIMES)
+constexpr int kMaximumPrime = 512;     // sieve_plan.hpp:30
+
+const std::array<int, kCandidatePrimes> &candidate_primes();  // ascending, 293 .. 509
+
+// Residue of a decimal integer modulo m (m < 2^31), sign folded into [0, m).
+int decimal_mod(const std::string &text, int modulus);
+long long mod_inverse(long long value, long long modulus);
+
+// affine[x] = 1 iff f(x) mod p is a square (0 included), for x in [0, p).
+std::vector<std::uint8_t> affine_mask(int prime, const std::vector<std::string> &coefficients);
+
+// Indices into candidate_primes() of the 32 largest candidates not dividing
+// denominator, largest first.  Returns false if fewer than 32 qualify.
+bool select_primes(long long denominator, int *indices);
+
+// ceil((2H + 1) / 64): 64-site words covering a in [-H, H].
+long long word_count64(long long bound);
+// floor((2H + 32) / 32): the reference's 32-site word count (sieve_plan.cpp:109),
+// reported by the -v metrics line.
+long long word_count32(long long bound);
+
+}  // namespace rpg

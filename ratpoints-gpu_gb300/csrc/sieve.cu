@@ -1,0 +1,648 @@
+// Device sieve: table build and sieve kernels for sm_103a, and the host driver.
+//
+// Reference behaviour restated here (see the file:line citations per item):
+//   - mask basis: bit j of word u of row r for prime p is
+//     affine[((-H + 64 u + j) * r^-1) mod p], row 0 zero (src/sieve.cu:141-172,
+//     with 64-site words);
+//   - sieve: a site survives iff all 32 selected primes accept it; the last word
+//     is clipped at +H (src/sieve.cu:221-388, 196-213, 324-330);
+//   - survivors are (a, d) pairs, d = k or k*k (src/sieve.cu:179-181, 250-252).
+//
+// GB300 design: the tables for all 36 candidate primes are built once per search
+// on the device; one persistent launch per denominator batch; each CTA stages
+// the rows of its denominator's 10 largest selected primes into shared memory,
+// sweeps 64-bit words (4 per thread per step, lane-contiguous, rows extended so
+// no wrap test is needed inside a step), and compacts the rare stage-1
+// survivors into a per-warp queue that a full warp then checks against the
+// remaining 22 primes from L2-resident tables before warp-aggregated emission.
+#include "sieve.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+
+#include "plan.hpp"
+#include "sieve_device.cuh"
+
+namespace rpg {
+
+void check_cuda(cudaError_t status, const char *what) {
+    if (status != cudaSuccess)
+        throw CudaError(std::string(what) + ": " + cudaGetErrorString(status));
+}
+
+namespace dev {
+
+constexpr int kK = 4;                        // words per thread per step
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * kWarpSize;
+constexpr int kStride = kThreads * kK;       // words per CTA step
+constexpr int kExt = kWarpSize * (kK - 1);   // row extension (words)
+constexpr int kRefFast = 10;                 // stage-1 primes held in shared memory
+constexpr int kSlotWords = 608;              // >= 509 + kExt, even
+constexpr int kQueue = 64;                   // per-warp stage-2 queue entries
+constexpr long long kMaxTileWords = 1LL << 30;
+constexpr std::size_t kRefSmem =
+    std::size_t(kRefFast) * kSlotWords * 8 + std::size_t(kWarps) * kQueue * 12;
+
+static_assert(kSlotWords >= kMaximumPrime + kExt, "slot must hold an extended row");
+static_assert(kSlotWords % 2 == 0, "slots must keep 16-byte alignment");
+
+struct RefTables {
+    const u64 *rows;
+    long long offset[kCandidatePrimes];   // word offset of (prime i, residue 0)
+    int length[kCandidatePrimes];         // words per row (p + kExt rounded up to even)
+    int prime[kCandidatePrimes];
+    u32 magic[kCandidatePrimes];
+};
+
+struct SieveArgs {
+    long long bound;     // H
+    long long words;     // 64-site words per denominator row
+    long long w_lo;      // word range of this launch
+    long long w_hi;
+    long long k_first;   // first parameter
+    int k_count;
+    int square;
+    long long *out_a;
+    int *out_d;
+    unsigned long long *out_count;
+    unsigned long long capacity;
+};
+
+__global__ void ref_table_kernel(u64 *rows, RefTables T, const unsigned char *affine,
+                                 const unsigned short *inverse, const int *neg_h_mod,
+                                 long long total) {
+    long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (id >= total) return;
+    int i = 0;
+    while (i + 1 < kCandidatePrimes && T.offset[i + 1] <= id) ++i;
+    const int p = T.prime[i], L = T.length[i];
+    const long long rel = id - T.offset[i];
+    const int r = int(rel / L);
+    const int u = int(rel % L) % p;
+    u64 word = 0;
+    if (r != 0) {
+        const int inv = inverse[i * kMaximumPrime + r];
+        const int x0 = (neg_h_mod[i] + int((64LL * u) % p)) % p;
+        int x = int((long long)x0 * inv % p);
+        const unsigned char *aff = affine + i * kMaximumPrime;
+        for (int j = 0; j < 64; ++j) {
+            if (aff[x]) word |= u64(1) << j;
+            x += inv;
+            if (x >= p) x -= p;
+        }
+    }
+    rows[id] = word;
+}
+
+// Stage 2 for up to 32 queued words (one per lane), then emission.
+__device__ __forceinline__ void ref_drain(const u64 *qmask, const u32 *qoff, int start, int n,
+                                          const RefTables &T, const SieveArgs &A, int denominator,
+                                          const int *s_prime, const u32 *s_magic,
+                                          const u32 *s_bmod, const long long *s_row) {
+    const int lane = threadIdx.x & 31;
+    u64 m = 0;
+    u32 off = 0;
+    if (lane < n) {
+        m = qmask[start + lane];
+        off = qoff[start + lane];
+    }
+    __syncwarp();
+    const long long w = A.w_lo + off;
+    if (m) {
+        for (int s = kRefFast; s < kSelectedPrimes; ++s) {
+            const u32 p = u32(s_prime[s]);
+            u32 idx = s_bmod[s] + mod_small(off, p, s_magic[s]);
+            if (idx >= p) idx -= p;
+            m &= __ldg(T.rows + s_row[s] + idx);
+            if (!m) break;
+        }
+        if (m && w == A.words - 1) {
+            const int valid = int(2 * A.bound + 1 - 64 * (A.words - 1));
+            if (valid < 64) m &= (u64(1) << valid) - 1;
+        }
+    }
+    emit_survivors(m, w, A.bound, denominator, A.out_a, A.out_d, A.out_count, A.capacity);
+}
+
+__global__ void __launch_bounds__(kThreads) ref_sieve_kernel(RefTables T, SieveArgs A) {
+    extern __shared__ __align__(16) u64 smem[];
+    u64 *rows = smem;
+    u64 *qmask = rows + kRefFast * kSlotWords;
+    u32 *qoff = reinterpret_cast<u32 *>(qmask + kWarps * kQueue);
+
+    __shared__ int s_prime[kSelectedPrimes];
+    __shared__ u32 s_magic[kSelectedPrimes];
+    __shared__ u32 s_bmod[kSelectedPrimes];
+    __shared__ long long s_row[kSelectedPrimes];
+    __shared__ int s_len[kSelectedPrimes];
+    __shared__ int s_ok;
+
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const long long tile_words = A.w_hi - A.w_lo;
+    u64 *wq_mask = qmask + warp * kQueue;
+    u32 *wq_off = qoff + warp * kQueue;
+
+    for (int item = blockIdx.x; item < A.k_count; item += gridDim.x) {
+        const long long k = A.k_first + item;
+        const long long d = A.square ? k * k : k;
+        if (threadIdx.x == 0) {
+            int n = 0;
+            for (int i = kCandidatePrimes - 1; i >= 0 && n < kSelectedPrimes; --i) {
+                const int p = T.prime[i];
+                const int r = int(d % p);
+                if (r == 0) continue;
+                s_prime[n] = p;
+                s_magic[n] = T.magic[i];
+                s_row[n] = T.offset[i] + (long long)r * T.length[i];
+                s_len[n] = T.length[i];
+                s_bmod[n] = u32(A.w_lo % p);
+                ++n;
+            }
+            s_ok = n == kSelectedPrimes;
+        }
+        __syncthreads();
+        if (!s_ok) {  // unreachable for d < 2^31 (at most 3 candidates divide it)
+            __syncthreads();
+            continue;
+        }
+        for (int s = 0; s < kRefFast; ++s) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(T.rows + s_row[s]);
+            uint4 *dst = reinterpret_cast<uint4 *>(rows + s * kSlotWords);
+            const int n16 = s_len[s] >> 1;
+            for (int t = threadIdx.x; t < n16; t += kThreads) dst[t] = __ldg(src + t);
+        }
+        __syncthreads();
+
+        u32 o[kRefFast], st[kRefFast], pb[kRefFast];
+        const u32 first = u32(warp * kWarpSize * kK + lane);
+#pragma unroll
+        for (int s = 0; s < kRefFast; ++s) {
+            const u32 p = u32(s_prime[s]);
+            o[s] = ((s_bmod[s] + first) % p) * 8u + u32(s * kSlotWords * 8);
+            st[s] = (u32(kStride) % p) * 8u;
+            pb[s] = p * 8u;
+        }
+        int qn = 0;
+        const unsigned char *rbase = reinterpret_cast<const unsigned char *>(rows);
+        for (long long off0 = 0; off0 < tile_words; off0 += kStride) {
+            u64 acc[kK];
+#pragma unroll
+            for (int kk = 0; kk < kK; ++kk) acc[kk] = ~u64(0);
+#pragma unroll
+            for (int s = 0; s < kRefFast; ++s) {
+                const unsigned char *rb = rbase + o[s];
+#pragma unroll
+                for (int kk = 0; kk < kK; ++kk)
+                    acc[kk] &= *reinterpret_cast<const u64 *>(rb + 256 * kk);
+                const u32 lo = u32(s * kSlotWords * 8);
+                const u32 t = o[s] + st[s];
+                o[s] = (t - lo >= pb[s]) ? t - pb[s] : t;
+            }
+#pragma unroll
+            for (int kk = 0; kk < kK; ++kk) {
+                const long long off = off0 + warp * kWarpSize * kK + kWarpSize * kk + lane;
+                const bool live = acc[kk] != 0 && off < tile_words;
+                const u32 b = __ballot_sync(kFullMask, live);
+                if (b) {
+                    const int pos = qn + __popc(b & lanemask_lt());
+                    if (live) {
+                        wq_mask[pos] = acc[kk];
+                        wq_off[pos] = u32(off);
+                    }
+                    qn += __popc(b);
+                    if (qn >= 32) {
+                        __syncwarp();
+                        ref_drain(wq_mask, wq_off, qn - 32, 32, T, A, int(d), s_prime, s_magic,
+                                  s_bmod, s_row);
+                        qn -= 32;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        ref_drain(wq_mask, wq_off, 0, qn, T, A, int(d), s_prime, s_magic, s_bmod, s_row);
+        __syncthreads();
+    }
+}
+
+}  // namespace dev
+
+// ---------------------------------------------------------------------------
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+double ms_since(Clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
+template <typename T>
+T *device_alloc(std::size_t count, const char *what) {
+    void *p = nullptr;
+    check_cuda(cudaMalloc(&p, std::max<std::size_t>(count, 1) * sizeof(T)), what);
+    return static_cast<T *>(p);
+}
+
+}  // namespace
+
+struct Sieve::Impl {
+    SieveOptions opt;
+    long long bound = 0, words = 0;
+    int device = 0, grid = 0;
+    cudaStream_t stream = nullptr, copy_stream = nullptr;
+    dev::RefTables T{};
+    dev::u64 *rows = nullptr;
+    long long capacity = 0;
+    SieveTimings timings;
+
+    struct Buffer {
+        long long *a = nullptr;
+        int *d = nullptr;
+        unsigned long long *count = nullptr;
+        cudaEvent_t begin = nullptr, end = nullptr;
+        long long first = 0, last = 0;
+        bool busy = false;
+    };
+    Buffer buf[2];
+    unsigned long long *h_count = nullptr;  // pinned, one per buffer
+    long long *h_a = nullptr;
+    int *h_d = nullptr;
+
+    // Batch queue.
+    long long q_next = 0, q_last = -1, q_batch = 1;
+    std::deque<int> order;  // buffers in flight, oldest first
+
+    // Pieces of an overflowed batch still to deliver, in parameter/word order.
+    struct Piece {
+        long long first, last, w_lo, w_hi;
+    };
+    std::deque<Piece> pieces;
+    long long piece_batch_first = 0, piece_batch_last = 0;
+
+    ~Impl() { release(); }
+
+    void release() {
+        for (auto &b : buf) {
+            cudaFree(b.a);
+            cudaFree(b.d);
+            cudaFree(b.count);
+            if (b.begin) cudaEventDestroy(b.begin);
+            if (b.end) cudaEventDestroy(b.end);
+            b = Buffer{};
+        }
+        cudaFree(rows);
+        rows = nullptr;
+        if (h_count) cudaFreeHost(h_count);
+        if (h_a) cudaFreeHost(h_a);
+        if (h_d) cudaFreeHost(h_d);
+        h_count = nullptr;
+        h_a = nullptr;
+        h_d = nullptr;
+        if (stream) cudaStreamDestroy(stream);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
+        stream = copy_stream = nullptr;
+    }
+
+    void build_tables(const std::vector<std::string> &coefficients) {
+        auto t0 = Clock::now();
+        const auto &primes = candidate_primes();
+        long long total = 0;
+        for (int i = 0; i < kCandidatePrimes; ++i) {
+            const int p = primes[i];
+            T.prime[i] = p;
+            T.length[i] = (p + dev::kExt + 1) & ~1;
+            T.offset[i] = total;
+            T.magic[i] = dev::magic40(dev::u32(p));
+            total += (long long)p * T.length[i];
+        }
+        std::vector<unsigned char> affine(std::size_t(kCandidatePrimes) * kMaximumPrime, 0);
+        std::vector<unsigned short> inverse(std::size_t(kCandidatePrimes) * kMaximumPrime, 0);
+        std::vector<int> neg_h(kCandidatePrimes);
+        for (int i = 0; i < kCandidatePrimes; ++i) {
+            const int p = primes[i];
+            auto aff = affine_mask(p, coefficients);
+            std::copy(aff.begin(), aff.end(), affine.begin() + std::size_t(i) * kMaximumPrime);
+            for (int v = 1; v < p; ++v)
+                inverse[std::size_t(i) * kMaximumPrime + v] = (unsigned short)mod_inverse(v, p);
+            neg_h[i] = int((p - bound % p) % p);
+        }
+        timings.plan_ms += ms_since(t0);
+        auto t1 = Clock::now();
+        rows = device_alloc<dev::u64>(std::size_t(total), "cudaMalloc(sieve tables)");
+        unsigned char *d_aff = device_alloc<unsigned char>(affine.size(), "cudaMalloc(affine)");
+        unsigned short *d_inv = device_alloc<unsigned short>(inverse.size(), "cudaMalloc(inverse)");
+        int *d_neg = device_alloc<int>(neg_h.size(), "cudaMalloc(bound residues)");
+        timings.workspace_ms += ms_since(t1);
+        T.rows = rows;
+        cudaEvent_t e0, e1;
+        check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
+        check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
+        check_cuda(cudaEventRecord(e0, stream), "cudaEventRecord");
+        check_cuda(cudaMemcpyAsync(d_aff, affine.data(), affine.size(), cudaMemcpyHostToDevice, stream),
+                   "upload affine tables");
+        check_cuda(cudaMemcpyAsync(d_inv, inverse.data(), inverse.size() * sizeof(unsigned short),
+                                   cudaMemcpyHostToDevice, stream),
+                   "upload inverses");
+        check_cuda(cudaMemcpyAsync(d_neg, neg_h.data(), neg_h.size() * sizeof(int),
+                                   cudaMemcpyHostToDevice, stream),
+                   "upload bound residues");
+        const int threads = 256;
+        const long long blocks = (total + threads - 1) / threads;
+        timings.h2d_bytes += affine.size() + inverse.size() * sizeof(unsigned short) +
+                             neg_h.size() * sizeof(int);
+        dev::ref_table_kernel<<<unsigned(blocks), threads, 0, stream>>>(rows, T, d_aff, d_inv, d_neg,
+                                                                         total);
+        check_cuda(cudaGetLastError(), "ref_table_kernel launch");
+        check_cuda(cudaEventRecord(e1, stream), "cudaEventRecord");
+        check_cuda(cudaEventSynchronize(e1), "table build");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        timings.table_ms += ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(d_aff);
+        cudaFree(d_inv);
+        cudaFree(d_neg);
+        timings.table_wall_ms += ms_since(t0);
+    }
+
+    void init(const std::vector<std::string> &coefficients) {
+        auto t0 = Clock::now();
+        if (opt.device >= 0) check_cuda(cudaSetDevice(opt.device), "cudaSetDevice");
+        check_cuda(cudaGetDevice(&device), "cudaGetDevice");
+        check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(cudaFuncSetAttribute(dev::ref_sieve_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(dev::kRefSmem)),
+                   "cudaFuncSetAttribute");
+        int sms = 0, per_sm = 0;
+        check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device),
+                   "cudaDeviceGetAttribute");
+        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::ref_sieve_kernel,
+                                                                 dev::kThreads, dev::kRefSmem),
+                   "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        grid = std::max(1, sms * std::max(1, per_sm));
+        // RPG_SURVIVOR_CAPACITY overrides the per-buffer survivor capacity (at
+        // least 64, one word's worth); tests use it to drive the split path.
+        capacity = opt.capacity;
+        if (const char *env = std::getenv("RPG_SURVIVOR_CAPACITY")) capacity = std::atoll(env);
+        capacity = std::max<long long>(capacity, 64);
+        for (auto &b : buf) {
+            b.a = device_alloc<long long>(std::size_t(capacity), "cudaMalloc(survivors)");
+            b.d = device_alloc<int>(std::size_t(capacity), "cudaMalloc(survivors)");
+            b.count = device_alloc<unsigned long long>(1, "cudaMalloc(count)");
+            check_cuda(cudaEventCreate(&b.begin), "cudaEventCreate");
+            check_cuda(cudaEventCreate(&b.end), "cudaEventCreate");
+        }
+        check_cuda(cudaMallocHost(&h_count, 2 * sizeof(unsigned long long)), "cudaMallocHost");
+        check_cuda(cudaMallocHost(&h_a, std::size_t(capacity) * sizeof(long long)), "cudaMallocHost");
+        check_cuda(cudaMallocHost(&h_d, std::size_t(capacity) * sizeof(int)), "cudaMallocHost");
+        timings.workspace_ms += ms_since(t0);
+        build_tables(coefficients);
+    }
+
+    dev::SieveArgs args(int which, long long first, long long last, long long w_lo, long long w_hi) {
+        dev::SieveArgs A{};
+        A.bound = bound;
+        A.words = words;
+        A.w_lo = w_lo;
+        A.w_hi = w_hi;
+        A.k_first = first;
+        A.k_count = int(last - first + 1);
+        A.square = opt.square ? 1 : 0;
+        A.out_a = buf[which].a;
+        A.out_d = buf[which].d;
+        A.out_count = buf[which].count;
+        A.capacity = (unsigned long long)capacity;
+        return A;
+    }
+
+    void launch_counting(long long first, long long last, long long w_lo, long long w_hi) {
+        const dev::SieveArgs A = args(0, first, last, w_lo, w_hi);
+        const int blocks = int(std::min<long long>(grid, A.k_count));
+        dev::ref_sieve_kernel<<<blocks, dev::kThreads, dev::kRefSmem, stream>>>(T, A);
+        check_cuda(cudaGetLastError(), "sieve kernel launch");
+        ++timings.launches;
+    }
+
+    void launch(int which, long long first, long long last, long long w_lo, long long w_hi) {
+        Buffer &b = buf[which];
+        b.first = first;
+        b.last = last;
+        b.busy = true;
+        const dev::SieveArgs A = args(which, first, last, w_lo, w_hi);
+        check_cuda(cudaMemsetAsync(b.count, 0, sizeof(unsigned long long), stream), "cudaMemsetAsync");
+        check_cuda(cudaEventRecord(b.begin, stream), "cudaEventRecord");
+        const int blocks = int(std::min<long long>(grid, A.k_count));
+        dev::ref_sieve_kernel<<<blocks, dev::kThreads, dev::kRefSmem, stream>>>(T, A);
+        check_cuda(cudaGetLastError(), "sieve kernel launch");
+        check_cuda(cudaEventRecord(b.end, stream), "cudaEventRecord");
+        check_cuda(cudaMemcpyAsync(h_count + which, b.count, sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, stream),
+                   "download survivor count");
+        timings.d2h_bytes += sizeof(unsigned long long);
+        ++timings.launches;
+    }
+
+    // Launch queued batches into free buffers (pipelined path, rows that fit
+    // one launch).  Rows longer than kMaxTileWords go through pieces instead.
+    void refill() {
+        if (words > dev::kMaxTileWords || !pieces.empty()) return;
+        while (order.size() < 2 && q_next <= q_last) {
+            const int which = buf[0].busy ? 1 : 0;
+            if (buf[which].busy) break;
+            const long long first = q_next;
+            const long long last = std::min(q_last, first + q_batch - 1);
+            q_next = last + 1;
+            launch(which, first, last, 0, words);
+            order.push_back(which);
+        }
+    }
+
+    float elapsed(const Buffer &b) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, b.begin, b.end);
+        return ms;
+    }
+
+    void copy_out(int which, std::size_t n) {
+        Buffer &b = buf[which];
+        if (!n) return;
+        check_cuda(cudaStreamWaitEvent(copy_stream, b.end, 0), "cudaStreamWaitEvent");
+        check_cuda(cudaMemcpyAsync(h_a, b.a, n * sizeof(long long), cudaMemcpyDeviceToHost,
+                                   copy_stream),
+                   "download survivors");
+        check_cuda(cudaMemcpyAsync(h_d, b.d, n * sizeof(int), cudaMemcpyDeviceToHost, copy_stream),
+                   "download survivors");
+        check_cuda(cudaStreamSynchronize(copy_stream), "download survivors");
+        timings.d2h_bytes += n * (sizeof(long long) + sizeof(int));
+    }
+
+    void deliver(BatchView &out, int which, std::size_t n, float ms, long long first,
+                 long long last, bool complete) {
+        copy_out(which, n);
+        out.first = first;
+        out.last = last;
+        out.a = h_a;
+        out.d = h_d;
+        out.count = n;
+        out.kernel_ms = ms;
+        out.complete = complete;
+    }
+
+    // Queue a batch as pieces: word tiles of at most kMaxTileWords.
+    void queue_pieces(long long first, long long last) {
+        piece_batch_first = first;
+        piece_batch_last = last;
+        for (long long w = 0; w < words; w += dev::kMaxTileWords)
+            pieces.push_back(Piece{first, last, w, std::min(words, w + dev::kMaxTileWords)});
+    }
+
+    // Split a piece into two halves (by parameter, else by word range).
+    void split_front(const Piece &p) {
+        if (p.last > p.first) {
+            const long long mid = p.first + (p.last - p.first) / 2;
+            pieces.push_front(Piece{mid + 1, p.last, p.w_lo, p.w_hi});
+            pieces.push_front(Piece{p.first, mid, p.w_lo, p.w_hi});
+        } else if (p.w_hi - p.w_lo > 1) {
+            const long long mid = p.w_lo + (p.w_hi - p.w_lo) / 2;
+            pieces.push_front(Piece{p.first, p.last, mid, p.w_hi});
+            pieces.push_front(Piece{p.first, p.last, p.w_lo, mid});
+        } else {
+            throw std::logic_error("survivor buffer cannot hold one word of survivors");
+        }
+    }
+
+    // Run pieces one at a time (synchronously) until one fits a buffer.
+    bool next_piece(BatchView &out) {
+        while (!pieces.empty()) {
+            const Piece p = pieces.front();
+            pieces.pop_front();
+            const int which = buf[0].busy ? 1 : 0;
+            if (buf[which].busy) throw std::logic_error("no free survivor buffer");
+            launch(which, p.first, p.last, p.w_lo, p.w_hi);
+            check_cuda(cudaStreamSynchronize(stream), "sieve kernel");
+            buf[which].busy = false;
+            const unsigned long long n = h_count[which];
+            const float ms = elapsed(buf[which]);
+            timings.sieve_ms += ms;
+            if (n > (unsigned long long)capacity) {
+                ++timings.reruns;
+                split_front(p);
+                continue;
+            }
+            deliver(out, which, std::size_t(n), ms, piece_batch_first, piece_batch_last,
+                    pieces.empty());
+            return true;
+        }
+        return false;
+    }
+
+    bool next(BatchView &out) {
+        if (!pieces.empty()) return next_piece(out);
+        if (order.empty() && words > dev::kMaxTileWords && q_next <= q_last) {
+            const long long first = q_next;
+            const long long last = std::min(q_last, first + q_batch - 1);
+            q_next = last + 1;
+            queue_pieces(first, last);
+            return next_piece(out);
+        }
+        refill();
+        if (order.empty()) return false;
+        const int which = order.front();
+        order.pop_front();
+        Buffer &b = buf[which];
+        // The count download is queued right after the kernel on the compute stream.
+        check_cuda(cudaEventSynchronize(b.end), "sieve kernel");
+        check_cuda(cudaStreamWaitEvent(copy_stream, b.end, 0), "cudaStreamWaitEvent");
+        unsigned long long n = 0;
+        check_cuda(cudaMemcpyAsync(&n, b.count, sizeof n, cudaMemcpyDeviceToHost, copy_stream),
+                   "download survivor count");
+        check_cuda(cudaStreamSynchronize(copy_stream), "download survivor count");
+        timings.d2h_bytes += sizeof n;
+        const float ms = elapsed(b);
+        timings.sieve_ms += ms;
+        if (n > (unsigned long long)capacity) {
+            ++timings.reruns;
+            b.busy = false;
+            piece_batch_first = b.first;
+            piece_batch_last = b.last;
+            split_front(Piece{b.first, b.last, 0, words});
+            return next_piece(out);
+        }
+        deliver(out, which, std::size_t(n), ms, b.first, b.last, true);
+        b.busy = false;
+        refill();
+        return true;
+    }
+};
+
+Sieve::Sieve(const std::vector<std::string> &coefficients, long long bound,
+             const SieveOptions &options)
+    : impl_(new Impl) {
+    if (bound < 1) throw std::invalid_argument("numerator bound must be positive");
+    impl_->opt = options;
+    impl_->bound = bound;
+    impl_->words = word_count64(bound);
+    try {
+        impl_->init(coefficients);
+    } catch (...) {
+        impl_->release();
+        throw;
+    }
+}
+
+Sieve::~Sieve() = default;
+
+void Sieve::start(long long first, long long last, long long batch_size) {
+    if (first < 1 || last < first) throw std::invalid_argument("invalid denominator range");
+    if (impl_->opt.square && last > 46340) throw std::invalid_argument("invalid denominator range");
+    if (last > 2147483647LL) throw std::invalid_argument("invalid denominator range");
+    cancel();
+    impl_->q_next = first;
+    impl_->q_last = last;
+    impl_->q_batch = std::max<long long>(1, batch_size);
+}
+
+bool Sieve::next(BatchView &out) { return impl_->next(out); }
+
+void Sieve::cancel() {
+    check_cuda(cudaStreamSynchronize(impl_->stream), "sieve stream");
+    for (auto &b : impl_->buf) b.busy = false;
+    impl_->order.clear();
+    impl_->pieces.clear();
+    impl_->q_next = 0;
+    impl_->q_last = -1;
+}
+
+const SieveTimings &Sieve::timings() const { return impl_->timings; }
+long long Sieve::words64() const { return impl_->words; }
+cudaStream_t Sieve::stream() const { return impl_->stream; }
+
+unsigned long long Sieve::count_only(long long first, long long last, long long batch_size) {
+    if (first < 1 || last < first) throw std::invalid_argument("invalid denominator range");
+    cancel();
+    auto &I = *impl_;
+    // Launches share buffer 0's counter: survivors past capacity are counted,
+    // not stored, so the total is exact while the stores stop early.
+    auto &b = I.buf[0];
+    check_cuda(cudaMemsetAsync(b.count, 0, sizeof(unsigned long long), I.stream), "cudaMemsetAsync");
+    for (long long f = first; f <= last; f += batch_size) {
+        const long long l = std::min(last, f + batch_size - 1);
+        for (long long w = 0; w < I.words; w += dev::kMaxTileWords)
+            I.launch_counting(f, l, w, std::min(I.words, w + dev::kMaxTileWords));
+    }
+    unsigned long long total = 0;
+    check_cuda(cudaMemcpyAsync(&total, b.count, sizeof total, cudaMemcpyDeviceToHost, I.stream),
+               "download survivor count");
+    check_cuda(cudaStreamSynchronize(I.stream), "sieve kernel");
+    return total;
+}
+
+}  // namespace rpg

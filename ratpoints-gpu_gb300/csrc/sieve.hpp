@@ -1,0 +1,89 @@
+// Host driver of the device sieve: builds the per-curve tables on the GPU,
+// launches the sieve over consecutive denominator batches on a CUDA stream,
+// and hands each batch's survivors to the caller while later batches run.
+//
+// It replaces the reference's run_modular_sieve driver (src/sieve.cu:503-580):
+// tables are built once per search instead of once per batch, device buffers
+// are allocated once, survivor copies go through pinned memory, and up to two
+// batches are in flight so host verification overlaps device work.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace rpg {
+
+enum class PlanKind : int { reference = 0, fast = 1 };
+
+class CudaError : public std::runtime_error {
+public:
+    using std::runtime_error::runtime_error;
+};
+
+void check_cuda(cudaError_t status, const char *what);
+
+struct SieveOptions {
+    PlanKind plan = PlanKind::reference;
+    bool square = false;            // parameters k give denominators k*k
+    long long capacity = 1 << 22;   // survivors per device buffer
+    int device = -1;                // -1: current device
+};
+
+// One delivery of survivors.  Pointers stay valid until the next call to
+// Sieve::next().  A batch whose survivors exceed one buffer arrives in several
+// pieces; complete marks its last piece.
+struct BatchView {
+    long long first = 0, last = 0;   // parameter range of the batch
+    const long long *a = nullptr;
+    const int *d = nullptr;
+    std::size_t count = 0;
+    bool complete = true;
+    float kernel_ms = 0.0f;          // event time of the launches behind this piece
+};
+
+struct SieveTimings {
+    float table_ms = 0.0f;           // device table build (events)
+    double table_wall_ms = 0.0;      // host + device table setup
+    double plan_ms = 0.0;            // host plan work
+    double workspace_ms = 0.0;       // allocations
+    double sieve_ms = 0.0;           // sum of sieve launch event times
+    unsigned long long launches = 0;
+    unsigned long long reruns = 0;   // overflowed launches that were split
+    unsigned long long h2d_bytes = 0;
+    unsigned long long d2h_bytes = 0;
+};
+
+class Sieve {
+public:
+    Sieve(const std::vector<std::string> &coefficients, long long bound, const SieveOptions &options);
+    ~Sieve();
+    Sieve(const Sieve &) = delete;
+    Sieve &operator=(const Sieve &) = delete;
+
+    // Queue parameters [first, last] as consecutive batches of batch_size.
+    void start(long long first, long long last, long long batch_size);
+    // Next piece in parameter order; false when every queued batch is delivered.
+    bool next(BatchView &out);
+    // Drop queued and in-flight work (e.g. after a first-point stop).
+    void cancel();
+
+    const SieveTimings &timings() const;
+    long long words64() const;
+
+    // Device-resident pass for benchmarks: sieve [first, last] in batches with
+    // survivors counted on the device only; returns the survivor count.  The
+    // caller times it with the events it records on stream().
+    unsigned long long count_only(long long first, long long last, long long batch_size);
+    cudaStream_t stream() const;
+
+private:
+    struct Impl;
+    std::unique_ptr<Impl> impl_;
+};
+
+}  // namespace rpg

@@ -1,0 +1,71 @@
+// Device-side pieces of the modular square sieve shared by the sieve kernels.
+//
+// Site layout: for a search bound H, the numerators a in [-H, H] of one
+// denominator d form a row of 64-site words; word w holds a = -H + 64 w + j in
+// bit j.  The reference uses 32-site words (src/sieve.cu:179-181); the site set
+// and the survivor set are the same.
+#pragma once
+
+#include <cstdint>
+
+namespace rpg {
+namespace dev {
+
+using u32 = std::uint32_t;
+using u64 = std::uint64_t;
+
+constexpr int kWarpSize = 32;
+constexpr unsigned kFullMask = 0xffffffffu;
+
+// Largest 32-bit quotient estimate used for n mod p with n < 2^31 and p < 2^9:
+// q = (n * ceil(2^40 / p)) >> 40 is exact in that range.
+__host__ __device__ inline u32 magic40(u32 p) {
+    return u32(((u64(1) << 40) + p - 1) / p);
+}
+__device__ __forceinline__ u32 mod_small(u32 n, u32 p, u32 magic) {
+    u32 q = u32((u64(n) * magic) >> 40);
+    return n - q * p;
+}
+
+__device__ __forceinline__ u32 lanemask_lt() {
+    u32 m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Warp-wide emission of surviving sites.  Every lane of the warp calls this
+// with its word index and final mask (0 if none).  One atomicAdd per warp
+// reserves output slots; slots past capacity are counted but not written, so
+// the host sees count > capacity and re-runs the work in smaller pieces.
+__device__ __forceinline__ void emit_survivors(u64 mask, long long word, long long bound,
+                                               int denominator, long long *out_a, int *out_d,
+                                               unsigned long long *out_count,
+                                               unsigned long long capacity) {
+    const int lane = threadIdx.x & 31;
+    u32 n = __popcll(mask);
+    if (!__any_sync(kFullMask, n != 0)) return;
+    u32 incl = n;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        u32 v = __shfl_up_sync(kFullMask, incl, off);
+        if (lane >= off) incl += v;
+    }
+    u32 total = __shfl_sync(kFullMask, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(out_count, (unsigned long long)total);
+    base = __shfl_sync(kFullMask, base, 0);
+    unsigned long long pos = base + incl - n;
+    long long a0 = -bound + 64 * word;
+    while (mask) {
+        int bit = __ffsll((long long)mask) - 1;
+        mask &= mask - 1;
+        if (pos < capacity) {
+            out_a[pos] = a0 + bit;
+            out_d[pos] = denominator;
+        }
+        ++pos;
+    }
+}
+
+}  // namespace dev
+}  // namespace rpg

@@ -1,0 +1,275 @@
+"""ctypes binding of librpgpu (include/ratpoints_gb300.h) for the Python test
+and benchmark harness.  The product is the C++/CUDA library and the
+ratpoints_gpu executable; this module only loads them.
+
+Loading fails loudly (RuntimeError) when the library has not been built: there
+is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+PACKAGE = Path(__file__).resolve().parent
+ROOT = PACKAGE.parent
+LIBRARY = PACKAGE / "lib" / "librpgpu.so"
+EXECUTABLE = PACKAGE / "bin" / "ratpoints_gpu"
+HEADER = ROOT / "include" / "ratpoints_gb300.h"
+
+RPG_SIEVE_SQUARE_DENOMINATORS = 1
+RPG_SIEVE_FAST_PLAN = 2
+RPG_PLAN_REFERENCE = 0
+RPG_PLAN_FAST = 1
+STATUS_NAMES = {0: "RPG_OK", 1: "RPG_E_ARG", 2: "RPG_E_CUDA", 3: "RPG_E_OOM",
+                4: "RPG_E_TIMEOUT", 5: "RPG_E_INTERNAL", 6: "RPG_E_NOT_SQUAREFREE"}
+
+
+class RpgError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+        self.message = message
+
+
+def build(force: bool = False):
+    sys.path.insert(0, str(PACKAGE))
+    try:
+        import build as _build  # noqa: WPS433 - build step beside the sources
+    finally:
+        sys.path.pop(0)
+    return _build.build(force=force)
+
+
+class SieveStats(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_uint64) for name in
+                ("survivor_count", "word_count", "denominator_count", "launches")] + \
+               [(name, ctypes.c_double) for name in
+                ("basis_ms", "sieve_ms", "plan_ms", "workspace_ms", "basis_wall_ms",
+                 "survivor_setup_ms", "verification_ms", "sieve_wall_ms", "initial_mask_bytes")] + \
+               [(name, ctypes.c_uint64) for name in ("h2d_bytes", "d2h_bytes")]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class Interval(ctypes.Structure):
+    _fields_ = [("lower", ctypes.c_char_p), ("upper", ctypes.c_char_p)]
+
+
+class SearchOptions(ctypes.Structure):
+    _fields_ = [("coefficients", ctypes.POINTER(ctypes.c_char_p)),
+                ("coefficient_count", ctypes.c_int32),
+                ("numerator_bound", ctypes.c_int64),
+                ("first", ctypes.c_int32), ("last", ctypes.c_int32),
+                ("intervals", ctypes.POINTER(Interval)), ("interval_count", ctypes.c_int32),
+                ("include_infinity", ctypes.c_int32), ("batch_size", ctypes.c_int32),
+                ("square_denominators", ctypes.c_int32), ("plan", ctypes.c_int32),
+                ("device", ctypes.c_int32), ("verify_threads", ctypes.c_int32)]
+
+
+CANDIDATE_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
+                                ctypes.POINTER(ctypes.c_int32), ctypes.c_size_t, ctypes.c_void_p)
+POINT_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int64, ctypes.c_char_p, ctypes.c_int64,
+                            ctypes.c_void_p)
+
+_lib = None
+
+
+def load():
+    """Load librpgpu.so; raises RuntimeError if it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIBRARY.exists():
+        raise RuntimeError(f"{LIBRARY} is not built; run python ratpoints-gpu_gb300/build.py")
+    lib = ctypes.CDLL(str(LIBRARY))
+    S = ctypes.c_int
+    pp = ctypes.POINTER(ctypes.c_char_p)
+    lib.rpg_sieve_run.restype = S
+    lib.rpg_sieve_run.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                                  ctypes.c_int32, ctypes.c_uint32, ctypes.c_int32, CANDIDATE_CB,
+                                  ctypes.c_void_p, ctypes.POINTER(SieveStats)]
+    lib.rpg_point_search.restype = S
+    lib.rpg_point_search.argtypes = [ctypes.POINTER(SearchOptions), POINT_CB, ctypes.c_void_p,
+                                     ctypes.POINTER(SieveStats)]
+    lib.rpg_is_squarefree.restype = S
+    lib.rpg_is_squarefree.argtypes = [pp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+    lib.rpg_square_root.restype = S
+    lib.rpg_square_root.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
+                                    ctypes.c_char_p, ctypes.c_size_t,
+                                    ctypes.POINTER(ctypes.c_int32)]
+    lib.rpg_cli_main.restype = ctypes.c_int32
+    lib.rpg_cli_main.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_char_p)]
+    lib.rpg_session_create.restype = S
+    lib.rpg_session_create.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.c_uint32,
+                                       ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]
+    lib.rpg_session_count.restype = S
+    lib.rpg_session_count.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                      ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64),
+                                      ctypes.POINTER(ctypes.c_double)]
+    lib.rpg_session_destroy.restype = None
+    lib.rpg_session_destroy.argtypes = [ctypes.c_void_p]
+    lib.rpg_device_count.restype = ctypes.c_int32
+    lib.rpg_abi_version.restype = ctypes.c_int32
+    lib.rpg_last_error.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def _check(status):
+    if status != 0:
+        raise RpgError(status, load().rpg_last_error().decode())
+
+
+def _strings(values):
+    arr = (ctypes.c_char_p * len(values))()
+    for i, v in enumerate(values):
+        arr[i] = str(v).encode()
+    return arr
+
+
+def coefficients_of(text_or_list):
+    if isinstance(text_or_list, str):
+        return text_or_list.split()
+    return [str(c) for c in text_or_list]
+
+
+def declared_functions():
+    """Names of the functions include/ratpoints_gb300.h declares."""
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:[A-Za-z_][\w ]*\*?\s*)\b(rpg_\w+)\s*\(", text, re.M)))
+
+
+def sieve(coefficients, bound, first, last, square=False, plan="reference", device=-1):
+    """Modular survivors as (a, d) int64/int32 arrays plus the stats dict."""
+    lib = load()
+    coeffs = coefficients_of(coefficients)
+    chunks_a, chunks_d = [], []
+
+    @CANDIDATE_CB
+    def on_batch(a, d, n, _user):
+        chunks_a.append(np.ctypeslib.as_array(a, shape=(n,)).copy())
+        chunks_d.append(np.ctypeslib.as_array(d, shape=(n,)).copy())
+        return 0
+
+    flags = (RPG_SIEVE_SQUARE_DENOMINATORS if square else 0) | \
+            (RPG_SIEVE_FAST_PLAN if plan == "fast" else 0)
+    stats = SieveStats()
+    _check(lib.rpg_sieve_run(_strings(coeffs), len(coeffs), int(bound), int(first), int(last),
+                             flags, device, on_batch, None, ctypes.byref(stats)))
+    a = np.concatenate(chunks_a) if chunks_a else np.zeros(0, np.int64)
+    d = np.concatenate(chunks_d) if chunks_d else np.zeros(0, np.int32)
+    return a, d, stats.as_dict()
+
+
+def point_search(coefficients, bound, first, last, intervals=(), include_infinity=True,
+                 batch_size=1 << 16, square=False, plan="fast", device=-1, verify_threads=0,
+                 stop_after=None):
+    """Verified points [(a, y, d)] in output order, plus the stats dict."""
+    lib = load()
+    coeffs = coefficients_of(coefficients)
+    points = []
+
+    @POINT_CB
+    def on_point(a, y, d, _user):
+        points.append((a, int(y.decode()), d))
+        return 0 if stop_after is not None and len(points) >= stop_after else 1
+
+    ivs = (Interval * max(1, len(intervals)))()
+    for i, (lo, hi) in enumerate(intervals):
+        ivs[i].lower = None if lo is None else str(lo).encode()
+        ivs[i].upper = None if hi is None else str(hi).encode()
+    opts = SearchOptions()
+    cstr = _strings(coeffs)
+    opts.coefficients = cstr
+    opts.coefficient_count = len(coeffs)
+    opts.numerator_bound = int(bound)
+    opts.first, opts.last = int(first), int(last)
+    opts.intervals = ivs
+    opts.interval_count = len(intervals)
+    opts.include_infinity = int(include_infinity)
+    opts.batch_size = int(batch_size)
+    opts.square_denominators = int(square)
+    opts.plan = RPG_PLAN_FAST if plan == "fast" else RPG_PLAN_REFERENCE
+    opts.device = device
+    opts.verify_threads = verify_threads
+    stats = SieveStats()
+    _check(lib.rpg_point_search(ctypes.byref(opts), on_point, None, ctypes.byref(stats)))
+    return points, stats.as_dict()
+
+
+def is_squarefree(coefficients):
+    coeffs = coefficients_of(coefficients)
+    out = ctypes.c_int32(-1)
+    _check(load().rpg_is_squarefree(_strings(coeffs), len(coeffs), ctypes.byref(out)))
+    return bool(out.value)
+
+
+def square_root(coefficients, a, b):
+    coeffs = coefficients_of(coefficients)
+    buf = ctypes.create_string_buffer(1 << 16)
+    flag = ctypes.c_int32(-1)
+    _check(load().rpg_square_root(_strings(coeffs), len(coeffs), int(a), int(b), buf,
+                                  len(buf), ctypes.byref(flag)))
+    return int(buf.value.decode()) if flag.value else None
+
+
+class Session:
+    """Device-resident tables; count() runs an event-timed counting pass."""
+
+    def __init__(self, coefficients, bound, square=False, plan="reference", device=-1):
+        lib = load()
+        coeffs = coefficients_of(coefficients)
+        flags = (RPG_SIEVE_SQUARE_DENOMINATORS if square else 0) | \
+                (RPG_SIEVE_FAST_PLAN if plan == "fast" else 0)
+        handle = ctypes.c_void_p()
+        _check(lib.rpg_session_create(_strings(coeffs), len(coeffs), int(bound), flags, device,
+                                      ctypes.byref(handle)))
+        self._handle = handle
+
+    def count(self, first, last, batch_size=1 << 16):
+        n = ctypes.c_uint64(0)
+        ms = ctypes.c_double(0)
+        _check(load().rpg_session_count(self._handle, int(first), int(last), int(batch_size),
+                                        ctypes.byref(n), ctypes.byref(ms)))
+        return n.value, ms.value
+
+    def close(self):
+        if self._handle:
+            load().rpg_session_destroy(self._handle)
+            self._handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def cli(args, env=None, timeout=600, check=False):
+    """Run the ratpoints_gpu executable; returns subprocess.CompletedProcess (bytes)."""
+    if not EXECUTABLE.exists():
+        raise RuntimeError(f"{EXECUTABLE} is not built; run python ratpoints-gpu_gb300/build.py")
+    merged = dict(os.environ)
+    merged.pop("RATPOINTS_GPU_BENCHMARK", None)
+    merged.update(env or {})
+    return subprocess.run([str(EXECUTABLE), *map(str, args)], capture_output=True,
+                          timeout=timeout, env=merged, check=check)
+
+
+def parse_metrics(stderr: bytes):
+    """Key=value fields of the -v metrics line."""
+    text = stderr.decode(errors="replace")
+    line = re.search(r"^wall_ms=.*$", text, re.M)
+    if not line:
+        return None
+    return {k: float(v) if "." in v else int(v)
+            for k, v in re.findall(r"([a-z_]+)=([0-9.]+)", line.group())}
