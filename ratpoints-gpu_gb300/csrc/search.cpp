@@ -83,8 +83,9 @@ void require_cuda(cudaError_t status, const char *operation) {
 bool SearchOptions::accepts(long long numerator, long long denominator) const {
     if (intervals.empty()) return true;
     for (const auto &iv : intervals) {
-        bool above = iv.lower_infinite || iv.lower.compare_fraction(numerator, denominator) <= 0;
-        bool below = iv.upper_infinite || iv.upper.compare_fraction(numerator, denominator) >= 0;
+        // compare_fraction gives sign(numerator/denominator - bound)
+        bool above = iv.lower_infinite || iv.lower.compare_fraction(numerator, denominator) >= 0;
+        bool below = iv.upper_infinite || iv.upper.compare_fraction(numerator, denominator) <= 0;
         if (above && below) return true;
     }
     return false;

@@ -16,7 +16,8 @@ INT_MAX = 2**31 - 1
 
 
 def pairs(a, d):
-    return sorted(zip(a.tolist(), d.tolist()))
+    """(a, d) pairs in the oracle's order: d ascending, then a."""
+    return sorted(zip(a.tolist(), d.tolist()), key=lambda t: (t[1], t[0]))
 
 
 def assert_same_set(rpg, oracle, coeffs, bound, first, last, square=False, plan="reference"):
