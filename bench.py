@@ -143,6 +143,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        return False
+
+
 def flush_l2(torch, buf, step):
     buf.fill_(step & 0xFF)
     torch.cuda.synchronize()
@@ -205,9 +213,10 @@ def main():
     parser.add_argument("--steps", type=int, default=5)
     parser.add_argument("--warmup", type=int, default=3)
     parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    parser.add_argument("--plan", choices=["reference", "fast"], default="reference")
+    parser.add_argument("--plan", choices=["reference", "fast"], default="fast")
+    parser.add_argument("--reference-plan-steps", type=int, default=2)
     parser.add_argument("--denominators", type=int, default=DENOMINATORS)
-    parser.add_argument("--e2e-steps", type=int, default=1)
+    parser.add_argument("--e2e-steps", type=int, default=1, choices=range(1, 100), metavar="N")
     parser.add_argument("--cpu-seconds", type=float, default=12.0)
     parser.add_argument("--no-cpu-baseline", action="store_true")
     args = parser.parse_args()
@@ -234,32 +243,44 @@ def main():
     last = args.denominators
     # weak scaling: rank r sieves its own block of `last` denominators
     first_b, last_b = rank * last + 1, (rank + 1) * last
-    session = rpg.Session(coeffs, HEIGHT, plan=args.plan, device=local)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
-    for step in range(args.warmup):
-        flush_l2(torch, flush, step)
-        session.count(first_b, last_b, BATCH)
-    times, counts = [], []
-    with ClockSampler(local) as clocks:
-        for step in range(args.steps):
+
+    def measure(plan, steps, warmup, sampler=None):
+        session = rpg.Session(coeffs, HEIGHT, plan=plan, device=local)
+        for step in range(warmup):
             flush_l2(torch, flush, step)
-            if dist:
-                dist.barrier()
-            n, ms = session.count(first_b, last_b, BATCH)
-            times.append(ms)
-            counts.append(n)
+            session.count(first_b, last_b, BATCH)
+        times, counts = [], []
+        ctx = sampler if sampler is not None else _Null()
+        with ctx:
+            for step in range(steps):
+                flush_l2(torch, flush, step)
+                if dist:
+                    dist.barrier()
+                n, ms = session.count(first_b, last_b, BATCH)
+                times.append(ms)
+                counts.append(n)
+        assert len(set(counts)) == 1, "survivor count changed between steps"
+        words, per_word = session.work(first_b, last_b)
+        session.close()
+        step_ms = sum(times) / len(times)
+        if dist:
+            t = torch.tensor([step_ms], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            step_ms = float(t.item())
+        return {"ms": step_ms, "survivors": counts[0], "words": words, "bytes_per_word": per_word}
+
+    clocks = ClockSampler(local)
+    fast = measure(args.plan, args.steps, args.warmup, clocks)
     clock = clocks.summary()
-    assert len(set(counts)) == 1, "survivor count changed between steps"
-    step_ms = sum(times) / len(times)
-    if dist:
-        t = torch.tensor([step_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms = float(t.item())
-    session.close()
+    ref = None
+    if args.plan != "reference" and args.reference_plan_steps > 0:
+        ref = measure("reference", args.reference_plan_steps, 1)
 
     mu = mobius(last)
     reduced = reduced_sites(HEIGHT, last, mu)
     rect = (2 * HEIGHT + 1) * last
+    step_ms = fast["ms"]
     value = reduced * world / (step_ms / 1e3) / 1e9
     launches_per_step = (last + BATCH - 1) // BATCH
 
@@ -274,10 +295,8 @@ def main():
     if rank != 0:
         return
     sm_hz = (clock.get("sm_mhz") or 1965.0) * 1e6
-    fast_primes = REF_FAST_PRIMES
-    bytes_per_launch = (2 * HEIGHT + 1) * BATCH * fast_primes * 8 / 64
-    launch_ms = step_ms / launches_per_step
-    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
+    total_bytes = fast["words"] * fast["bytes_per_word"]
+    achieved = total_bytes / (step_ms / 1e3) / 1e9
     peak = SMS * SMEM_BYTES_PER_CLK * sm_hz / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -288,14 +307,15 @@ def main():
         "config": {**workload_config(), "denominators": last, "rectangle_sites": rect,
                    "reduced_sites": reduced, "plan": args.plan,
                    "rectangle_gsites_per_s": rect * world / (step_ms / 1e3) / 1e9,
-                   "modular_survivors": counts[0]},
+                   "modular_survivors": fast["survivors"],
+                   "words_swept_per_step": fast["words"]},
         "roofline": {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
-                     "algorithmic": f"{fast_primes} shared-memory primes x 8 B per 64 sites "
-                                    f"= {fast_primes / 8:.3f} B/site x {(2 * HEIGHT + 1) * BATCH} "
-                                    f"sites per launch",
-                     "peak_source": "152 SMs x 128 B/clk (LDS.64, measured) x median SM clock "
-                                    "sampled in the timed region"},
+                     "algorithmic": f"{fast['bytes_per_word']} B of stage-1 shared-memory rows per "
+                                    f"swept 64-site word x {fast['words']} words per step "
+                                    f"/ {launches_per_step} launches",
+                     "peak_source": "152 SMs x 128 B/clk (LDS.64 lane-contiguous, measured on "
+                                    "GB300) x median SM clock sampled in the timed region"},
         "e2e": {"value": reduced * world / e2e_s / 1e9, "unit": UNIT,
                 "seconds": e2e_s, "points": len(points),
                 "h2d_bytes_per_step": int(e2e_stats.get("h2d_bytes", 0)) if e2e_stats else 0,
@@ -303,6 +323,12 @@ def main():
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clock,
     }
+    if ref is not None:
+        line["reference_plan"] = {
+            "value": reduced * world / (ref["ms"] / 1e3) / 1e9, "unit": UNIT,
+            "ms_per_step": ref["ms"], "modular_survivors": ref["survivors"],
+            "note": "same kernel family with the reference's 32-prime plan: survivor set "
+                    "identical to the reference implementation's"}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(coeffs, seconds=args.cpu_seconds)
     print(json.dumps(line))

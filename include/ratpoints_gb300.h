@@ -146,6 +146,11 @@ rpg_status rpg_session_create(const char *const *coefficients, int32_t coefficie
                               rpg_session **session);
 rpg_status rpg_session_count(rpg_session *session, int32_t first, int32_t last,
                              int32_t batch_size, uint64_t *survivors, double *device_ms);
+/* Work a pass over parameters [first, last] does: 64-site words the sieve
+ * kernel sweeps (admissible classes only under the fast plan) and the
+ * shared-memory bytes its first stage reads per swept word. */
+rpg_status rpg_session_work(rpg_session *session, int32_t first, int32_t last,
+                            uint64_t *words_swept, uint32_t *smem_bytes_per_word);
 void rpg_session_destroy(rpg_session *session);
 
 int32_t rpg_device_count(void);

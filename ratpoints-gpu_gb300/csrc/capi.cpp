@@ -278,6 +278,16 @@ rpg_status rpg_session_count(rpg_session *session, int32_t first, int32_t last, 
     });
 }
 
+rpg_status rpg_session_work(rpg_session *session, int32_t first, int32_t last,
+                            uint64_t *words_swept, uint32_t *smem_bytes_per_word) {
+    return guarded([&]() -> rpg_status {
+        if (!session) return fail(RPG_E_ARG, "session must not be NULL");
+        if (words_swept) *words_swept = session->sieve->swept_words(first, last);
+        if (smem_bytes_per_word) *smem_bytes_per_word = session->sieve->smem_bytes_per_word();
+        return RPG_OK;
+    });
+}
+
 void rpg_session_destroy(rpg_session *session) { delete session; }
 
 int32_t rpg_device_count(void) {

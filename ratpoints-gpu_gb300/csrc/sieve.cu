@@ -25,6 +25,7 @@
 
 #include "plan.hpp"
 #include "sieve_device.cuh"
+#include "sieve_fast.cuh"
 
 namespace rpg {
 
@@ -56,20 +57,6 @@ struct RefTables {
     int length[kCandidatePrimes];         // words per row (p + kExt rounded up to even)
     int prime[kCandidatePrimes];
     u32 magic[kCandidatePrimes];
-};
-
-struct SieveArgs {
-    long long bound;     // H
-    long long words;     // 64-site words per denominator row
-    long long w_lo;      // word range of this launch
-    long long w_hi;
-    long long k_first;   // first parameter
-    int k_count;
-    int square;
-    long long *out_a;
-    int *out_d;
-    unsigned long long *out_count;
-    unsigned long long capacity;
 };
 
 __global__ void ref_table_kernel(u64 *rows, RefTables T, const unsigned char *affine,
@@ -257,13 +244,20 @@ struct Sieve::Impl {
     cudaStream_t stream = nullptr, copy_stream = nullptr;
     dev::RefTables T{};
     dev::u64 *rows = nullptr;
+    // fast plan
+    dev::FastTables F{};
+    dev::u64 *fast_rows = nullptr;
+    dev::u64 *fast_adm = nullptr;
+    std::size_t fast_smem = 0;
+    std::vector<dev::u64> fast_adm_host;
+    long long max_tile = dev::kMaxTileWords;
     long long capacity = 0;
     SieveTimings timings;
 
     struct Buffer {
         long long *a = nullptr;
         int *d = nullptr;
-        unsigned long long *count = nullptr;
+        unsigned long long *count = nullptr;  // [0] survivors, [1] work counter
         cudaEvent_t begin = nullptr, end = nullptr;
         long long first = 0, last = 0;
         bool busy = false;
@@ -297,6 +291,10 @@ struct Sieve::Impl {
         }
         cudaFree(rows);
         rows = nullptr;
+        cudaFree(fast_rows);
+        fast_rows = nullptr;
+        cudaFree(fast_adm);
+        fast_adm = nullptr;
         if (h_count) cudaFreeHost(h_count);
         if (h_a) cudaFreeHost(h_a);
         if (h_d) cudaFreeHost(h_d);
@@ -396,7 +394,7 @@ struct Sieve::Impl {
         for (auto &b : buf) {
             b.a = device_alloc<long long>(std::size_t(capacity), "cudaMalloc(survivors)");
             b.d = device_alloc<int>(std::size_t(capacity), "cudaMalloc(survivors)");
-            b.count = device_alloc<unsigned long long>(1, "cudaMalloc(count)");
+            b.count = device_alloc<unsigned long long>(2, "cudaMalloc(count)");
             check_cuda(cudaEventCreate(&b.begin), "cudaEventCreate");
             check_cuda(cudaEventCreate(&b.end), "cudaEventCreate");
         }
@@ -404,7 +402,173 @@ struct Sieve::Impl {
         check_cuda(cudaMallocHost(&h_a, std::size_t(capacity) * sizeof(long long)), "cudaMallocHost");
         check_cuda(cudaMallocHost(&h_d, std::size_t(capacity) * sizeof(int)), "cudaMallocHost");
         timings.workspace_ms += ms_since(t0);
-        build_tables(coefficients);
+        if (opt.plan == PlanKind::fast) build_fast_tables(coefficients);
+        else build_tables(coefficients);
+    }
+
+    // Fast plan: class-layout tables for the stage-1 composite moduli and the
+    // 36 reference candidates, and the 2-adic admissible-class table.
+    void build_fast_tables(const std::vector<std::string> &coefficients) {
+        auto t0 = Clock::now();
+        // Stage-1 moduli: products of small odd primes (3*5*7, 11*13, 17*19, 23*29, 31*37).
+        static const int kFactors[dev::kFastSlots][dev::kFastMaxFactors + 1] = {
+            {3, 3, 5, 7}, {2, 11, 13, 0}, {2, 17, 19, 0}, {2, 23, 29, 0}, {2, 31, 37, 0}};
+        const int n = int(coefficients.size()) - 1;
+        std::vector<int> primes_used;
+        for (const auto &f : kFactors)
+            for (int i = 1; i <= f[0]; ++i) primes_used.push_back(f[i]);
+        for (int p : candidate_primes()) primes_used.push_back(p);
+        std::vector<unsigned char> affine;
+        std::vector<unsigned short> inverse;
+        std::vector<int> base(kMaximumPrime, -1), lead(kMaximumPrime, 1);
+        for (int q : primes_used) {
+            if (base[q] >= 0) continue;
+            base[q] = int(affine.size());
+            auto aff = affine_mask(q, coefficients);
+            affine.insert(affine.end(), aff.begin(), aff.end());
+            inverse.push_back(0);
+            for (int v = 1; v < q; ++v) inverse.push_back((unsigned short)mod_inverse(v, q));
+            if (n % 2 == 0) {
+                const int lc = decimal_mod(coefficients.back(), q);
+                bool square = false;
+                for (int v = 0; v < q && !square; ++v) square = (v * v) % q == lc;
+                lead[q] = square ? 1 : 0;
+            }
+        }
+        std::vector<dev::TableSpec> specs;
+        long long total = 0;
+        int smem_words = 0;
+        F.slots = dev::kFastSlots;
+        for (int sl = 0; sl < dev::kFastSlots; ++sl) {
+            dev::TableSpec S{};
+            S.nf = kFactors[sl][0];
+            S.m = 1;
+            for (int i = 0; i < S.nf; ++i) {
+                S.q[i] = kFactors[sl][i + 1];
+                S.m *= S.q[i];
+                S.factor_base[i] = base[S.q[i]];
+                S.lead_ok[i] = lead[S.q[i]];
+            }
+            S.length = (S.m + dev::kFExt + 1) & ~1;
+            S.offset = total;
+            total += (long long)S.m * S.length;
+            specs.push_back(S);
+            dev::FastModulus &M = F.mod[sl];
+            M.m = S.m;
+            M.nf = S.nf;
+            for (int i = 0; i < S.nf; ++i) M.q[i] = S.q[i];
+            M.length = S.length;
+            M.offset = S.offset;
+            M.smem_offset = smem_words;
+            smem_words += S.length;
+            M.inv4096 = dev::u32(mod_inverse(4096 % S.m, S.m));
+            M.neg_h = dev::u32((S.m - bound % S.m) % S.m);
+            M.wlo_mod = 0;
+            M.magic = (unsigned long long)((~0ull) / (unsigned long long)S.m) + 1;
+        }
+        F.smem_words = smem_words;
+        const auto &cands = candidate_primes();
+        for (int i = 0; i < kCandidatePrimes; ++i) {
+            const int p = cands[i];
+            dev::TableSpec S{};
+            S.nf = 1;
+            S.m = p;
+            S.q[0] = p;
+            S.factor_base[0] = base[p];
+            S.lead_ok[0] = 0;
+            S.length = p;
+            S.offset = total;
+            total += (long long)p * p;
+            specs.push_back(S);
+            dev::FastPrime &P = F.prime[i];
+            P.offset = S.offset;
+            P.p = p;
+            P.inv4096 = dev::u32(mod_inverse(4096 % p, p));
+            P.neg_h = dev::u32((p - bound % p) % p);
+            P.magic = dev::magic40(dev::u32(p));
+            P.wlo_mod = 0;
+        }
+        F.h_mod64 = int(bound % 64);
+        // 2-adic admissibility: class r for d (mod 64) iff F(r, d) is a square
+        // mod 64 and r is odd when d is even.
+        std::vector<int> c64(coefficients.size());
+        for (std::size_t i = 0; i < coefficients.size(); ++i) c64[i] = decimal_mod(coefficients[i], 64);
+        bool square64[64] = {};
+        for (int v = 0; v < 64; ++v) square64[(v * v) & 63] = true;
+        std::vector<dev::u64> adm(64, 0);
+        for (int dd = 0; dd < 64; ++dd) {
+            for (int r = 0; r < 64; ++r) {
+                if (dd % 2 == 0 && r % 2 == 0) continue;
+                int value = c64[n], power = 1;
+                for (int i = n - 1; i >= 0; --i) {
+                    value = (value * r) & 63;
+                    power = (power * dd) & 63;
+                    value = (value + c64[i] * power) & 63;
+                }
+                if (n % 2 == 1) value = (value * dd) & 63;
+                if (square64[value]) adm[dd] |= dev::u64(1) << r;
+            }
+        }
+        fast_adm_host = adm;
+        timings.plan_ms += ms_since(t0);
+        auto t1 = Clock::now();
+        fast_rows = device_alloc<dev::u64>(std::size_t(total), "cudaMalloc(class tables)");
+        fast_adm = device_alloc<dev::u64>(64, "cudaMalloc(admissible classes)");
+        unsigned char *d_aff = device_alloc<unsigned char>(affine.size(), "cudaMalloc(affine)");
+        unsigned short *d_inv = device_alloc<unsigned short>(inverse.size(), "cudaMalloc(inverse)");
+        dev::TableSpec *d_specs = device_alloc<dev::TableSpec>(specs.size(), "cudaMalloc(specs)");
+        timings.workspace_ms += ms_since(t1);
+        cudaEvent_t e0, e1;
+        check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
+        check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
+        check_cuda(cudaEventRecord(e0, stream), "cudaEventRecord");
+        check_cuda(cudaMemcpyAsync(d_aff, affine.data(), affine.size(), cudaMemcpyHostToDevice, stream),
+                   "upload affine tables");
+        check_cuda(cudaMemcpyAsync(d_inv, inverse.data(), inverse.size() * sizeof(unsigned short),
+                                   cudaMemcpyHostToDevice, stream),
+                   "upload inverses");
+        check_cuda(cudaMemcpyAsync(d_specs, specs.data(), specs.size() * sizeof(dev::TableSpec),
+                                   cudaMemcpyHostToDevice, stream),
+                   "upload table specs");
+        check_cuda(cudaMemcpyAsync(fast_adm, adm.data(), 64 * sizeof(dev::u64), cudaMemcpyHostToDevice,
+                                   stream),
+                   "upload admissible classes");
+        timings.h2d_bytes += affine.size() + inverse.size() * sizeof(unsigned short) +
+                             specs.size() * sizeof(dev::TableSpec) + 64 * sizeof(dev::u64);
+        const int threads = 256;
+        const long long blocks = (total + threads - 1) / threads;
+        dev::class_table_kernel<<<unsigned(blocks), threads, 0, stream>>>(
+            fast_rows, d_specs, int(specs.size()), d_aff, d_inv, total);
+        check_cuda(cudaGetLastError(), "class_table_kernel launch");
+        check_cuda(cudaEventRecord(e1, stream), "cudaEventRecord");
+        check_cuda(cudaEventSynchronize(e1), "class table build");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        timings.table_ms += ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(d_aff);
+        cudaFree(d_inv);
+        cudaFree(d_specs);
+        F.rows = fast_rows;
+        F.prime_rows = fast_rows;
+        F.admissible = fast_adm;
+        fast_smem = std::size_t(F.smem_words) * 8 + std::size_t(dev::kFWarps) * dev::kFQueue * 12;
+        check_cuda(cudaFuncSetAttribute(dev::fast_sieve_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(fast_smem)),
+                   "cudaFuncSetAttribute");
+        int sms = 0, per_sm = 0;
+        check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device),
+                   "cudaDeviceGetAttribute");
+        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::fast_sieve_kernel,
+                                                                 dev::kFThreads, fast_smem),
+                   "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        grid = std::max(1, sms * std::max(1, per_sm));
+        // Word dimension of a launch: class words (64 sites spaced 64 apart).
+        const long long sites = 2 * bound + 1;
+        words = (sites / 64 + 1 + 63) / 64;
+        max_tile = dev::kFMaxClassWords;
+        timings.table_wall_ms += ms_since(t0);
     }
 
     dev::SieveArgs args(int which, long long first, long long last, long long w_lo, long long w_hi) {
@@ -423,12 +587,28 @@ struct Sieve::Impl {
         return A;
     }
 
+    // Counting pass: survivors accumulate in buffer 0's counter across launches.
     void launch_counting(long long first, long long last, long long w_lo, long long w_hi) {
         const dev::SieveArgs A = args(0, first, last, w_lo, w_hi);
-        const int blocks = int(std::min<long long>(grid, A.k_count));
-        dev::ref_sieve_kernel<<<blocks, dev::kThreads, dev::kRefSmem, stream>>>(T, A);
-        check_cuda(cudaGetLastError(), "sieve kernel launch");
+        check_cuda(cudaMemsetAsync(buf[0].count + 1, 0, sizeof(unsigned long long), stream),
+                   "cudaMemsetAsync");
+        launch_kernel(A, buf[0].count + 1);
         ++timings.launches;
+    }
+
+    void launch_kernel(const dev::SieveArgs &A, unsigned long long *work) {
+        if (opt.plan == PlanKind::fast) {
+            dev::FastTables Fl = F;
+            for (int i = 0; i < kCandidatePrimes; ++i)
+                Fl.prime[i].wlo_mod = dev::u32(A.w_lo % Fl.prime[i].p);
+            for (int i = 0; i < Fl.slots; ++i) Fl.mod[i].wlo_mod = dev::u32(A.w_lo % Fl.mod[i].m);
+            const int blocks = int(std::min<long long>(grid, (A.k_count + dev::kFFetch - 1) / dev::kFFetch));
+            dev::fast_sieve_kernel<<<blocks, dev::kFThreads, fast_smem, stream>>>(Fl, A, work);
+        } else {
+            const int blocks = int(std::min<long long>(grid, A.k_count));
+            dev::ref_sieve_kernel<<<blocks, dev::kThreads, dev::kRefSmem, stream>>>(T, A);
+        }
+        check_cuda(cudaGetLastError(), "sieve kernel launch");
     }
 
     void launch(int which, long long first, long long last, long long w_lo, long long w_hi) {
@@ -437,11 +617,10 @@ struct Sieve::Impl {
         b.last = last;
         b.busy = true;
         const dev::SieveArgs A = args(which, first, last, w_lo, w_hi);
-        check_cuda(cudaMemsetAsync(b.count, 0, sizeof(unsigned long long), stream), "cudaMemsetAsync");
+        check_cuda(cudaMemsetAsync(b.count, 0, 2 * sizeof(unsigned long long), stream),
+                   "cudaMemsetAsync");
         check_cuda(cudaEventRecord(b.begin, stream), "cudaEventRecord");
-        const int blocks = int(std::min<long long>(grid, A.k_count));
-        dev::ref_sieve_kernel<<<blocks, dev::kThreads, dev::kRefSmem, stream>>>(T, A);
-        check_cuda(cudaGetLastError(), "sieve kernel launch");
+        launch_kernel(A, b.count + 1);
         check_cuda(cudaEventRecord(b.end, stream), "cudaEventRecord");
         check_cuda(cudaMemcpyAsync(h_count + which, b.count, sizeof(unsigned long long),
                                    cudaMemcpyDeviceToHost, stream),
@@ -453,7 +632,7 @@ struct Sieve::Impl {
     // Launch queued batches into free buffers (pipelined path, rows that fit
     // one launch).  Rows longer than kMaxTileWords go through pieces instead.
     void refill() {
-        if (words > dev::kMaxTileWords || !pieces.empty()) return;
+        if (words > max_tile || !pieces.empty()) return;
         while (order.size() < 2 && q_next <= q_last) {
             const int which = buf[0].busy ? 1 : 0;
             if (buf[which].busy) break;
@@ -500,8 +679,8 @@ struct Sieve::Impl {
     void queue_pieces(long long first, long long last) {
         piece_batch_first = first;
         piece_batch_last = last;
-        for (long long w = 0; w < words; w += dev::kMaxTileWords)
-            pieces.push_back(Piece{first, last, w, std::min(words, w + dev::kMaxTileWords)});
+        for (long long w = 0; w < words; w += max_tile)
+            pieces.push_back(Piece{first, last, w, std::min(words, w + max_tile)});
     }
 
     // Split a piece into two halves (by parameter, else by word range).
@@ -546,7 +725,7 @@ struct Sieve::Impl {
 
     bool next(BatchView &out) {
         if (!pieces.empty()) return next_piece(out);
-        if (order.empty() && words > dev::kMaxTileWords && q_next <= q_last) {
+        if (order.empty() && words > max_tile && q_next <= q_last) {
             const long long first = q_next;
             const long long last = std::min(q_last, first + q_batch - 1);
             q_next = last + 1;
@@ -622,6 +801,40 @@ void Sieve::cancel() {
 }
 
 const SieveTimings &Sieve::timings() const { return impl_->timings; }
+
+unsigned long long Sieve::swept_words(long long first, long long last) const {
+    const auto &I = *impl_;
+    if (last < first) return 0;
+    if (I.opt.plan != PlanKind::fast) return (unsigned long long)(last - first + 1) * I.words;
+    // Denominators per residue mod 64, then the words of each admissible class.
+    unsigned long long per_residue[64] = {};
+    for (int t = 0; t < 64; ++t) {
+        // parameters k in [first, last] with k = t (mod 64)
+        long long lo = first + ((t - first % 64) % 64 + 64) % 64;
+        unsigned long long n = lo > last ? 0 : (unsigned long long)((last - lo) / 64 + 1);
+        const int dres = I.opt.square ? int((long long)t * t % 64) : t;
+        per_residue[dres] += n;
+    }
+    const long long sites = 2 * I.bound + 1;
+    unsigned long long total = 0;
+    for (int dres = 0; dres < 64; ++dres) {
+        if (!per_residue[dres]) continue;
+        unsigned long long words = 0;
+        for (int r = 0; r < 64; ++r) {
+            if (!((I.fast_adm_host[dres] >> r) & 1)) continue;
+            const long long ofs = (r + I.bound % 64) % 64;
+            const long long count = ofs < sites ? (sites - 1 - ofs) / 64 + 1 : 0;
+            words += (unsigned long long)((count + 63) / 64);
+        }
+        total += per_residue[dres] * words;
+    }
+    return total;
+}
+
+unsigned Sieve::smem_bytes_per_word() const {
+    return impl_->opt.plan == PlanKind::fast ? unsigned(8 * impl_->F.slots)
+                                             : unsigned(8 * dev::kRefFast);
+}
 long long Sieve::words64() const { return impl_->words; }
 cudaStream_t Sieve::stream() const { return impl_->stream; }
 
@@ -635,8 +848,8 @@ unsigned long long Sieve::count_only(long long first, long long last, long long 
     check_cuda(cudaMemsetAsync(b.count, 0, sizeof(unsigned long long), I.stream), "cudaMemsetAsync");
     for (long long f = first; f <= last; f += batch_size) {
         const long long l = std::min(last, f + batch_size - 1);
-        for (long long w = 0; w < I.words; w += dev::kMaxTileWords)
-            I.launch_counting(f, l, w, std::min(I.words, w + dev::kMaxTileWords));
+        for (long long w = 0; w < I.words; w += I.max_tile)
+            I.launch_counting(f, l, w, std::min(I.words, w + I.max_tile));
     }
     unsigned long long total = 0;
     check_cuda(cudaMemcpyAsync(&total, b.count, sizeof total, cudaMemcpyDeviceToHost, I.stream),

@@ -81,6 +81,11 @@ public:
     unsigned long long count_only(long long first, long long last, long long batch_size);
     cudaStream_t stream() const;
 
+    // Work of a pass over parameters [first, last]: 64-site words swept by the
+    // sieve kernel and shared-memory bytes read per swept word (stage 1).
+    unsigned long long swept_words(long long first, long long last) const;
+    unsigned smem_bytes_per_word() const;
+
 private:
     struct Impl;
     std::unique_ptr<Impl> impl_;

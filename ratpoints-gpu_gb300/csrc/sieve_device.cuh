@@ -17,6 +17,23 @@ using u64 = std::uint64_t;
 constexpr int kWarpSize = 32;
 constexpr unsigned kFullMask = 0xffffffffu;
 
+// Arguments of one sieve launch: parameters k_first .. k_first + k_count - 1
+// (denominators k, or k*k when square), word range [w_lo, w_hi) of each row,
+// and the survivor output (structure of arrays, capacity entries).
+struct SieveArgs {
+    long long bound;     // H
+    long long words;     // words per denominator row (64-site words)
+    long long w_lo;
+    long long w_hi;
+    long long k_first;
+    int k_count;
+    int square;
+    long long *out_a;
+    int *out_d;
+    unsigned long long *out_count;
+    unsigned long long capacity;
+};
+
 // Largest 32-bit quotient estimate used for n mod p with n < 2^31 and p < 2^9:
 // q = (n * ceil(2^40 / p)) >> 40 is exact in that range.
 __host__ __device__ inline u32 magic40(u32 p) {

@@ -114,6 +114,10 @@ def load():
     lib.rpg_session_count.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                       ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64),
                                       ctypes.POINTER(ctypes.c_double)]
+    lib.rpg_session_work.restype = S
+    lib.rpg_session_work.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                     ctypes.POINTER(ctypes.c_uint64),
+                                     ctypes.POINTER(ctypes.c_uint32)]
     lib.rpg_session_destroy.restype = None
     lib.rpg_session_destroy.argtypes = [ctypes.c_void_p]
     lib.rpg_device_count.restype = ctypes.c_int32
@@ -241,6 +245,14 @@ class Session:
         _check(load().rpg_session_count(self._handle, int(first), int(last), int(batch_size),
                                         ctypes.byref(n), ctypes.byref(ms)))
         return n.value, ms.value
+
+    def work(self, first, last):
+        """(64-site words swept, shared-memory bytes per swept word) of a pass."""
+        words = ctypes.c_uint64(0)
+        per = ctypes.c_uint32(0)
+        _check(load().rpg_session_work(self._handle, int(first), int(last), ctypes.byref(words),
+                                       ctypes.byref(per)))
+        return words.value, per.value
 
     def close(self):
         if self._handle:
