@@ -153,6 +153,29 @@ rpg_status rpg_session_work(rpg_session *session, int32_t first, int32_t last,
                             uint64_t *words_swept, uint32_t *smem_bytes_per_word);
 void rpg_session_destroy(rpg_session *session);
 
+/*
+ * Sieve [first, last] with the session's resident tables without allocating
+ * any memory.  No counterpart in the reference; it exists for callers that
+ * cannot allocate when they sieve: code running under CUDA graph capture,
+ * engines that own their device memory through their own pool, host
+ * callbacks that must not enter the allocator.
+ *
+ * Survivors go to the caller's device arrays (capacity entries each); the
+ * caller's *device_count receives the total, which exceeds capacity when the
+ * arrays were too small (entries past capacity are not written).  Work is
+ * enqueued on `stream` (a cudaStream_t, NULL for the legacy default stream)
+ * and the call returns without waiting; read the count after synchronizing.
+ * At most 16,777,216 denominators (256 launches of 65536) per call: larger
+ * ranges fail with RPG_E_ARG.  The launches' scheduling counters live in one
+ * fixed 2 KiB device array per GPU, shared by all calls: calls that overlap
+ * on the GPU race on it, so serialize them (one stream, or events).  The
+ * first call on a device looks up that array's device address; make that
+ * first call before any stream capture.
+ */
+rpg_status rpg_session_sieve_noalloc(rpg_session *session, int32_t first, int32_t last,
+                                     int64_t *device_numerators, int32_t *device_denominators,
+                                     uint64_t capacity, uint64_t *device_count, void *stream);
+
 int32_t rpg_device_count(void);
 int32_t rpg_abi_version(void);
 const char *rpg_last_error(void);

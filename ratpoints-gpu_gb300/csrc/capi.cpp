@@ -12,6 +12,7 @@
 #include "exact.hpp"
 #include "plan.hpp"
 #include "search.hpp"
+#include "session.hpp"
 #include "sieve.hpp"
 
 namespace {
@@ -95,14 +96,11 @@ void fill_stats(rpg_sieve_stats *stats, const rpg::SearchMetrics &m) {
 
 }  // namespace
 
-struct rpg_session {
-    std::unique_ptr<rpg::Sieve> sieve;
-    cudaEvent_t begin = nullptr, end = nullptr;
-    ~rpg_session() {
-        if (begin) cudaEventDestroy(begin);
-        if (end) cudaEventDestroy(end);
-    }
-};
+namespace rpg {
+// Records the message rpg_last_error() returns on this thread (for entry
+// points defined outside this file).
+void set_last_error(const std::string &message) { g_last_error = message; }
+}  // namespace rpg
 
 extern "C" {
 

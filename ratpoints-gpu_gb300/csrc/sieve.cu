@@ -831,6 +831,37 @@ unsigned long long Sieve::swept_words(long long first, long long last) const {
     return total;
 }
 
+int Sieve::device() const { return impl_->device; }
+
+bool Sieve::launch_into(long long first, long long last, long long *out_a, int *out_d,
+                        unsigned long long capacity, unsigned long long *out_count,
+                        unsigned long long *work, cudaStream_t stream) {
+    const auto &I = *impl_;
+    if (I.words > I.max_tile || last < first || last - first + 1 > (1 << 16)) return false;
+    dev::SieveArgs A{};
+    A.bound = I.bound;
+    A.words = I.words;
+    A.w_lo = 0;
+    A.w_hi = I.words;
+    A.k_first = first;
+    A.k_count = int(last - first + 1);
+    A.square = I.opt.square ? 1 : 0;
+    A.out_a = out_a;
+    A.out_d = out_d;
+    A.out_count = out_count;
+    A.capacity = capacity;
+    if (I.opt.plan == PlanKind::fast) {
+        const int blocks =
+            int(std::min<long long>(I.grid, (A.k_count + dev::kFFetch - 1) / dev::kFFetch));
+        dev::fast_sieve_kernel<<<blocks, dev::kFThreads, I.fast_smem, stream>>>(I.F, A, work);
+    } else {
+        const int blocks = int(std::min<long long>(I.grid, A.k_count));
+        dev::ref_sieve_kernel<<<blocks, dev::kThreads, dev::kRefSmem, stream>>>(I.T, A);
+    }
+    check_cuda(cudaGetLastError(), "sieve kernel launch");
+    return true;
+}
+
 unsigned Sieve::smem_bytes_per_word() const {
     return impl_->opt.plan == PlanKind::fast ? unsigned(8 * impl_->F.slots)
                                              : unsigned(8 * dev::kRefFast);

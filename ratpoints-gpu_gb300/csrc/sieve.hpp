@@ -86,6 +86,16 @@ public:
     unsigned long long swept_words(long long first, long long last) const;
     unsigned smem_bytes_per_word() const;
 
+    // Enqueue one sieve launch for parameters [first, last] (at most one batch
+    // of 65536) on `stream`, writing survivors into caller-owned device arrays
+    // and counting them in *out_count; `work` is a zeroed device counter the
+    // launch uses for dynamic scheduling.  Allocates nothing; returns false if
+    // a row does not fit one launch (very large H).
+    bool launch_into(long long first, long long last, long long *out_a, int *out_d,
+                     unsigned long long capacity, unsigned long long *out_count,
+                     unsigned long long *work, cudaStream_t stream);
+    int device() const;
+
 private:
     struct Impl;
     std::unique_ptr<Impl> impl_;
