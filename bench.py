@@ -198,6 +198,34 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def reference_gpu(coeffs, denominators, rpg):
+    """The reference's own sieve kernels (src/sieve.cu compiled unchanged for
+    sm_103a) on the first `denominators` denominators of the workload, with the
+    reference's host loop restated; parity against this project's reference
+    plan on the same sample."""
+    sys.path.insert(0, str(ROOT / "oracle" / "ref_gpu"))
+    import ref_gpu
+    import ratpoints_oracle as oracle
+
+    if not ref_gpu.available():
+        return {"unavailable": "reference cubin not built (needs the reference tree at build time)"}
+    ref_gpu.run(coeffs, HEIGHT, 1, min(denominators, 4096))  # warm-up
+    ref = ref_gpu.run(coeffs, HEIGHT, 1, denominators)
+    a, d, _ = rpg.sieve(coeffs, HEIGHT, 1, denominators, plan="reference")
+    digest = sum(oracle.mix_pair(x, y) for x, y in zip(a.tolist(), d.tolist())) % 2**64
+    reduced = reduced_sites(HEIGHT, denominators)
+    rect = (2 * HEIGHT + 1) * denominators
+    return {"denominators": denominators, "kernel_ms": ref["sieve_ms"], "basis_ms": ref["basis_ms"],
+            "wall_ms": ref["wall_ms"],
+            "value": reduced / (ref["sieve_ms"] / 1e3) / 1e9, "unit": UNIT,
+            "rectangle_gsites_per_s": rect / (ref["sieve_ms"] / 1e3) / 1e9,
+            "survivors": ref["survivors"],
+            "survivor_set_matches_reference_plan": (len(a), digest) == (ref["survivors"],
+                                                                        ref["digest"]),
+            "note": "reference src/sieve.cu compiled for sm_103a, kernel event time; basis built "
+                    "once (the reference rebuilds it per batch)"}
+
+
 def workload_config():
     rect = (2 * HEIGHT + 1) * DENOMINATORS
     return {"workload": "degree-6 curve, coefficients uniform in [-2^32, 2^32), "
@@ -215,6 +243,7 @@ def main():
     parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
     parser.add_argument("--plan", choices=["reference", "fast"], default="fast")
     parser.add_argument("--reference-plan-steps", type=int, default=2)
+    parser.add_argument("--reference-gpu-denominators", type=int, default=655360)
     parser.add_argument("--denominators", type=int, default=DENOMINATORS)
     parser.add_argument("--e2e-steps", type=int, default=1, choices=range(1, 100), metavar="N")
     parser.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -323,6 +352,8 @@ def main():
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clock,
     }
+    if args.reference_gpu_denominators > 0:
+        line["reference_gpu"] = reference_gpu(coeffs, args.reference_gpu_denominators, rpg)
     if ref is not None:
         line["reference_plan"] = {
             "value": reduced * world / (ref["ms"] / 1e3) / 1e9, "unit": UNIT,

@@ -1,0 +1,262 @@
+// ref_driver.cpp - host driver for the reference's own GPU sieve kernels.
+//
+// BASELINE AND CHECKER INFRASTRUCTURE ONLY (tests/ and bench.py load it; no
+// product path does).  oracle/_ref/ref_sieve.cubin is the reference's
+// src/sieve.cu compiled unchanged for sm_103a (oracle/ref_gpu/build_ref.py).
+// This file loads that cubin through the CUDA driver API, finds its
+// basis_kernel and sieve_kernel<unsigned, mode> entries by name, and restates
+// the reference's host driver around them:
+//   - SievePlan: 36 candidate primes, Sum p^2 mask words, 32 selected primes
+//     per denominator, word_count = (2H + 32) / 32, shared bytes = 4 x the 14
+//     largest primes (src/sieve_plan.cpp:104-151) - via the oracle's C helpers;
+//   - build_mask_basis: per prime, affine mask + inverses, one basis_kernel
+//     launch over p*p words (src/sieve.cu:390-409);
+//   - initial_survivor_capacity (src/sieve.cu:97-118);
+//   - run_modular_sieve's loop: fast launch; on output_full, clear resume words
+//     and rerun in streaming_initial, then streaming_resume until complete
+//     (src/sieve.cu:503-564).
+// Deviations, all in the reference's favour for timing: the basis is built
+// once per run instead of once per batch, and buffers are allocated once.
+#include <cuda.h>
+#include <cxxabi.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+extern "C" {
+int rpo_candidate_primes(int *out);
+int rpo_select(long long denominator, int *out_indices);
+long long rpo_mod_inverse(long long value, long long modulus);
+void rpo_affine_mask(int prime, const char *const *coefficients, int count, unsigned char *out);
+uint64_t rpo_mix_pair(long long a, long long d);
+}
+
+namespace {
+
+struct State {
+    bool open = false;
+    CUdevice dev = 0;
+    CUcontext ctx = nullptr;
+    CUmodule mod = nullptr;
+    CUfunction basis = nullptr, fast = nullptr, stream_init = nullptr, stream_resume = nullptr;
+};
+State g;
+std::string g_error;
+
+bool ok(CUresult r, const char *what) {
+    if (r == CUDA_SUCCESS) return true;
+    const char *s = nullptr;
+    cuGetErrorString(r, &s);
+    g_error = std::string(what) + ": " + (s ? s : "unknown CUDA error");
+    return false;
+}
+
+std::string demangle(const char *name) {
+    int status = 0;
+    char *out = abi::__cxa_demangle(name, nullptr, nullptr, &status);
+    std::string s = (status == 0 && out) ? out : name;
+    std::free(out);
+    return s;
+}
+
+struct DevBuf {
+    CUdeviceptr p = 0;
+    ~DevBuf() {
+        if (p) cuMemFree(p);
+    }
+    bool alloc(size_t bytes, const char *what) { return ok(cuMemAlloc(&p, bytes ? bytes : 8), what); }
+};
+
+}  // namespace
+
+extern "C" const char *rgd_error(void) { return g_error.c_str(); }
+
+extern "C" int rgd_open(const char *cubin) {
+    if (g.open) return 0;
+    if (!ok(cuInit(0), "cuInit")) return -1;
+    if (!ok(cuDeviceGet(&g.dev, 0), "cuDeviceGet")) return -1;
+    if (!ok(cuDevicePrimaryCtxRetain(&g.ctx, g.dev), "cuDevicePrimaryCtxRetain")) return -1;
+    if (!ok(cuCtxSetCurrent(g.ctx), "cuCtxSetCurrent")) return -1;
+    if (!ok(cuModuleLoad(&g.mod, cubin), "cuModuleLoad")) return -1;
+    unsigned count = 0;
+    if (!ok(cuModuleGetFunctionCount(&count, g.mod), "cuModuleGetFunctionCount")) return -1;
+    std::vector<CUfunction> fs(count);
+    if (!ok(cuModuleEnumerateFunctions(fs.data(), count, g.mod), "cuModuleEnumerateFunctions"))
+        return -1;
+    for (CUfunction f : fs) {
+        const char *raw = nullptr;
+        if (!ok(cuFuncGetName(&raw, f), "cuFuncGetName")) return -1;
+        const std::string name = demangle(raw);
+        if (name.find("basis_kernel(") != std::string::npos) g.basis = f;
+        if (name.find("sieve_kernel<unsigned int,") == std::string::npos) continue;
+        if (name.find(")0>(") != std::string::npos) g.fast = f;
+        if (name.find(")1>(") != std::string::npos) g.stream_init = f;
+        if (name.find(")2>(") != std::string::npos) g.stream_resume = f;
+    }
+    if (!g.basis || !g.fast || !g.stream_init || !g.stream_resume) {
+        g_error = "reference kernels not found in the cubin";
+        return -1;
+    }
+    g.open = true;
+    return 0;
+}
+
+// Sieve parameters [first, last] in batches; returns 0 on success.  Survivor
+// count and order-independent digest (sum of rpo_mix_pair) as the oracle.
+extern "C" int rgd_run(const char *const *coefficients, int ncoeff, long long bound, int first,
+                       int last, int batch, int square, unsigned long long *survivors,
+                       unsigned long long *digest, double *sieve_ms, double *basis_ms,
+                       double *wall_ms) {
+    using Clock = std::chrono::steady_clock;
+    const auto t0 = Clock::now();
+    if (!g.open) {
+        g_error = "rgd_open has not succeeded";
+        return -1;
+    }
+    if (!ok(cuCtxSetCurrent(g.ctx), "cuCtxSetCurrent")) return -1;
+    const int kPrimes = 32, kCandidates = 36, kInitial = 14, kBlock = 256, kWarps = 8;
+    int primes[36];
+    rpo_candidate_primes(primes);
+    std::vector<long long> offsets(kCandidates);
+    long long mask_count = 0;
+    for (int i = 0; i < kCandidates; ++i) {
+        offsets[i] = mask_count;
+        mask_count += (long long)primes[i] * primes[i];
+    }
+    const long long words = (2 * bound + 32) / 32;
+    if (words > (long long)UINT32_MAX - (kBlock - 1)) {
+        g_error = "64-bit word counts are not driven by this baseline";
+        return -1;
+    }
+    size_t shared_bytes = 0;
+    for (int i = 0; i < kInitial; ++i) shared_bytes += primes[kCandidates - 1 - i] * 4;
+    batch = std::max(1, std::min(batch, 65536));
+    // initial_survivor_capacity (src/sieve.cu:97-118), without the free-memory cap.
+    long double sites = (long double)batch * (2.0L * bound + 1.0L);
+    long double est = std::ldexp(sites, -kInitial);
+    est = std::max(est, (long double)batch);
+    est = std::max(est, 4096.0L);
+    est = std::min(est, (long double)(1 << 24));
+    const unsigned long long capacity = (unsigned long long)std::ceil(est);
+
+    DevBuf masks, affine, inverses, dprimes, doffsets, selected, resume, count, full, out_num, out_den;
+    if (!masks.alloc(mask_count * 4, "cuMemAlloc masks") || !affine.alloc(512, "cuMemAlloc") ||
+        !inverses.alloc(512 * 4, "cuMemAlloc") || !dprimes.alloc(kCandidates * 4, "cuMemAlloc") ||
+        !doffsets.alloc(kCandidates * 8, "cuMemAlloc") ||
+        !selected.alloc(size_t(batch) * kPrimes * 4, "cuMemAlloc") ||
+        !resume.alloc(size_t(batch) * kWarps * 8, "cuMemAlloc") || !count.alloc(8, "cuMemAlloc") ||
+        !full.alloc(4, "cuMemAlloc") || !out_num.alloc(capacity * 8, "cuMemAlloc survivors") ||
+        !out_den.alloc(capacity * 4, "cuMemAlloc survivors"))
+        return -1;
+    if (!ok(cuMemcpyHtoD(dprimes.p, primes, sizeof primes), "upload primes")) return -1;
+    if (!ok(cuMemcpyHtoD(doffsets.p, offsets.data(), offsets.size() * 8), "upload offsets")) return -1;
+
+    CUevent e0, e1;
+    cuEventCreate(&e0, CU_EVENT_DEFAULT);
+    cuEventCreate(&e1, CU_EVENT_DEFAULT);
+    float ms = 0;
+    // Basis (src/sieve.cu:390-409): one launch per candidate prime.
+    cuEventRecord(e0, nullptr);
+    for (int i = 0; i < kCandidates; ++i) {
+        const int p = primes[i];
+        unsigned char aff[512];
+        int inv[512] = {0};
+        rpo_affine_mask(p, coefficients, ncoeff, aff);
+        for (int v = 1; v < p; ++v) inv[v] = (int)rpo_mod_inverse(v, p);
+        if (!ok(cuMemcpyHtoD(affine.p, aff, p), "upload affine")) return -1;
+        if (!ok(cuMemcpyHtoD(inverses.p, inv, p * 4), "upload inverses")) return -1;
+        CUdeviceptr mp = masks.p, ap = affine.p, ip = inverses.p;
+        int prime = p;
+        long long off = offsets[i], b = bound;
+        void *args[] = {&mp, &ap, &ip, &prime, &off, &b};
+        const unsigned blocks = unsigned((p * p + kBlock - 1) / kBlock);
+        if (!ok(cuLaunchKernel(g.basis, blocks, 1, 1, kBlock, 1, 1, 0, nullptr, args, nullptr),
+                "basis_kernel launch"))
+            return -1;
+    }
+    cuEventRecord(e1, nullptr);
+    if (!ok(cuEventSynchronize(e1), "basis_kernel")) return -1;
+    cuEventElapsedTime(&ms, e0, e1);
+    *basis_ms = ms;
+
+    unsigned long long total = 0, sum = 0;
+    double sieve_total = 0;
+    std::vector<int> sel;
+    std::vector<long long> host_num;
+    std::vector<int> host_den;
+    for (long long lo = first; lo <= last; lo += batch) {
+        const long long hi = std::min<long long>(last, lo + batch - 1);
+        const int n = int(hi - lo + 1);
+        sel.assign(size_t(n) * kPrimes, 0);
+        for (int j = 0; j < n; ++j) {
+            const long long k = lo + j;
+            const long long d = square ? k * k : k;
+            if (rpo_select(d, &sel[size_t(j) * kPrimes]) != 0) {
+                g_error = "insufficient denominator sieve primes";
+                return -1;
+            }
+        }
+        if (!ok(cuMemcpyHtoD(selected.p, sel.data(), sel.size() * 4), "upload selected")) return -1;
+        int mode = 0;  // 0 fast, 1 streaming_initial, 2 streaming_resume
+        for (;;) {
+            cuMemsetD8(count.p, 0, 8);
+            cuMemsetD8(full.p, 0, 4);
+            CUdeviceptr mp = masks.p, pp = dprimes.p, op = doffsets.p, sp = selected.p;
+            unsigned w = unsigned(words);
+            long long b = bound;
+            int min_den = int(lo);
+            bool sq = square != 0;
+            CUdeviceptr np = out_num.p, dp = out_den.p, cp = count.p, fp = full.p, rp = resume.p;
+            unsigned long long cap = capacity;
+            void *args[] = {&mp, &pp, &op, &sp, &w, &b, &min_den, &sq, &np, &dp, &cp, &fp, &rp, &cap};
+            CUfunction f = mode == 0 ? g.fast : (mode == 1 ? g.stream_init : g.stream_resume);
+            cuEventRecord(e0, nullptr);
+            if (!ok(cuLaunchKernel(f, unsigned(n), 1, 1, kBlock, 1, 1, unsigned(shared_bytes), nullptr,
+                                   args, nullptr),
+                    "sieve_kernel launch"))
+                return -1;
+            cuEventRecord(e1, nullptr);
+            if (!ok(cuEventSynchronize(e1), "sieve_kernel")) return -1;
+            cuEventElapsedTime(&ms, e0, e1);
+            sieve_total += ms;
+            unsigned long long c = 0;
+            unsigned flag = 0;
+            if (!ok(cuMemcpyDtoH(&c, count.p, 8), "download count") ||
+                !ok(cuMemcpyDtoH(&flag, full.p, 4), "download full flag"))
+                return -1;
+            if (mode == 0 && flag) {  // rerun through the resumable path
+                cuMemsetD8(resume.p, 0, size_t(n) * kWarps * 8);
+                mode = 1;
+                continue;
+            }
+            if (c > capacity) {
+                g_error = "streaming survivor count exceeds capacity";
+                return -1;
+            }
+            if (c) {
+                host_num.resize(c);
+                host_den.resize(c);
+                if (!ok(cuMemcpyDtoH(host_num.data(), out_num.p, c * 8), "download survivors") ||
+                    !ok(cuMemcpyDtoH(host_den.data(), out_den.p, c * 4), "download survivors"))
+                    return -1;
+                for (unsigned long long i = 0; i < c; ++i) sum += rpo_mix_pair(host_num[i], host_den[i]);
+            }
+            total += c;
+            if (!flag) break;
+            mode = 2;
+        }
+    }
+    cuEventDestroy(e0);
+    cuEventDestroy(e1);
+    *survivors = total;
+    *digest = sum;
+    *sieve_ms = sieve_total;
+    *wall_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+    return 0;
+}

@@ -1,0 +1,61 @@
+"""The reference plan against the reference's own CUDA kernels on the GPU.
+
+oracle/_ref/ref_sieve.cubin is the reference's src/sieve.cu compiled unchanged
+for sm_103a; oracle/ref_gpu drives it with a restatement of the reference's
+host loop.  The survivor multiset of this project's reference plan must equal
+the reference kernels' (count and order-independent digest), including the
+streaming overflow path of the reference (dense curve).
+"""
+
+import random
+import sys
+from pathlib import Path
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+sys.path.insert(0, str(Path(__file__).resolve().parent.parent / "oracle" / "ref_gpu"))
+import ref_gpu  # noqa: E402
+
+if not ref_gpu.available():
+    pytest.skip("reference cubin not built (needs the reference tree at build time)",
+                allow_module_level=True)
+
+RECORD = "247747600 -985905640 567207969 2396040466 52485681 -470135160 82342800".split()
+
+
+def compare(rpg, oracle, coeffs, bound, first, last, square=False, batch=65536):
+    ref = ref_gpu.run(coeffs, bound, first, last, batch=batch, square=square)
+    a, d, _ = rpg.sieve(coeffs, bound, first, last, square=square, plan="reference")
+    digest = sum(oracle.mix_pair(x, y) for x, y in zip(a.tolist(), d.tolist())) % 2**64
+    assert (len(a), digest) == (ref["survivors"], ref["digest"]), (coeffs[:2], bound, first, last)
+    return ref
+
+
+def test_dense_streaming_path(rpg, oracle, golden):
+    ref = compare(rpg, oracle, golden["dense"]["coefficients"].split(), 5000, 1, 2)
+    assert ref["survivors"] == 20002
+
+
+def test_record_curve(rpg, oracle):
+    compare(rpg, oracle, RECORD, 100_000, 1, 3000, batch=1000)
+
+
+def test_c1_box(rpg, oracle, golden):
+    compare(rpg, oracle, golden["c1"]["coefficients"].split(), 2000, 1, 2000, batch=499)
+
+
+def test_square_denominators(rpg, oracle):
+    compare(rpg, oracle, ["5", "-3", "0", "1"], 20000, 1, 4000, square=True)
+
+
+def test_random_large_coefficients(rpg, oracle):
+    rng = random.Random(37)
+    coeffs = [str(rng.randint(-(2**128), 2**128)) for _ in range(11)]
+    compare(rpg, oracle, coeffs, 30000, 100, 1100)
+
+
+def test_c2_sample(rpg, oracle):
+    import bench
+    compare(rpg, oracle, bench.c2_curve(), 5_000_000, 1, 2048)
