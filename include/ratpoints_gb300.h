@@ -146,6 +146,13 @@ rpg_status rpg_session_create(const char *const *coefficients, int32_t coefficie
                               rpg_session **session);
 rpg_status rpg_session_count(rpg_session *session, int32_t first, int32_t last,
                              int32_t batch_size, uint64_t *survivors, double *device_ms);
+/* The fast plan the session chose for its curve: numerator classes are taken
+ * modulo 64 * class_prime (1: 2-adic classes only) and the first-stage rows
+ * test the small primes written to primes[0 .. *count).  For a reference-plan
+ * session class_prime and *count are 0. */
+rpg_status rpg_session_plan(rpg_session *session, int32_t *class_prime, int32_t *primes,
+                            int32_t capacity, int32_t *count);
+
 /* Work a pass over parameters [first, last] does: 64-site words the sieve
  * kernel sweeps (admissible classes only under the fast plan) and the
  * shared-memory bytes its first stage reads per swept word. */

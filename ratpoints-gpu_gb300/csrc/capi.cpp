@@ -286,6 +286,19 @@ rpg_status rpg_session_work(rpg_session *session, int32_t first, int32_t last,
     });
 }
 
+rpg_status rpg_session_plan(rpg_session *session, int32_t *class_prime, int32_t *primes,
+                            int32_t capacity, int32_t *count) {
+    return guarded([&]() -> rpg_status {
+        if (!session || !class_prime || !count) return fail(RPG_E_ARG, "arguments must not be NULL");
+        const rpg::FastPlanInfo info = session->sieve->fast_plan_info();
+        *class_prime = info.class_prime;
+        *count = int32_t(info.primes.size());
+        if (*count > capacity || (*count && !primes)) return fail(RPG_E_ARG, "prime buffer too small");
+        for (int32_t i = 0; i < *count; ++i) primes[i] = info.primes[i];
+        return RPG_OK;
+    });
+}
+
 void rpg_session_destroy(rpg_session *session) { delete session; }
 
 int32_t rpg_device_count(void) {

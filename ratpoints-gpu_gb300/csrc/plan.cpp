@@ -1,5 +1,8 @@
 #include "plan.hpp"
 
+#include <algorithm>
+#include <cmath>
+
 namespace rpg {
 
 const std::array<int, kCandidatePrimes> &candidate_primes() {
@@ -70,5 +73,131 @@ long long word_count64(long long bound) {
     return sites / 64 + (sites % 64 != 0);
 }
 long long word_count32(long long bound) { return (2 * bound + 32) / 32; }
+
+double pass_rate(int q, const std::vector<std::string> &coefficients) {
+    const auto aff = affine_mask(q, coefficients);
+    int n = 0;
+    for (auto v : aff) n += v;
+    return double(n) / q;
+}
+
+namespace {
+// Worst-case number of numerator classes for class prime q: admissible
+// 2-adic classes times admissible residues mod q, over all d.
+int max_classes(int q, const std::vector<std::string> &coefficients) {
+    const int n = int(coefficients.size()) - 1;
+    std::vector<int> c64(coefficients.size()), cq(coefficients.size());
+    for (std::size_t i = 0; i < coefficients.size(); ++i) {
+        c64[i] = decimal_mod(coefficients[i], 64);
+        cq[i] = decimal_mod(coefficients[i], q);
+    }
+    bool sq64[64] = {};
+    for (int v = 0; v < 64; ++v) sq64[(v * v) & 63] = true;
+    int worst2 = 0;
+    for (int dd = 0; dd < 64; ++dd) {
+        int count = 0;
+        for (int r = 0; r < 64; ++r) {
+            if (dd % 2 == 0 && r % 2 == 0) continue;
+            int value = c64[n], power = 1;
+            for (int i = n - 1; i >= 0; --i) {
+                value = (value * r) & 63;
+                power = (power * dd) & 63;
+                value = (value + c64[i] * power) & 63;
+            }
+            if (n % 2 == 1) value = (value * dd) & 63;
+            count += sq64[value];
+        }
+        worst2 = std::max(worst2, count);
+    }
+    const auto aff = affine_mask(q, coefficients);
+    int admissible = 0;
+    for (auto v : aff) admissible += v;
+    // q | d admits every class r != 0 (mod q) at most
+    return worst2 * std::max(admissible, q - 1);
+}
+}  // namespace
+
+FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long long bound) {
+    FastPlan plan;
+    std::vector<std::pair<double, int>> strength;  // (bits, prime)
+    for (int q = 3; q < kFastPrimeLimit; q += 2) {
+        bool prime = true;
+        for (int f = 3; f * f <= q; f += 2) prime = prime && q % f;
+        if (!prime) continue;
+        const double rate = pass_rate(q, coefficients);
+        strength.push_back({rate > 0 ? -std::log2(rate) : 8.0, q});
+    }
+    // Class prime: the strongest of 3..13 whose classes stay long enough
+    // (at least 256 words of 64 sites per class) and few enough.
+    const long double sites = 2.0L * bound + 1.0L;
+    double best = 0.45;  // below ~0.45 bits a class prime does not pay for its classes
+    for (const auto &s : strength) {
+        const int q = s.second;
+        if (q > 13) continue;
+        if (sites / (64.0L * 64.0L * q) < 256.0L) continue;
+        if (max_classes(q, coefficients) > kMaxFastClasses) continue;
+        if (s.first > best) {
+            best = s.first;
+            plan.class_prime = q;
+        }
+    }
+    // Stage-1 moduli: pack primes into at most kMaxFastSlots products below
+    // kMaxModulus.  Each packing puts a prime into the open modulus with the
+    // most headroom that it fits, else opens a new one; it is tried with the
+    // primes ordered by bits and by bits per bit of size, over primes below 72
+    // and below kFastPrimeLimit, and the packing with the most bits is kept.
+    auto pack = [&](std::vector<std::pair<double, int>> order, int limit, bool by_density) {
+        if (by_density)
+            std::sort(order.begin(), order.end(),
+                      [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+                          const double da = a.first / std::log2(double(a.second));
+                          const double db = b.first / std::log2(double(b.second));
+                          return da != db ? da > db : a.second < b.second;
+                      });
+        else
+            std::sort(order.begin(), order.end(),
+                      [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+                          return a.first != b.first ? a.first > b.first : a.second < b.second;
+                      });
+        FastPlan out;
+        out.class_prime = plan.class_prime;
+        for (const auto &s : order) {
+            const int q = s.second;
+            if (q >= limit || q == plan.class_prime || s.first < 0.3) continue;
+            int target = -1;
+            long long headroom = -1;
+            for (std::size_t i = 0; i < out.moduli.size(); ++i) {
+                const long long product = (long long)out.moduli[i] * q;
+                if (product <= kMaxModulus && kMaxModulus - product > headroom) {
+                    headroom = kMaxModulus - product;
+                    target = int(i);
+                }
+            }
+            if (target < 0) {
+                if ((int)out.moduli.size() == kMaxFastSlots) continue;
+                out.moduli.push_back(1);
+                out.slots.push_back({});
+                target = int(out.moduli.size()) - 1;
+            }
+            out.moduli[target] *= q;
+            out.slots[target].push_back(q);
+            out.bits += s.first;
+        }
+        return out;
+    };
+    FastPlan best_plan = plan;
+    best_plan.bits = -1;
+    for (int limit : {72, kFastPrimeLimit})
+        for (bool density : {false, true}) {
+            FastPlan candidate = pack(strength, limit, density);
+            if (candidate.bits > best_plan.bits) best_plan = candidate;
+        }
+    plan = best_plan;
+    if (plan.moduli.empty()) {  // every small prime is weak: keep one modulus anyway
+        plan.moduli.push_back(5 * 7);
+        plan.slots.push_back({5, 7});
+    }
+    return plan;
+}
 
 }  // namespace rpg

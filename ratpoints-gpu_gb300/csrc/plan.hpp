@@ -46,4 +46,25 @@ long long word_count64(long long bound);
 // reported by the -v metrics line.
 long long word_count32(long long bound);
 
+// Fraction of x in [0, q) with f(x) a square mod q (0 included): the share of
+// sites (a, d), q !| d, that pass the test mod q.
+double pass_rate(int q, const std::vector<std::string> &coefficients);
+
+// Per-curve choice of the fast plan's small-prime filters (this project's
+// autotuner).  Numerator classes are taken modulo 64 * class_prime (2-adic
+// classes crossed with the admissible residues mod class_prime; class_prime 1
+// means 2-adic classes only); the first-stage rows are products of the other
+// strong small primes, at most kMaxFastSlots of them, each below kMaxModulus.
+constexpr int kMaxFastSlots = 6;
+constexpr int kMaxModulus = 1500;
+constexpr int kMaxFastClasses = 256;
+constexpr int kFastPrimeLimit = 128;  // small primes considered: 3 .. 127
+struct FastPlan {
+    int class_prime = 1;
+    std::vector<std::vector<int>> slots;   // prime factors of each stage-1 modulus
+    std::vector<int> moduli;               // their products
+    double bits = 0;                       // expected filtering of the stage-1 rows (bits)
+};
+FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long long bound);
+
 }  // namespace rpg

@@ -250,6 +250,7 @@ struct Sieve::Impl {
     dev::u64 *fast_adm = nullptr;
     std::size_t fast_smem = 0;
     std::vector<dev::u64> fast_adm_host;
+    FastPlan fast_plan;
     long long max_tile = dev::kMaxTileWords;
     long long capacity = 0;
     SieveTimings timings;
@@ -406,96 +407,104 @@ struct Sieve::Impl {
         else build_tables(coefficients);
     }
 
-    // Fast plan: class-layout tables for the stage-1 composite moduli and the
-    // 36 reference candidates, and the 2-adic admissible-class table.
+    // Fast plan: the per-curve plan (class prime, stage-1 moduli), class-layout
+    // tables for the stage-1 moduli and the 36 reference candidates, and the
+    // admissible-class tables (2-adic by d mod 64, residues mod q by d mod q).
     void build_fast_tables(const std::vector<std::string> &coefficients) {
         auto t0 = Clock::now();
-        // Stage-1 moduli: products of small odd primes (3*5*7, 11*13, 17*19, 23*29, 31*37).
-        static const int kFactors[dev::kFastSlots][dev::kFastMaxFactors + 1] = {
-            {3, 3, 5, 7}, {2, 11, 13, 0}, {2, 17, 19, 0}, {2, 23, 29, 0}, {2, 31, 37, 0}};
+        fast_plan = choose_fast_plan(coefficients, bound);
         const int n = int(coefficients.size()) - 1;
+        const int q = fast_plan.class_prime;
+        const long long M = 64LL * q;
+        const long long S = 64LL * M;
         std::vector<int> primes_used;
-        for (const auto &f : kFactors)
-            for (int i = 1; i <= f[0]; ++i) primes_used.push_back(f[i]);
+        for (const auto &f : fast_plan.slots)
+            for (int p : f) primes_used.push_back(p);
+        if (q > 1) primes_used.push_back(q);
         for (int p : candidate_primes()) primes_used.push_back(p);
         std::vector<unsigned char> affine;
         std::vector<unsigned short> inverse;
         std::vector<int> base(kMaximumPrime, -1), lead(kMaximumPrime, 1);
-        for (int q : primes_used) {
-            if (base[q] >= 0) continue;
-            base[q] = int(affine.size());
-            auto aff = affine_mask(q, coefficients);
+        for (int p : primes_used) {
+            if (base[p] >= 0) continue;
+            base[p] = int(affine.size());
+            auto aff = affine_mask(p, coefficients);
             affine.insert(affine.end(), aff.begin(), aff.end());
             inverse.push_back(0);
-            for (int v = 1; v < q; ++v) inverse.push_back((unsigned short)mod_inverse(v, q));
+            for (int v = 1; v < p; ++v) inverse.push_back((unsigned short)mod_inverse(v, p));
             if (n % 2 == 0) {
-                const int lc = decimal_mod(coefficients.back(), q);
+                const int lc = decimal_mod(coefficients.back(), p);
                 bool square = false;
-                for (int v = 0; v < q && !square; ++v) square = (v * v) % q == lc;
-                lead[q] = square ? 1 : 0;
+                for (int v = 0; v < p && !square; ++v) square = (v * v) % p == lc;
+                lead[p] = square ? 1 : 0;
             }
         }
         std::vector<dev::TableSpec> specs;
         long long total = 0;
         int smem_words = 0;
-        F.slots = dev::kFastSlots;
-        for (int sl = 0; sl < dev::kFastSlots; ++sl) {
-            dev::TableSpec S{};
-            S.nf = kFactors[sl][0];
-            S.m = 1;
-            for (int i = 0; i < S.nf; ++i) {
-                S.q[i] = kFactors[sl][i + 1];
-                S.m *= S.q[i];
-                S.factor_base[i] = base[S.q[i]];
-                S.lead_ok[i] = lead[S.q[i]];
+        F = dev::FastTables{};
+        F.slots = int(fast_plan.moduli.size());
+        for (int sl = 0; sl < F.slots; ++sl) {
+            dev::TableSpec Sp{};
+            Sp.nf = int(fast_plan.slots[sl].size());
+            Sp.m = fast_plan.moduli[sl];
+            for (int i = 0; i < Sp.nf; ++i) {
+                Sp.q[i] = fast_plan.slots[sl][i];
+                Sp.factor_base[i] = base[Sp.q[i]];
+                Sp.lead_ok[i] = lead[Sp.q[i]];
             }
-            S.length = (S.m + dev::kFExt + 1) & ~1;
-            S.offset = total;
-            total += (long long)S.m * S.length;
-            specs.push_back(S);
-            dev::FastModulus &M = F.mod[sl];
-            M.m = S.m;
-            M.nf = S.nf;
-            for (int i = 0; i < S.nf; ++i) M.q[i] = S.q[i];
-            M.length = S.length;
-            M.offset = S.offset;
-            M.smem_offset = smem_words;
-            smem_words += S.length;
-            M.inv4096 = dev::u32(mod_inverse(4096 % S.m, S.m));
-            M.neg_h = dev::u32((S.m - bound % S.m) % S.m);
-            M.wlo_mod = 0;
-            M.magic = (unsigned long long)((~0ull) / (unsigned long long)S.m) + 1;
+            Sp.length = (Sp.m + dev::kFExt + 1) & ~1;
+            Sp.offset = total;
+            total += (long long)Sp.m * Sp.length;
+            specs.push_back(Sp);
+            dev::FastModulus &Md = F.mod[sl];
+            Md.m = Sp.m;
+            Md.nf = Sp.nf;
+            for (int i = 0; i < Sp.nf; ++i) Md.q[i] = Sp.q[i];
+            Md.length = Sp.length;
+            Md.offset = Sp.offset;
+            Md.smem_offset = smem_words;
+            smem_words += Sp.length;
+            Md.inv_stride = dev::u32(mod_inverse(S % Sp.m, Sp.m));
+            Md.neg_h = dev::u32((Sp.m - bound % Sp.m) % Sp.m);
+            Md.wlo_mod = 0;
+            Md.step = dev::u32((dev::kWarpSize * dev::kFK) % Sp.m);
+            Md.magic = (unsigned long long)((~0ull) / (unsigned long long)Sp.m) + 1;
         }
         F.smem_words = smem_words;
         const auto &cands = candidate_primes();
         for (int i = 0; i < kCandidatePrimes; ++i) {
             const int p = cands[i];
-            dev::TableSpec S{};
-            S.nf = 1;
-            S.m = p;
-            S.q[0] = p;
-            S.factor_base[0] = base[p];
-            S.lead_ok[0] = 0;
-            S.length = p;
-            S.offset = total;
+            dev::TableSpec Sp{};
+            Sp.nf = 1;
+            Sp.m = p;
+            Sp.q[0] = p;
+            Sp.factor_base[0] = base[p];
+            Sp.lead_ok[0] = 0;
+            Sp.length = p;
+            Sp.offset = total;
             total += (long long)p * p;
-            specs.push_back(S);
+            specs.push_back(Sp);
             dev::FastPrime &P = F.prime[i];
-            P.offset = S.offset;
+            P.offset = Sp.offset;
             P.p = p;
-            P.inv4096 = dev::u32(mod_inverse(4096 % p, p));
+            P.inv_stride = dev::u32(mod_inverse(S % p, p));
             P.neg_h = dev::u32((p - bound % p) % p);
             P.magic = dev::magic40(dev::u32(p));
             P.wlo_mod = 0;
         }
-        F.h_mod64 = int(bound % 64);
-        // 2-adic admissibility: class r for d (mod 64) iff F(r, d) is a square
-        // mod 64 and r is odd when d is even.
+        F.class_prime = q;
+        F.class_mod = int(M);
+        F.h_mod_m = int(bound % M);
+        F.inv64_q = q > 1 ? int(mod_inverse(64 % q, q)) : 0;
+        F.stride = S;
+        // Admissible classes: 2-adic by d mod 64 (F(r, d) square mod 64, r odd
+        // when d is even), then residues r mod q by d mod q.
         std::vector<int> c64(coefficients.size());
         for (std::size_t i = 0; i < coefficients.size(); ++i) c64[i] = decimal_mod(coefficients[i], 64);
         bool square64[64] = {};
         for (int v = 0; v < 64; ++v) square64[(v * v) & 63] = true;
-        std::vector<dev::u64> adm(64, 0);
+        std::vector<dev::u64> adm(64 + dev::kFAdmQ, 0);
         for (int dd = 0; dd < 64; ++dd) {
             for (int r = 0; r < 64; ++r) {
                 if (dd % 2 == 0 && r % 2 == 0) continue;
@@ -509,11 +518,22 @@ struct Sieve::Impl {
                 if (square64[value]) adm[dd] |= dev::u64(1) << r;
             }
         }
+        if (q > 1) {
+            const auto aff = affine_mask(q, coefficients);
+            for (int dq = 0; dq < q; ++dq) {
+                for (int r = 0; r < q; ++r) {
+                    bool ok;
+                    if (dq == 0) ok = r != 0 && lead[q];
+                    else ok = aff[(r * mod_inverse(dq, q)) % q] != 0;
+                    if (ok) adm[64 + dq] |= dev::u64(1) << r;
+                }
+            }
+        }
         fast_adm_host = adm;
         timings.plan_ms += ms_since(t0);
         auto t1 = Clock::now();
         fast_rows = device_alloc<dev::u64>(std::size_t(total), "cudaMalloc(class tables)");
-        fast_adm = device_alloc<dev::u64>(64, "cudaMalloc(admissible classes)");
+        fast_adm = device_alloc<dev::u64>(adm.size(), "cudaMalloc(admissible classes)");
         unsigned char *d_aff = device_alloc<unsigned char>(affine.size(), "cudaMalloc(affine)");
         unsigned short *d_inv = device_alloc<unsigned short>(inverse.size(), "cudaMalloc(inverse)");
         dev::TableSpec *d_specs = device_alloc<dev::TableSpec>(specs.size(), "cudaMalloc(specs)");
@@ -530,15 +550,15 @@ struct Sieve::Impl {
         check_cuda(cudaMemcpyAsync(d_specs, specs.data(), specs.size() * sizeof(dev::TableSpec),
                                    cudaMemcpyHostToDevice, stream),
                    "upload table specs");
-        check_cuda(cudaMemcpyAsync(fast_adm, adm.data(), 64 * sizeof(dev::u64), cudaMemcpyHostToDevice,
-                                   stream),
+        check_cuda(cudaMemcpyAsync(fast_adm, adm.data(), adm.size() * sizeof(dev::u64),
+                                   cudaMemcpyHostToDevice, stream),
                    "upload admissible classes");
         timings.h2d_bytes += affine.size() + inverse.size() * sizeof(unsigned short) +
-                             specs.size() * sizeof(dev::TableSpec) + 64 * sizeof(dev::u64);
+                             specs.size() * sizeof(dev::TableSpec) + adm.size() * sizeof(dev::u64);
         const int threads = 256;
         const long long blocks = (total + threads - 1) / threads;
         dev::class_table_kernel<<<unsigned(blocks), threads, 0, stream>>>(
-            fast_rows, d_specs, int(specs.size()), d_aff, d_inv, total);
+            fast_rows, d_specs, int(specs.size()), d_aff, d_inv, S, int(M), total);
         check_cuda(cudaGetLastError(), "class_table_kernel launch");
         check_cuda(cudaEventRecord(e1, stream), "cudaEventRecord");
         check_cuda(cudaEventSynchronize(e1), "class table build");
@@ -553,22 +573,48 @@ struct Sieve::Impl {
         F.rows = fast_rows;
         F.prime_rows = fast_rows;
         F.admissible = fast_adm;
-        fast_smem = std::size_t(F.smem_words) * 8 + std::size_t(dev::kFWarps) * dev::kFQueue * 12;
-        check_cuda(cudaFuncSetAttribute(dev::fast_sieve_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(fast_smem)),
+        fast_smem = std::size_t(F.smem_words) * 8 + std::size_t(dev::kFWarps) * dev::kFQueue * 12 +
+                    std::size_t(dev::kFMaxClasses) * F.slots * 4;
+        const void *kernel = fast_kernel_ptr(F.slots);
+        check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(fast_smem)),
                    "cudaFuncSetAttribute");
         int sms = 0, per_sm = 0;
         check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device),
                    "cudaDeviceGetAttribute");
-        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::fast_sieve_kernel,
-                                                                 dev::kFThreads, fast_smem),
+        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, dev::kFThreads,
+                                                                 fast_smem),
                    "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
         grid = std::max(1, sms * std::max(1, per_sm));
-        // Word dimension of a launch: class words (64 sites spaced 64 apart).
+        // Word dimension of a launch: class words (64 sites spaced M apart).
         const long long sites = 2 * bound + 1;
-        words = (sites / 64 + 1 + 63) / 64;
+        words = (sites / M + 1 + 63) / 64;
         max_tile = dev::kFMaxClassWords;
         timings.table_wall_ms += ms_since(t0);
+    }
+
+    static const void *fast_kernel_ptr(int slots) {
+        switch (slots) {
+        case 1: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<1>);
+        case 2: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<2>);
+        case 3: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<3>);
+        case 4: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<4>);
+        case 5: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<5>);
+        default: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<6>);
+        }
+    }
+
+    void launch_fast(const dev::FastTables &Fl, const dev::SieveArgs &A, unsigned long long *work,
+                     cudaStream_t st) const {
+        const int blocks = int(std::min<long long>(grid, (A.k_count + dev::kFFetch - 1) / dev::kFFetch));
+        switch (Fl.slots) {
+        case 1: dev::fast_sieve_kernel<1><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
+        case 2: dev::fast_sieve_kernel<2><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
+        case 3: dev::fast_sieve_kernel<3><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
+        case 4: dev::fast_sieve_kernel<4><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
+        case 5: dev::fast_sieve_kernel<5><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
+        default: dev::fast_sieve_kernel<6><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
+        }
     }
 
     dev::SieveArgs args(int which, long long first, long long last, long long w_lo, long long w_hi) {
@@ -602,8 +648,7 @@ struct Sieve::Impl {
             for (int i = 0; i < kCandidatePrimes; ++i)
                 Fl.prime[i].wlo_mod = dev::u32(A.w_lo % Fl.prime[i].p);
             for (int i = 0; i < Fl.slots; ++i) Fl.mod[i].wlo_mod = dev::u32(A.w_lo % Fl.mod[i].m);
-            const int blocks = int(std::min<long long>(grid, (A.k_count + dev::kFFetch - 1) / dev::kFFetch));
-            dev::fast_sieve_kernel<<<blocks, dev::kFThreads, fast_smem, stream>>>(Fl, A, work);
+            launch_fast(Fl, A, work, stream);
         } else {
             const int blocks = int(std::min<long long>(grid, A.k_count));
             dev::ref_sieve_kernel<<<blocks, dev::kThreads, dev::kRefSmem, stream>>>(T, A);
@@ -806,29 +851,43 @@ unsigned long long Sieve::swept_words(long long first, long long last) const {
     const auto &I = *impl_;
     if (last < first) return 0;
     if (I.opt.plan != PlanKind::fast) return (unsigned long long)(last - first + 1) * I.words;
-    // Denominators per residue mod 64, then the words of each admissible class.
-    unsigned long long per_residue[64] = {};
-    for (int t = 0; t < 64; ++t) {
-        // parameters k in [first, last] with k = t (mod 64)
-        long long lo = first + ((t - first % 64) % 64 + 64) % 64;
-        unsigned long long n = lo > last ? 0 : (unsigned long long)((last - lo) / 64 + 1);
-        const int dres = I.opt.square ? int((long long)t * t % 64) : t;
+    // Denominators per residue mod M, then the words of each admissible class.
+    const int q = I.F.class_prime;
+    const long long M = I.F.class_mod;
+    std::vector<unsigned long long> per_residue(M, 0);
+    for (long long t = 0; t < M; ++t) {
+        const long long lo = first + ((t - first % M) % M + M) % M;  // first k >= first, k = t (mod M)
+        const unsigned long long n = lo > last ? 0 : (unsigned long long)((last - lo) / M + 1);
+        const long long dres = I.opt.square ? (t * t) % M : t;
         per_residue[dres] += n;
     }
     const long long sites = 2 * I.bound + 1;
     unsigned long long total = 0;
-    for (int dres = 0; dres < 64; ++dres) {
+    for (long long dres = 0; dres < M; ++dres) {
         if (!per_residue[dres]) continue;
+        const dev::u64 c2 = I.fast_adm_host[dres % 64];
+        const dev::u64 cq = q > 1 ? I.fast_adm_host[64 + dres % q] : 1;
         unsigned long long words = 0;
-        for (int r = 0; r < 64; ++r) {
-            if (!((I.fast_adm_host[dres] >> r) & 1)) continue;
-            const long long ofs = (r + I.bound % 64) % 64;
-            const long long count = ofs < sites ? (sites - 1 - ofs) / 64 + 1 : 0;
+        for (int r = 0; r < M; ++r) {
+            if (!((c2 >> (r % 64)) & 1)) continue;
+            if (q > 1 && !((cq >> (r % q)) & 1)) continue;
+            const long long ofs = (r + I.bound % M) % M;
+            const long long count = ofs < sites ? (sites - 1 - ofs) / M + 1 : 0;
             words += (unsigned long long)((count + 63) / 64);
         }
         total += per_residue[dres] * words;
     }
     return total;
+}
+
+FastPlanInfo Sieve::fast_plan_info() const {
+    FastPlanInfo info;
+    if (impl_->opt.plan != PlanKind::fast) return info;
+    info.class_prime = impl_->fast_plan.class_prime;
+    info.moduli = impl_->fast_plan.moduli;
+    for (const auto &f : impl_->fast_plan.slots)
+        for (int p : f) info.primes.push_back(p);
+    return info;
 }
 
 int Sieve::device() const { return impl_->device; }
@@ -851,9 +910,7 @@ bool Sieve::launch_into(long long first, long long last, long long *out_a, int *
     A.out_count = out_count;
     A.capacity = capacity;
     if (I.opt.plan == PlanKind::fast) {
-        const int blocks =
-            int(std::min<long long>(I.grid, (A.k_count + dev::kFFetch - 1) / dev::kFFetch));
-        dev::fast_sieve_kernel<<<blocks, dev::kFThreads, I.fast_smem, stream>>>(I.F, A, work);
+        I.launch_fast(I.F, A, work, stream);
     } else {
         const int blocks = int(std::min<long long>(I.grid, A.k_count));
         dev::ref_sieve_kernel<<<blocks, dev::kThreads, dev::kRefSmem, stream>>>(I.T, A);

@@ -58,6 +58,13 @@ struct SieveTimings {
     unsigned long long d2h_bytes = 0;
 };
 
+// The fast plan a sieve chose for its curve (empty for the reference plan).
+struct FastPlanInfo {
+    int class_prime = 0;           // numerator classes are taken mod 64 * class_prime
+    std::vector<int> primes;       // small primes tested by the stage-1 rows
+    std::vector<int> moduli;       // the stage-1 row moduli (products of those primes)
+};
+
 class Sieve {
 public:
     Sieve(const std::vector<std::string> &coefficients, long long bound, const SieveOptions &options);
@@ -85,6 +92,7 @@ public:
     // sieve kernel and shared-memory bytes read per swept word (stage 1).
     unsigned long long swept_words(long long first, long long last) const;
     unsigned smem_bytes_per_word() const;
+    FastPlanInfo fast_plan_info() const;
 
     // Enqueue one sieve launch for parameters [first, last] (at most one batch
     // of 65536) on `stream`, writing survivors into caller-owned device arrays

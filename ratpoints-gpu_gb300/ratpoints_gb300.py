@@ -118,6 +118,10 @@ def load():
     lib.rpg_session_work.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                      ctypes.POINTER(ctypes.c_uint64),
                                      ctypes.POINTER(ctypes.c_uint32)]
+    lib.rpg_session_plan.restype = S
+    lib.rpg_session_plan.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                     ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
+                                     ctypes.POINTER(ctypes.c_int32)]
     lib.rpg_session_destroy.restype = None
     lib.rpg_session_destroy.argtypes = [ctypes.c_void_p]
     lib.rpg_device_count.restype = ctypes.c_int32
@@ -245,6 +249,15 @@ class Session:
         _check(load().rpg_session_count(self._handle, int(first), int(last), int(batch_size),
                                         ctypes.byref(n), ctypes.byref(ms)))
         return n.value, ms.value
+
+    def plan(self):
+        """(class_prime, [small primes of the stage-1 rows]) of a fast-plan session."""
+        cp = ctypes.c_int32(0)
+        count = ctypes.c_int32(0)
+        primes = (ctypes.c_int32 * 64)()
+        _check(load().rpg_session_plan(self._handle, ctypes.byref(cp), primes, 64,
+                                       ctypes.byref(count)))
+        return cp.value, [primes[i] for i in range(count.value)]
 
     def work(self, first, last):
         """(64-site words swept, shared-memory bytes per swept word) of a pass."""

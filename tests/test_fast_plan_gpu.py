@@ -1,8 +1,9 @@
 """Fast plan parity: its survivor set is exactly the reference plan's survivor
 set intersected with the extra filters the fast plan documents (2-adic
-classes mod 64 with gcd parity, and f(a/d) a square mod each small prime
-3..37, or gcd and the leading-coefficient test when the prime divides d).
-Every extra filter holds for every point, so the point sets are equal."""
+classes mod 64 with gcd parity, and f(a/d) a square mod each small prime the
+per-curve plan chose, or gcd and the leading-coefficient test when the prime
+divides d).  Every extra filter holds for every point, so the point sets are
+equal."""
 
 import math
 import random
@@ -11,15 +12,18 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-SMALL_PRIMES = [3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37]
+def plan_primes(rpg, coeffs, bound):
+    with rpg.Session(coeffs, bound, plan="fast") as session:
+        class_prime, primes = session.plan()
+    return sorted(set(primes) | ({class_prime} if class_prime > 1 else set()))
 
 
-def fast_filter(coeffs, square_test_cache=None):
+def fast_filter(coeffs, small_primes):
     c = [int(x) for x in coeffs]
     n = len(c) - 1
     squares64 = {v * v % 64 for v in range(64)}
-    sq = {q: {v * v % q for v in range(q)} for q in SMALL_PRIMES}
-    lead_ok = {q: (n % 2 == 1) or (c[-1] % q in sq[q]) for q in SMALL_PRIMES}
+    sq = {q: {v * v % q for v in range(q)} for q in small_primes}
+    lead_ok = {q: (n % 2 == 1) or (c[-1] % q in sq[q]) for q in small_primes}
 
     def F_mod(a, d, m):
         value = sum(ci * pow(a, i, m) * pow(d, n - i, m) for i, ci in enumerate(c)) % m
@@ -30,7 +34,7 @@ def fast_filter(coeffs, square_test_cache=None):
             return False
         if F_mod(a % 64, d % 64, 64) not in squares64:
             return False
-        for q in SMALL_PRIMES:
+        for q in small_primes:
             if d % q == 0:
                 if a % q == 0 or not lead_ok[q]:
                     return False
@@ -51,7 +55,7 @@ def check(rpg, oracle, coeffs, bound, first, last, square=False):
     sieve = oracle.ModularSieve(coeffs, bound)
     ref = sieve.survivors(first, last, square)
     sieve.close()
-    passes = fast_filter(coeffs)
+    passes = fast_filter(coeffs, plan_primes(rpg, coeffs, bound))
     expected = [(x, y) for x, y in ref if passes(x, y)]
     assert got == expected, (coeffs, bound, first, last, len(got), len(expected))
     return got
@@ -96,6 +100,23 @@ def test_fast_plan_small_buffers(rpg, oracle, golden, monkeypatch):
     monkeypatch.setenv("RPG_SURVIVOR_CAPACITY", "64")
     dense = golden["dense"]
     check(rpg, oracle, dense["coefficients"].split(), 5000, 1, 2)
+
+
+def test_plan_choice_for_the_benchmark_curve(rpg):
+    import bench
+    coeffs = bench.c2_curve()
+    with rpg.Session(coeffs, 5_000_000, plan="fast") as session:
+        class_prime, primes = session.plan()
+    # strong small primes for this curve: 5, 7, 11 (f(x) mod 3 is always a square)
+    assert class_prime in (5, 7, 11)
+    assert 3 not in primes and 13 not in primes and class_prime not in primes
+    assert 61 in primes
+
+
+def test_fast_plan_large_height(rpg, oracle):
+    # class prime in use (long classes), last-word clipping per class
+    check(rpg, oracle, ["247747600", "-985905640", "567207969", "2396040466", "52485681",
+                        "-470135160", "82342800"], 3_000_003, 1, 40)
 
 
 def test_fast_plan_keeps_every_point(rpg, oracle):
