@@ -29,6 +29,8 @@ rpg_status guarded(F &&body) {
     try {
         g_last_error.clear();
         return body();
+    } catch (const rpg::DeviceTimeout &e) {
+        return fail(RPG_E_TIMEOUT, e.what());
     } catch (const rpg::CudaError &e) {
         const std::string what = e.what();
         if (what.find("out of memory") != std::string::npos) return fail(RPG_E_OOM, what);

@@ -258,7 +258,7 @@ struct Sieve::Impl {
     struct Buffer {
         long long *a = nullptr;
         int *d = nullptr;
-        unsigned long long *count = nullptr;  // [0] survivors, [1] work counter
+        unsigned long long *count = nullptr;  // [0] survivors, [1] work counter, [2] error word
         cudaEvent_t begin = nullptr, end = nullptr;
         long long first = 0, last = 0;
         bool busy = false;
@@ -395,7 +395,7 @@ struct Sieve::Impl {
         for (auto &b : buf) {
             b.a = device_alloc<long long>(std::size_t(capacity), "cudaMalloc(survivors)");
             b.d = device_alloc<int>(std::size_t(capacity), "cudaMalloc(survivors)");
-            b.count = device_alloc<unsigned long long>(2, "cudaMalloc(count)");
+            b.count = device_alloc<unsigned long long>(3, "cudaMalloc(count)");
             check_cuda(cudaEventCreate(&b.begin), "cudaEventCreate");
             check_cuda(cudaEventCreate(&b.end), "cudaEventCreate");
         }
@@ -498,6 +498,13 @@ struct Sieve::Impl {
         F.h_mod_m = int(bound % M);
         F.inv64_q = q > 1 ? int(mod_inverse(64 % q, q)) : 0;
         F.stride = S;
+        F.count_q = (2 * bound) / M;
+        F.count_r = int((2 * bound) % M);
+        for (int r64 = 0; r64 < 64; ++r64) F.mod_q[r64] = (unsigned char)(q > 1 ? r64 % q : 0);
+        if (q > 1)
+            for (int a = 0; a < q; ++a)
+                for (int rq = 0; rq < q; ++rq)
+                    F.crt[a * 13 + rq] = (unsigned char)(((rq - a + q) % q) * F.inv64_q % q);
         // Admissible classes: 2-adic by d mod 64 (F(r, d) square mod 64, r odd
         // when d is even), then residues r mod q by d mod q.
         std::vector<int> c64(coefficients.size());
@@ -630,6 +637,7 @@ struct Sieve::Impl {
         A.out_d = buf[which].d;
         A.out_count = buf[which].count;
         A.capacity = (unsigned long long)capacity;
+        A.error = buf[which].count + 2;
         return A;
     }
 
@@ -662,7 +670,7 @@ struct Sieve::Impl {
         b.last = last;
         b.busy = true;
         const dev::SieveArgs A = args(which, first, last, w_lo, w_hi);
-        check_cuda(cudaMemsetAsync(b.count, 0, 2 * sizeof(unsigned long long), stream),
+        check_cuda(cudaMemsetAsync(b.count, 0, 3 * sizeof(unsigned long long), stream),
                    "cudaMemsetAsync");
         check_cuda(cudaEventRecord(b.begin, stream), "cudaEventRecord");
         launch_kernel(A, b.count + 1);
@@ -687,6 +695,14 @@ struct Sieve::Impl {
             launch(which, first, last, 0, words);
             order.push_back(which);
         }
+    }
+
+    // Raise if a launch into buffer `which` reported a timed-out device wait.
+    void check_error_word(int which) {
+        unsigned long long err = 0;
+        check_cuda(cudaMemcpy(&err, buf[which].count + 2, sizeof err, cudaMemcpyDeviceToHost),
+                   "download error word");
+        if (err) throw DeviceTimeout("sieve kernel: bounded wait for a row copy timed out");
     }
 
     float elapsed(const Buffer &b) {
@@ -753,6 +769,7 @@ struct Sieve::Impl {
             launch(which, p.first, p.last, p.w_lo, p.w_hi);
             check_cuda(cudaStreamSynchronize(stream), "sieve kernel");
             buf[which].busy = false;
+            check_error_word(which);
             const unsigned long long n = h_count[which];
             const float ms = elapsed(buf[which]);
             timings.sieve_ms += ms;
@@ -790,6 +807,7 @@ struct Sieve::Impl {
                    "download survivor count");
         check_cuda(cudaStreamSynchronize(copy_stream), "download survivor count");
         timings.d2h_bytes += sizeof n;
+        check_error_word(which);
         const float ms = elapsed(b);
         timings.sieve_ms += ms;
         if (n > (unsigned long long)capacity) {
@@ -909,6 +927,7 @@ bool Sieve::launch_into(long long first, long long last, long long *out_a, int *
     A.out_d = out_d;
     A.out_count = out_count;
     A.capacity = capacity;
+    A.error = nullptr;  // the caller's launch reports no timeouts
     if (I.opt.plan == PlanKind::fast) {
         I.launch_fast(I.F, A, work, stream);
     } else {
@@ -933,7 +952,8 @@ unsigned long long Sieve::count_only(long long first, long long last, long long 
     // Launches share buffer 0's counter: survivors past capacity are counted,
     // not stored, so the total is exact while the stores stop early.
     auto &b = I.buf[0];
-    check_cuda(cudaMemsetAsync(b.count, 0, sizeof(unsigned long long), I.stream), "cudaMemsetAsync");
+    check_cuda(cudaMemsetAsync(b.count, 0, 3 * sizeof(unsigned long long), I.stream),
+               "cudaMemsetAsync");
     for (long long f = first; f <= last; f += batch_size) {
         const long long l = std::min(last, f + batch_size - 1);
         for (long long w = 0; w < I.words; w += I.max_tile)
@@ -943,6 +963,7 @@ unsigned long long Sieve::count_only(long long first, long long last, long long 
     check_cuda(cudaMemcpyAsync(&total, b.count, sizeof total, cudaMemcpyDeviceToHost, I.stream),
                "download survivor count");
     check_cuda(cudaStreamSynchronize(I.stream), "sieve kernel");
+    I.check_error_word(0);
     return total;
 }
 

@@ -25,6 +25,12 @@ public:
     using std::runtime_error::runtime_error;
 };
 
+// A bounded wait inside a sieve kernel ran out; the launch's output is invalid.
+class DeviceTimeout : public std::runtime_error {
+public:
+    using std::runtime_error::runtime_error;
+};
+
 void check_cuda(cudaError_t status, const char *what);
 
 struct SieveOptions {

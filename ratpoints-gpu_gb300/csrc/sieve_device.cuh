@@ -32,6 +32,7 @@ struct SieveArgs {
     int *out_d;
     unsigned long long *out_count;
     unsigned long long capacity;
+    unsigned long long *error;   // set nonzero if a bounded device wait ran out (may be null)
 };
 
 // Largest 32-bit quotient estimate used for n mod p with n < 2^31 and p < 2^9:

@@ -76,6 +76,10 @@ struct FastTables {
     int h_mod_m;                   // H mod M
     int inv64_q;                   // 64^-1 mod q (CRT), 0 when q = 1
     long long stride;              // S = 64 M: numerator step between words of a class
+    long long count_q;             // 2H = count_q * M + count_r: a class with offset
+    int count_r;                   //   ofs <= count_r holds count_q + 1 sites, else count_q
+    unsigned char crt[13 * 13];    // [r64 mod q][rq] -> t with r = r64 + 64 t (mod 64 q)
+    unsigned char mod_q[64];       // r64 mod q
     FastModulus mod[kFastSlots];
     FastPrime prime[kCandidatePrimes];
     int slots;                     // stage-1 moduli in use
@@ -86,6 +90,44 @@ __device__ __forceinline__ u32 mod_u32(u32 n, u32 m, unsigned long long magic) {
     u32 q = u32(__umul64hi((unsigned long long)n, magic));
     u32 r = n - q * m;
     return r >= m ? r - m : r;
+}
+
+// Shared-memory address, mbarrier and bulk-copy (TMA, non-tensor) helpers.
+__device__ __forceinline__ u32 smem_addr(const void *p) {
+    return u32(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(u32 bar, u32 count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(u32 bar, u32 bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(u32 bar, u32 parity) {
+    u32 done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
+        "selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Bounded wait for the phase with the given parity; false if the limit ran out.
+__device__ __forceinline__ bool mbar_wait(u32 bar, u32 parity) {
+    for (int i = 0; i < (1 << 24); ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_copy_to_shared(u32 dst, const void *src, u32 bytes, u32 bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_shared() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 // Position of the n-th set bit (n counted from 0) of a 64-bit mask.
@@ -204,7 +246,7 @@ __device__ __forceinline__ void fast_drain(const u64 *qmask, const u32 *qinfo, i
 }
 
 template <int NS>
-__global__ void __launch_bounds__(kFThreads) fast_sieve_kernel(FastTables T, SieveArgs A,
+__global__ void __launch_bounds__(kFThreads, 3) fast_sieve_kernel(FastTables T, SieveArgs A,
                                                                unsigned long long *work) {
     extern __shared__ __align__(16) u64 smem[];
     u64 *rows = smem;
@@ -222,6 +264,8 @@ __global__ void __launch_bounds__(kFThreads) fast_sieve_kernel(FastTables T, Sie
     __shared__ int s_sel[kSelectedPrimes];
     __shared__ long long s_prow[kSelectedPrimes];
     __shared__ int s_next;
+    __shared__ int s_abort;
+    __shared__ __align__(8) unsigned long long s_bar;   // row-copy completion
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -231,6 +275,15 @@ __global__ void __launch_bounds__(kFThreads) fast_sieve_kernel(FastTables T, Sie
     const int q = T.class_prime;
     const int M = T.class_mod;
     const unsigned char *sbase = reinterpret_cast<const unsigned char *>(rows);
+    const u32 rows_addr = smem_addr(rows);
+    const u32 bar = smem_addr(&s_bar);
+    u32 phase = 0;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
 
     for (;;) {
         if (threadIdx.x == 0) {
@@ -246,17 +299,31 @@ __global__ void __launch_bounds__(kFThreads) fast_sieve_kernel(FastTables T, Sie
         for (int it = 0; it < nitems; ++it) {
             const long long k = A.k_first + s_items[it];
             const long long d = A.square ? k * k : k;
-            const u64 classes2 = __ldg(T.admissible + (d & 63));
-            const u64 classesq = q > 1 ? __ldg(T.admissible + 64 + int(d % q)) : u64(1);
+            const u32 du = u32(d);  // d < 2^31 (k <= INT_MAX, or k <= 46340 when square)
+            const u64 classes2 = __ldg(T.admissible + (du & 63));
+            const u64 classesq = q > 1 ? __ldg(T.admissible + 64 + int(du % u32(q))) : u64(1);
             if (!classes2 || !classesq) continue;
             const int nq = __popcll(classesq);
             const int nclass = __popcll(classes2) * nq;
 
             // ---- per-denominator setup ----
+            // Thread 0 starts the bulk copies of this denominator's stage-1 rows
+            // (all rows are contiguous in shared memory: one transaction count).
+            if (threadIdx.x == 0) {
+                fence_proxy_async_shared();
+                mbar_arrive_expect_tx(bar, u32(T.smem_words) * 8u);
+#pragma unroll
+                for (int sl = 0; sl < NS; ++sl) {
+                    const FastModulus &Md = T.mod[sl];
+                    const u32 rho = mod_u32(du, u32(Md.m), Md.magic);
+                    bulk_copy_to_shared(rows_addr + u32(Md.smem_offset) * 8u,
+                                        T.rows + Md.offset + (long long)rho * Md.length,
+                                        u32(Md.length) * 8u, bar);
+                }
+            }
             if (warp == 0) {
-                // The 32 largest candidates not dividing d (d < 2^31): lane l tests
+                // The 32 largest candidates not dividing d: lane l tests
                 // candidate 35 - l, lanes 0..3 also candidate 3 - l.
-                const u32 du = u32(d);
                 const int ch = kCandidatePrimes - 1 - lane;
                 const u32 rh = du % u32(T.prime[ch].p);
                 const u32 hi_div = __ballot_sync(kFullMask, rh == 0);
@@ -275,57 +342,60 @@ __global__ void __launch_bounds__(kFThreads) fast_sieve_kernel(FastTables T, Sie
                     s_prow[rank_l] = T.prime[cl].offset + (long long)rl * T.prime[cl].p;
                 }
                 if (lane == 0) s_next = 0;
-            }
-            for (int c = threadIdx.x; c < nclass; c += kFThreads) {
-                // class c = (c / nq)-th 2-adic class crossed with the (c % nq)-th residue mod q
-                const int r64 = nth_set_bit(classes2, c / nq);
-                int r = r64;
-                if (q > 1) {
-                    const int rq = nth_set_bit(classesq, c % nq);
-                    r = r64 + 64 * (((rq - r64 % q + q) % q) * T.inv64_q % q);
-                }
-                int ofs = r + T.h_mod_m;
-                if (ofs >= M) ofs -= M;
-                // sites of class r: a = -H + ofs + M t, t in [0, count)
-                const long long count = ofs < sites_total ? (sites_total - 1 - ofs) / M + 1 : 0;
-                const long long words = (count + 63) / 64;
-                const long long lo = A.w_lo < words ? A.w_lo : words;
-                const long long hi = A.w_hi < words ? A.w_hi : words;
-                s_ofs[c] = u32(ofs);
-                s_wtile[c] = int(hi - lo);
-                const bool has_last = hi == words && words > 0 && hi > lo;
-                s_last_word[c] = has_last ? int(words - 1 - lo) : -1;
-                s_last_bits[c] = has_last ? int(count - 64 * (words - 1)) : 64;
+            } else if (warp == 1) {
+                // Classes, 32 per pass: class c = (c / nq)-th 2-adic class crossed
+                // with the (c % nq)-th admissible residue mod q; item prefix by scan.
+                int carry = 0;
+                for (int base = 0; base < nclass; base += 32) {
+                    const int c = base + lane;
+                    int items = 0;
+                    if (c < nclass) {
+                        const int r64 = nth_set_bit(classes2, c / nq);
+                        int r = r64;
+                        if (q > 1) {
+                            const int rq = nth_set_bit(classesq, c % nq);
+                            r = r64 + 64 * int(T.crt[T.mod_q[r64] * 13 + rq]);
+                        }
+                        int ofs = r + T.h_mod_m;
+                        if (ofs >= M) ofs -= M;
+                        // sites of class r: a = -H + ofs + M t, t in [0, count)
+                        const long long count = T.count_q + (ofs <= T.count_r ? 1 : 0);
+                        const long long words = (count + 63) >> 6;
+                        const long long lo = A.w_lo < words ? A.w_lo : words;
+                        const long long hi = A.w_hi < words ? A.w_hi : words;
+                        const int wt = int(hi - lo);
+                        s_ofs[c] = u32(ofs);
+                        s_wtile[c] = wt;
+                        const bool has_last = hi == words && words > 0 && hi > lo;
+                        s_last_word[c] = has_last ? int(words - 1 - lo) : -1;
+                        s_last_bits[c] = has_last ? int(count - 64 * (words - 1)) : 64;
 #pragma unroll
-                for (int sl = 0; sl < NS; ++sl) {
-                    // row index of tile word 0: (a0 * S^-1 + w_lo) mod m, a0 = -H + ofs
-                    const FastModulus &Md = T.mod[sl];
-                    const u32 a0m = mod_u32(Md.neg_h + u32(ofs), u32(Md.m), Md.magic);
-                    s_start[c * NS + sl] =
-                        mod_u32(a0m * Md.inv_stride + Md.wlo_mod, u32(Md.m), Md.magic);
+                        for (int sl = 0; sl < NS; ++sl) {
+                            // row index of tile word 0: (a0 * S^-1 + w_lo) mod m, a0 = -H + ofs
+                            const FastModulus &Md = T.mod[sl];
+                            const u32 a0m = mod_u32(Md.neg_h + u32(ofs), u32(Md.m), Md.magic);
+                            s_start[c * NS + sl] =
+                                mod_u32(a0m * Md.inv_stride + Md.wlo_mod, u32(Md.m), Md.magic);
+                        }
+                        items = (wt + kFItemWords - 1) / kFItemWords;
+                    }
+                    int incl = items;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int v = __shfl_up_sync(kFullMask, incl, o);
+                        if (lane >= o) incl += v;
+                    }
+                    if (c < nclass) s_prefix[c] = carry + incl - items;
+                    carry += __shfl_sync(kFullMask, incl, 31);
                 }
+                if (lane == 0) s_prefix[nclass] = carry;
             }
             __syncthreads();
-            if (threadIdx.x == 0) {
-                int acc = 0;
-                for (int c = 0; c < nclass; ++c) {
-                    s_prefix[c] = acc;
-                    acc += (s_wtile[c] + kFItemWords - 1) / kFItemWords;
-                }
-                s_prefix[nclass] = acc;
+            if (!mbar_wait(bar, phase)) {  // rows landed (bounded wait)
+                s_abort = 1;
+                if (A.error) atomicOr(A.error, 1ull);
             }
-            // stage the stage-1 rows of this denominator
-#pragma unroll
-            for (int sl = 0; sl < NS; ++sl) {
-                const FastModulus &Md = T.mod[sl];
-                const int rho = int(d % Md.m);
-                const uint4 *src =
-                    reinterpret_cast<const uint4 *>(T.rows + Md.offset + (long long)rho * Md.length);
-                uint4 *dst = reinterpret_cast<uint4 *>(rows + Md.smem_offset);
-                const int n16 = Md.length >> 1;
-                for (int t = threadIdx.x; t < n16; t += kFThreads) dst[t] = __ldg(src + t);
-            }
-            __syncthreads();
+            phase ^= 1u;
 
             // ---- sweep: warps take work items (class, 512-word chunk) ----
             const int total_items = s_prefix[nclass];
@@ -410,6 +480,12 @@ __global__ void __launch_bounds__(kFThreads) fast_sieve_kernel(FastTables T, Sie
             __syncwarp();
             fast_drain(wq_mask, wq_info, 0, qn, T, A, int(d), s_sel, s_prow, s_ofs);
             __syncthreads();
+            if (s_abort) {
+                // a bulk copy did not complete in time: give in-flight copies a
+                // last bounded chance to land, then leave (the host reports it)
+                if (threadIdx.x == 0) mbar_wait(bar, phase ^ 1u);
+                return;
+            }
         }
         __syncthreads();
     }
