@@ -183,6 +183,55 @@ rpg_status rpg_session_sieve_noalloc(rpg_session *session, int32_t first, int32_
                                      int64_t *device_numerators, int32_t *device_denominators,
                                      uint64_t capacity, uint64_t *device_count, void *stream);
 
+/*
+ * Batched search of many curves in one pass: every curve's tables resident on
+ * the device, two persistent sieve kernels over device work queues, one
+ * captured CUDA graph.  No counterpart in the reference, which searches one
+ * curve per process (src/main.cpp:48-85); each curve's points are exactly
+ * what rpg_point_search reports for the same options, in the same order.
+ *
+ * Each curves[i] is read as by rpg_point_search; batch_size, plan, device
+ * and verify_threads are ignored (the batch has its own plan and uses
+ * `device`).  callback(i, ...) receives curve i's points in order, curves in
+ * input order; returning 0 stops the delivery of curve i's remaining points
+ * (as a single search stops).  curve_status[i] (optional) receives
+ * RPG_OK, RPG_E_ARG or RPG_E_NOT_SQUAREFREE for curve i; a failing curve
+ * gets no points and does not fail the call.  curve_survivors[i] (optional)
+ * receives the modular survivors of curve i.  The call fails only for a NULL
+ * argument, a negative count, or a device error.
+ */
+#define RPG_BATCH_NO_GRAPH 1u /* launch the batch's kernels directly, not as a CUDA graph */
+
+typedef struct rpg_batch_stats {
+    uint64_t curves;           /* curves searched (valid, with denominators) */
+    uint64_t wide_curves;      /* of those, swept by the class-layout kernel */
+    uint64_t denominators;
+    uint64_t survivors;        /* modular survivors of all curves */
+    uint64_t points;           /* verified points of all curves, infinity included */
+    uint64_t launches;         /* kernel launches (table build and sieve) */
+    uint64_t words;            /* 64-site row words of all denominators */
+    uint64_t table_words;      /* stage-1 table words resident on the device */
+    double rectangle_sites;    /* sum over curves of (2H + 1) x denominators */
+    double plan_ms;            /* host: validation, plans, descriptors */
+    double table_ms;           /* device table build, CUDA events */
+    double sieve_ms;           /* both sieve kernels, CUDA events */
+    double wide_ms;
+    double narrow_ms;
+    double verify_ms;          /* host exact verification */
+    double wall_ms;            /* the whole call */
+    uint64_t h2d_bytes;
+    uint64_t d2h_bytes;
+    int32_t graph;             /* nonzero if the kernels ran as a CUDA graph */
+} rpg_batch_stats;
+
+typedef int (*rpg_batch_point_cb)(int32_t curve, int64_t numerator, const char *ordinate,
+                                  int64_t denominator, void *user);
+
+rpg_status rpg_batch_search(const rpg_search_options *curves, int32_t curve_count, int32_t device,
+                            uint32_t flags, rpg_batch_point_cb callback, void *user,
+                            int32_t *curve_status, uint64_t *curve_survivors,
+                            rpg_batch_stats *stats);
+
 int32_t rpg_device_count(void);
 int32_t rpg_abi_version(void);
 const char *rpg_last_error(void);

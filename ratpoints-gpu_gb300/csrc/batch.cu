@@ -1,0 +1,1350 @@
+// Batched many-curve sieve (batch.hpp): device kernels and host driver.
+#include "batch.hpp"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <thread>
+
+#include "exact.hpp"
+#include "plan.hpp"
+#include "sieve.hpp"
+#include "sieve_device.cuh"
+
+namespace rpg {
+namespace dev {
+
+constexpr int kWideSlots = kMaxFastSlots;          // stage-1 moduli of a wide curve (padded)
+constexpr int kWK = 4;                             // words per lane per step (lanes 32 apart)
+constexpr int kWWarps = 8;
+constexpr int kWThreads = kWWarps * kWarpSize;
+constexpr int kWSteps = 4;
+constexpr int kWItemWords = kWarpSize * kWK * kWSteps;  // class words per sweep item
+constexpr int kWExt = kWarpSize * (kWK - 1);            // row extension
+constexpr int kWMaxSmemWords = 5800;                    // staged row words (3 CTAs per SM)
+constexpr int kQueue = 64;
+constexpr int kClassBits = 8;
+constexpr int kMaxClasses = kMaxFastClasses;
+constexpr long long kMaxClassWords = 1LL << 23;         // class word index fits 24 bits
+constexpr int kAdmQ = 16;                               // residue words for class primes <= 13
+constexpr int kNarrowSlots = 6;
+constexpr int kNWarps = 8;
+constexpr int kNThreads = kNWarps * kWarpSize;
+constexpr int kNarrowTableWords = 8192;                 // sum of m^2 (+ padding) per curve
+constexpr int kRefWords = 8;                            // u64 words of a bitmask over [0, 512)
+constexpr int kMaxFactors = 4;
+
+static_assert(kMaxClasses <= (1 << kClassBits), "class index must fit the queue entry");
+
+struct Modulus {                   // one stage-1 modulus of a wide curve (class layout)
+    long long offset;              // word offset of row 0 in the table pool
+    unsigned long long magic;      // mod_u32 constant (all ones for m = 1)
+    int m;
+    int length;                    // row length in words (m + kWExt, even)
+    int smem_offset;               // word offset of the staged row
+    u32 inv_stride;                // S^-1 mod m
+    u32 neg_h;                     // (-H) mod m
+    u32 step;                      // (32 kWK) mod m
+};
+
+struct WideCurve {
+    long long bound;               // H
+    long long stride;              // S = 64 M: numerator step between words of a class
+    long long count_q;             // 2H = count_q M + count_r
+    long long aff;                 // u64 offset of the 36 candidate bitmasks
+    Modulus mod[kWideSlots];
+    u64 admissible[64 + kAdmQ];    // 2-adic classes by d mod 64, residues mod q by d mod q
+    int count_r;
+    int class_prime;               // q (1: 2-adic classes only)
+    int class_mod;                 // M = 64 q
+    int h_mod_m;                   // H mod M
+    int inv64_q;                   // 64^-1 mod q (CRT)
+    int smem_words;
+    int square;
+    int index;                     // position in the caller's curve list
+    unsigned short neg_h[kCandidatePrimes];   // (-H) mod p
+    unsigned short s_mod[kCandidatePrimes];   // S mod p
+    unsigned short m_mod[kCandidatePrimes];   // M mod p
+    unsigned char crt[13 * 13];    // [r64 mod q][rq] -> t with r = r64 + 64 t (mod 64 q)
+    unsigned char mod_q[64];       // r64 mod q
+};
+
+struct NarrowCurve {
+    long long bound;
+    long long words;               // W: dense 64-site words per denominator row
+    long long tables;              // word offset of the curve's table block (even)
+    long long aff;
+    unsigned long long magic[kNarrowSlots];
+    u64 dense2[64];                // by d mod 64: bit j set iff a = -H + j (mod 64) may hold points
+    int table_words;               // even
+    int square;
+    int index;
+    int m[kNarrowSlots];           // moduli (1: padding)
+    int off[kNarrowSlots];         // word offset of each table inside the block
+    u32 shift[kNarrowSlots];       // (-H) 64^-1 mod m: table word of row word 0
+    u32 step[kNarrowSlots];        // 32 mod m
+    unsigned short neg_h[kCandidatePrimes];
+};
+
+static_assert(sizeof(WideCurve) % 4 == 0 && sizeof(NarrowCurve) % 4 == 0, "u32 copies");
+
+struct BatchItem {
+    long long first;               // first parameter k
+    int curve;                     // descriptor index
+    int count;                     // parameters in this item
+};
+
+struct AffineSpec {                // bitmask of x in [0, p) with f(x) a square mod p
+    long long out;                 // u64 offset of the 8-word output
+    long long residues;            // offset of c_0 .. c_n mod p
+    int p, n;
+};
+
+struct PatternSpec {               // q x q words: bit j of word (rho, u) tests x = (s u + t j) mod q
+    long long offset;
+    long long aff;
+    int q, lead_ok, s, t;
+};
+
+struct CompositeSpec {             // m rows of `length` words: AND of the factor patterns
+    long long offset;
+    long long pattern[kMaxFactors];
+    int m, length, nf;
+    int q[kMaxFactors];
+};
+
+struct BatchOut {
+    long long *a;
+    int *d;
+    int *curve;
+    unsigned long long *count;
+    unsigned long long capacity;
+    unsigned long long *error;
+};
+
+struct Candidates {
+    int p[kCandidatePrimes];
+    u32 magic[kCandidatePrimes];
+};
+
+// ---------------------------------------------------------------------------
+// Table construction
+
+__global__ void affine_kernel(const AffineSpec *specs, long long nspecs,
+                              const unsigned short *residues, const u64 *square_masks, u64 *out) {
+    const long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (id >= nspecs * kRefWords) return;
+    const AffineSpec S = specs[id / kRefWords];
+    const int k = int(id % kRefWords);
+    const int p = S.p;
+    const unsigned short *c = residues + S.residues;
+    const u64 *sq = square_masks + (long long)p * kRefWords;
+    u64 word = 0;
+    for (int b = 0; b < 64; ++b) {
+        const int x = 64 * k + b;
+        if (x >= p) break;
+        int v = c[S.n];
+        for (int i = S.n - 1; i >= 0; --i) v = (v * x + c[i]) % p;
+        if ((sq[v >> 6] >> (v & 63)) & 1) word |= u64(1) << b;
+    }
+    out[S.out + k] = word;
+}
+
+// Index of the last spec whose offset is <= id (specs sorted by offset).
+template <typename Spec>
+__device__ __forceinline__ int find_spec(const Spec *specs, int nspecs, long long id) {
+    int lo = 0, hi = nspecs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (specs[mid].offset <= id) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void pattern_kernel(const PatternSpec *specs, int nspecs, const u64 *affine,
+                               const unsigned short *inv_table, u64 *patterns, long long total) {
+    const long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (id >= total) return;
+    const PatternSpec S = specs[find_spec(specs, nspecs, id)];
+    const int q = S.q;
+    const int rel = int(id - S.offset);
+    const int rho = rel / q;
+    const int u = rel % q;
+    const u64 *aff = affine + S.aff;
+    const int inv = rho ? inv_table[q * kMaximumPrime + rho] : 0;
+    int x = (S.s * u) % q;
+    u64 word = 0;
+    for (int j = 0; j < 64; ++j) {
+        bool ok;
+        if (rho == 0) {
+            ok = x != 0 && S.lead_ok;  // q | d: q !| a, and c_n a square mod q for even degree
+        } else {
+            const int y = (x * inv) % q;
+            ok = (__ldg(aff + (y >> 6)) >> (y & 63)) & 1;
+        }
+        if (ok) word |= u64(1) << j;
+        x += S.t;
+        if (x >= q) x -= q;
+    }
+    patterns[id] = word;
+}
+
+__global__ void composite_kernel(const CompositeSpec *specs, int nspecs, const u64 *patterns,
+                                 u64 *rows, long long total) {
+    const long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (id >= total) return;
+    const CompositeSpec &S = specs[find_spec(specs, nspecs, id)];
+    const long long rel = id - S.offset;
+    const int rho = int(rel / S.length);
+    const int u = int(rel % S.length) % S.m;
+    u64 word = ~u64(0);
+    for (int f = 0; f < S.nf; ++f) {
+        const int q = S.q[f];
+        word &= __ldg(patterns + S.pattern[f] + (rho % q) * q + (u % q));
+    }
+    rows[id] = word;
+}
+
+// ---------------------------------------------------------------------------
+// Stage 2 and emission
+
+// The 32 largest candidates not dividing d with 1/d mod p, by one warp: lane l
+// tests candidate 35 - l, lanes 0..3 also candidate 3 - l.
+__device__ __forceinline__ void select_warp(u32 du, const Candidates &cand,
+                                            const unsigned short *inv_table, int *s_ci,
+                                            u32 *s_dinv) {
+    const int lane = threadIdx.x & 31;
+    const int ch = kCandidatePrimes - 1 - lane;
+    const u32 rh = mod_small(du, u32(cand.p[ch]), cand.magic[ch]);
+    const u32 hi_div = __ballot_sync(kFullMask, rh == 0);
+    const int cl = kCandidatePrimes - 1 - 32 - lane;
+    const u32 rl = lane < kCandidatePrimes - 32 ? mod_small(du, u32(cand.p[cl]), cand.magic[cl]) : 1u;
+    const u32 lo_div = __ballot_sync(kFullMask, rl == 0);
+    const u32 below = lanemask_lt();
+    const int rank_h = lane - __popc(hi_div & below);
+    if (rh != 0 && rank_h < kSelectedPrimes) {
+        s_ci[rank_h] = ch;
+        s_dinv[rank_h] = __ldg(inv_table + cand.p[ch] * kMaximumPrime + rh);
+    }
+    const int rank_l = 32 - __popc(hi_div) + lane - __popc(lo_div & below);
+    if (lane < kCandidatePrimes - 32 && rl != 0 && rank_l < kSelectedPrimes) {
+        s_ci[rank_l] = cl;
+        s_dinv[rank_l] = __ldg(inv_table + cand.p[cl] * kMaximumPrime + rl);
+    }
+    __syncwarp();
+}
+
+// Clears the bits j of m whose site a = base + step j fails one of the 32
+// selected primes: f(a/d) mod p must be a square.  residue(ci, p, magic)
+// returns base mod p; step_mod(ci) returns step mod p.
+template <typename Residue, typename StepMod>
+__device__ __forceinline__ u64 stage2(u64 m, const int *s_ci, const u32 *s_dinv,
+                                      const Candidates &cand, const u64 *aff, Residue residue,
+                                      StepMod step_mod) {
+    for (int s = 0; s < kSelectedPrimes && m; ++s) {
+        const int ci = s_ci[s];
+        const u32 p = u32(cand.p[ci]), magic = cand.magic[ci];
+        const u32 dinv = s_dinv[s];
+        const u32 x0 = mod_small(residue(ci, p, magic) * dinv, p, magic);
+        const u32 dx = mod_small(step_mod(ci) * dinv, p, magic);
+        const u64 *bits = aff + ci * kRefWords;
+        u64 rest = m;
+        while (rest) {
+            const int j = __ffsll((long long)rest) - 1;
+            rest &= rest - 1;
+            const u32 x = mod_small(x0 + u32(j) * dx, p, magic);
+            if (!((__ldg(bits + (x >> 6)) >> (x & 63)) & 1)) m &= ~(u64(1) << j);
+        }
+    }
+    return m;
+}
+
+// Warp-collective emission of sites a = base + step j for the set bits j of m.
+__device__ __forceinline__ void emit(u64 m, long long base, long long step, long long d, int curve,
+                                     const BatchOut &out) {
+    const int lane = threadIdx.x & 31;
+    const u32 cnt = __popcll(m);
+    if (!__any_sync(kFullMask, cnt != 0)) return;
+    u32 incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const u32 v = __shfl_up_sync(kFullMask, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const u32 total = __shfl_sync(kFullMask, incl, 31);
+    unsigned long long pos = 0;
+    if (lane == 0) pos = atomicAdd(out.count, (unsigned long long)total);
+    pos = __shfl_sync(kFullMask, pos, 0) + incl - cnt;
+    while (m) {
+        const int j = __ffsll((long long)m) - 1;
+        m &= m - 1;
+        if (pos < out.capacity) {
+            out.a[pos] = base + step * j;
+            out.d[pos] = int(d);
+            out.curve[pos] = curve;
+        }
+        ++pos;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Wide rows: class layout, one CTA per denominator.
+
+__device__ __forceinline__ void wide_drain(const u64 *qmask, const u32 *qinfo, int start, int n,
+                                           const WideCurve &C, const Candidates &cand,
+                                           const u64 *affine, const int *s_ci, const u32 *s_dinv,
+                                           const u32 *s_ofs, long long d, const BatchOut &out) {
+    const int lane = threadIdx.x & 31;
+    u64 m = 0;
+    u32 info = 0;
+    if (lane < n) {
+        m = qmask[start + lane];
+        info = qinfo[start + lane];
+    }
+    __syncwarp();
+    const u32 off = info >> kClassBits;
+    const u32 ofs = s_ofs[info & ((1u << kClassBits) - 1)];
+    if (m) {
+        m = stage2(
+            m, s_ci, s_dinv, cand, affine + C.aff,
+            [&](int ci, u32 p, u32 magic) {
+                u32 r = C.neg_h[ci] + mod_small(ofs, p, magic);
+                if (r >= p) r -= p;
+                r += mod_small(u32(C.s_mod[ci]) * mod_small(off, p, magic), p, magic);
+                return r >= p ? r - p : r;
+            },
+            [&](int ci) { return u32(C.m_mod[ci]); });
+    }
+    emit(m, -C.bound + ofs + C.stride * off, C.class_mod, d, C.index, out);
+}
+
+__global__ void __launch_bounds__(kWThreads, 3)
+    wide_kernel(const WideCurve *__restrict__ curves, const BatchItem *__restrict__ items,
+                int nitems, const u64 *__restrict__ pool, const u64 *__restrict__ affine,
+                const unsigned short *__restrict__ inv_table, Candidates cand, BatchOut out,
+                unsigned long long *work) {
+    extern __shared__ __align__(16) u64 smem[];
+    __shared__ WideCurve C;
+    __shared__ int s_item;
+    __shared__ u32 s_ofs[kMaxClasses];
+    __shared__ int s_wtile[kMaxClasses];
+    __shared__ int s_last_bits[kMaxClasses];
+    __shared__ int s_prefix[kMaxClasses + 1];
+    __shared__ int s_ci[kSelectedPrimes];
+    __shared__ u32 s_dinv[kSelectedPrimes];
+    __shared__ int s_next;
+    __shared__ int s_abort;
+    __shared__ __align__(8) unsigned long long s_bar;
+
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const u32 bar = smem_addr(&s_bar);
+    u32 phase = 0;
+    int cur = -1;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    for (;;) {
+        if (threadIdx.x == 0) s_item = int(atomicAdd(work, 1ull));
+        __syncthreads();
+        const int it = s_item;
+        if (it >= nitems) break;
+        const BatchItem item = items[it];
+        if (item.curve != cur) {
+            const u32 *src = reinterpret_cast<const u32 *>(curves + item.curve);
+            u32 *dst = reinterpret_cast<u32 *>(&C);
+            for (int i = threadIdx.x; i < int(sizeof(WideCurve) / 4); i += kWThreads) dst[i] = src[i];
+            cur = item.curve;
+            __syncthreads();
+        }
+        u64 *rows = smem;
+        u64 *qmask = rows + C.smem_words;
+        u32 *qinfo = reinterpret_cast<u32 *>(qmask + kWWarps * kQueue);
+        u32 *s_start = qinfo + kWWarps * kQueue;  // [kMaxClasses][kWideSlots]
+        u64 *wq_mask = qmask + warp * kQueue;
+        u32 *wq_info = qinfo + warp * kQueue;
+        const u32 rows_addr = smem_addr(rows);
+        const unsigned char *sbase = reinterpret_cast<const unsigned char *>(rows);
+        const int q = C.class_prime;
+        const int M = C.class_mod;
+
+        for (int i = 0; i < item.count; ++i) {
+            const long long k = item.first + i;
+            const long long d = C.square ? k * k : k;
+            const u32 du = u32(d);
+            const u64 classes2 = C.admissible[du & 63];
+            const u64 classesq = q > 1 ? C.admissible[64 + int(du % u32(q))] : u64(1);
+            if (!classes2 || !classesq) continue;
+            const int nq = __popcll(classesq);
+            const int nclass = __popcll(classes2) * nq;
+
+            if (threadIdx.x == 0) {
+                fence_proxy_async_shared();
+                mbar_arrive_expect_tx(bar, u32(C.smem_words) * 8u);
+#pragma unroll
+                for (int sl = 0; sl < kWideSlots; ++sl) {
+                    const Modulus &Md = C.mod[sl];
+                    const u32 rho = mod_u32(du, u32(Md.m), Md.magic);
+                    bulk_copy_to_shared(rows_addr + u32(Md.smem_offset) * 8u,
+                                        pool + Md.offset + (long long)rho * Md.length,
+                                        u32(Md.length) * 8u, bar);
+                }
+            }
+            if (warp == 0) {
+                select_warp(du, cand, inv_table, s_ci, s_dinv);
+                if (lane == 0) s_next = 0;
+            } else if (warp == 1) {
+                // classes, 32 per pass: class c = (c / nq)-th 2-adic class crossed
+                // with the (c % nq)-th admissible residue mod q; item prefix by scan
+                int carry = 0;
+                for (int base = 0; base < nclass; base += 32) {
+                    const int c = base + lane;
+                    int nitems_c = 0;
+                    if (c < nclass) {
+                        u64 b2 = classes2;
+                        for (int t = c / nq; t > 0; --t) b2 &= b2 - 1;
+                        const int r64 = __ffsll((long long)b2) - 1;
+                        int r = r64;
+                        if (q > 1) {
+                            u64 bq = classesq;
+                            for (int t = c % nq; t > 0; --t) bq &= bq - 1;
+                            const int rq = __ffsll((long long)bq) - 1;
+                            r = r64 + 64 * int(C.crt[C.mod_q[r64] * 13 + rq]);
+                        }
+                        int ofs = r + C.h_mod_m;
+                        if (ofs >= M) ofs -= M;
+                        // sites of class r: a = -H + ofs + M t, t in [0, count)
+                        const long long count = C.count_q + (ofs <= C.count_r ? 1 : 0);
+                        const long long words = (count + 63) >> 6;
+                        s_ofs[c] = u32(ofs);
+                        s_wtile[c] = int(words);
+                        s_last_bits[c] = words > 0 ? int(count - 64 * (words - 1)) : 64;
+#pragma unroll
+                        for (int sl = 0; sl < kWideSlots; ++sl) {
+                            const Modulus &Md = C.mod[sl];
+                            const u32 a0m = mod_u32(Md.neg_h + u32(ofs), u32(Md.m), Md.magic);
+                            s_start[c * kWideSlots + sl] =
+                                mod_u32(a0m * Md.inv_stride, u32(Md.m), Md.magic);
+                        }
+                        nitems_c = int((words + kWItemWords - 1) / kWItemWords);
+                    }
+                    int incl = nitems_c;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int v = __shfl_up_sync(kFullMask, incl, o);
+                        if (lane >= o) incl += v;
+                    }
+                    if (c < nclass) s_prefix[c] = carry + incl - nitems_c;
+                    carry += __shfl_sync(kFullMask, incl, 31);
+                }
+                if (lane == 0) s_prefix[nclass] = carry;
+            }
+            __syncthreads();
+            if (!mbar_wait(bar, phase)) {  // rows landed (bounded wait)
+                s_abort = 1;
+                if (out.error) atomicOr(out.error, 1ull);
+            }
+            phase ^= 1u;
+
+            const int total_items = s_prefix[nclass];
+            int qn = 0;
+            u32 step8[kWideSlots], mod8[kWideSlots];
+            const unsigned char *slot_base[kWideSlots];
+#pragma unroll
+            for (int sl = 0; sl < kWideSlots; ++sl) {
+                step8[sl] = 8u * C.mod[sl].step;
+                mod8[sl] = 8u * u32(C.mod[sl].m);
+                slot_base[sl] = sbase + 8 * C.mod[sl].smem_offset;
+            }
+            for (;;) {
+                int sweep = 0;
+                if (lane == 0) sweep = atomicAdd(&s_next, 1);
+                sweep = __shfl_sync(kFullMask, sweep, 0);
+                if (sweep >= total_items) break;
+                int c = 0;
+                for (int base = 0; base < nclass; base += 32) {
+                    const int cc = base + lane;
+                    const u32 b = __ballot_sync(kFullMask, cc < nclass && s_prefix[cc] <= sweep);
+                    if (b) c = base + 31 - __clz(b);
+                    if (b != kFullMask) break;
+                }
+                const int w0 = (sweep - s_prefix[c]) * kWItemWords;
+                const int wt = s_wtile[c];
+                const u64 last_mask =
+                    s_last_bits[c] >= 64 ? ~u64(0) : ((u64(1) << s_last_bits[c]) - 1);
+                u32 o[kWideSlots];
+#pragma unroll
+                for (int sl = 0; sl < kWideSlots; ++sl)
+                    o[sl] = 8u * mod_u32(s_start[c * kWideSlots + sl] + u32(w0 + lane),
+                                         u32(C.mod[sl].m), C.mod[sl].magic);
+#pragma unroll 1
+                for (int step = 0; step < kWSteps; ++step) {
+                    const int ws = w0 + step * kWarpSize * kWK;
+                    if (ws >= wt) break;
+                    u64 acc[kWK];
+#pragma unroll
+                    for (int kk = 0; kk < kWK; ++kk)
+                        acc[kk] = *reinterpret_cast<const u64 *>(slot_base[0] + o[0] + 256 * kk);
+#pragma unroll
+                    for (int sl = 1; sl < kWideSlots; ++sl) {
+#pragma unroll
+                        for (int kk = 0; kk < kWK; ++kk)
+                            acc[kk] &= *reinterpret_cast<const u64 *>(slot_base[sl] + o[sl] + 256 * kk);
+                    }
+#pragma unroll
+                    for (int sl = 0; sl < kWideSlots; ++sl) {
+                        // advance (32 kWK) mod m words; unsigned min wraps into [0, m)
+                        const u32 t = o[sl] + step8[sl];
+                        o[sl] = min(t, t - mod8[sl]);
+                    }
+                    const u64 any = acc[0] | acc[1] | acc[2] | acc[3];
+                    if (!__ballot_sync(kFullMask, any != 0)) continue;
+#pragma unroll
+                    for (int kk = 0; kk < kWK; ++kk) {
+                        const int w = ws + kWarpSize * kk + lane;
+                        u64 a = acc[kk];
+                        if (w == wt - 1) a &= last_mask;
+                        const bool live = a != 0 && w < wt;
+                        const u32 b = __ballot_sync(kFullMask, live);
+                        if (b) {
+                            const int pos = qn + __popc(b & lanemask_lt());
+                            if (live) {
+                                wq_mask[pos] = a;
+                                wq_info[pos] = (u32(w) << kClassBits) | u32(c);
+                            }
+                            qn += __popc(b);
+                            if (qn >= 32) {
+                                __syncwarp();
+                                wide_drain(wq_mask, wq_info, qn - 32, 32, C, cand, affine, s_ci,
+                                           s_dinv, s_ofs, d, out);
+                                qn -= 32;
+                            }
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            wide_drain(wq_mask, wq_info, 0, qn, C, cand, affine, s_ci, s_dinv, s_ofs, d, out);
+            __syncthreads();
+            if (s_abort) {
+                // a bulk copy did not complete in time: give in-flight copies a
+                // last bounded chance to land, then leave (the host reports it)
+                if (threadIdx.x == 0) mbar_wait(bar, phase ^ 1u);
+                return;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Narrow rows: dense layout, one warp per denominator, whole tables in shared memory.
+
+__device__ __forceinline__ void narrow_drain(const u64 *qmask, const u32 *qword, int start, int n,
+                                             const NarrowCurve &C, const Candidates &cand,
+                                             const u64 *affine, const int *s_ci, const u32 *s_dinv,
+                                             long long d, const BatchOut &out) {
+    const int lane = threadIdx.x & 31;
+    u64 m = 0;
+    u32 w = 0;
+    if (lane < n) {
+        m = qmask[start + lane];
+        w = qword[start + lane];
+    }
+    __syncwarp();
+    if (m) {
+        m = stage2(
+            m, s_ci, s_dinv, cand, affine + C.aff,
+            [&](int ci, u32 p, u32 magic) {
+                const u32 r = C.neg_h[ci] + mod_small(64u * mod_small(w, p, magic), p, magic);
+                return r >= p ? r - p : r;
+            },
+            [&](int) { return 1u; });
+    }
+    emit(m, -C.bound + 64LL * w, 1, d, C.index, out);
+}
+
+__global__ void __launch_bounds__(kNThreads, 3)
+    narrow_kernel(const NarrowCurve *__restrict__ curves, const BatchItem *__restrict__ items,
+                  int nitems, const u64 *__restrict__ pool, const u64 *__restrict__ affine,
+                  const unsigned short *__restrict__ inv_table, Candidates cand, BatchOut out,
+                  unsigned long long *work) {
+    extern __shared__ __align__(16) u64 smem[];
+    __shared__ NarrowCurve C;
+    __shared__ int s_item;
+    __shared__ int s_next;
+    __shared__ int s_abort;
+    __shared__ int s_ci[kNWarps][kSelectedPrimes];
+    __shared__ u32 s_dinv[kNWarps][kSelectedPrimes];
+    __shared__ __align__(8) unsigned long long s_bar;
+
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const u64 *tab = smem;
+    u64 *wq_mask = smem + kNarrowTableWords + warp * kQueue;
+    u32 *wq_word = reinterpret_cast<u32 *>(smem + kNarrowTableWords + kNWarps * kQueue) + warp * kQueue;
+    const u32 bar = smem_addr(&s_bar);
+    u32 phase = 0;
+    int cur = -1;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_item = int(atomicAdd(work, 1ull));
+            s_next = 0;
+        }
+        __syncthreads();
+        const int it = s_item;
+        if (it >= nitems) break;
+        const BatchItem item = items[it];
+        if (item.curve != cur) {
+            const u32 *src = reinterpret_cast<const u32 *>(curves + item.curve);
+            u32 *dst = reinterpret_cast<u32 *>(&C);
+            for (int i = threadIdx.x; i < int(sizeof(NarrowCurve) / 4); i += kNThreads) dst[i] = src[i];
+            cur = item.curve;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                fence_proxy_async_shared();
+                mbar_arrive_expect_tx(bar, u32(C.table_words) * 8u);
+                bulk_copy_to_shared(smem_addr(smem), pool + C.tables, u32(C.table_words) * 8u, bar);
+            }
+            if (!mbar_wait(bar, phase)) {
+                s_abort = 1;
+                if (out.error) atomicOr(out.error, 1ull);
+            }
+            phase ^= 1u;
+            __syncthreads();
+            if (s_abort) {
+                if (threadIdx.x == 0) mbar_wait(bar, phase ^ 1u);
+                return;
+            }
+        }
+        const long long W = C.words;
+        const int last_bits = int(2 * C.bound + 1 - 64 * (W - 1));
+        const u64 last_mask = last_bits >= 64 ? ~u64(0) : ((u64(1) << last_bits) - 1);
+        int *w_ci = s_ci[warp];
+        u32 *w_dinv = s_dinv[warp];
+        for (;;) {
+            int idx = 0;
+            if (lane == 0) idx = atomicAdd(&s_next, 1);
+            idx = __shfl_sync(kFullMask, idx, 0);
+            if (idx >= item.count) break;
+            const long long k = item.first + idx;
+            const long long d = C.square ? k * k : k;
+            const u32 du = u32(d);
+            const u64 mask2 = C.dense2[du & 63];
+            if (!mask2) continue;
+            u32 base[kNarrowSlots], at[kNarrowSlots], mods[kNarrowSlots], steps[kNarrowSlots];
+#pragma unroll
+            for (int s = 0; s < kNarrowSlots; ++s) {
+                const u32 m = u32(C.m[s]);
+                mods[s] = m;
+                steps[s] = C.step[s];
+                base[s] = u32(C.off[s]) + mod_u32(du, m, C.magic[s]) * m;
+                at[s] = mod_u32(C.shift[s] + u32(lane), m, C.magic[s]);
+            }
+            bool selected = false;
+            int qn = 0;
+            for (long long w0 = 0; w0 < W; w0 += kWarpSize) {
+                const long long w = w0 + lane;
+                u64 acc = mask2;
+#pragma unroll
+                for (int s = 0; s < kNarrowSlots; ++s) {
+                    acc &= tab[base[s] + at[s]];
+                    const u32 t = at[s] + steps[s];  // advance 32 words mod m
+                    at[s] = min(t, t - mods[s]);
+                }
+                if (w >= W) acc = 0;
+                else if (w == W - 1) acc &= last_mask;
+                const u32 b = __ballot_sync(kFullMask, acc != 0);
+                if (!b) continue;
+                const int pos = qn + __popc(b & lanemask_lt());
+                if (acc) {
+                    wq_mask[pos] = acc;
+                    wq_word[pos] = u32(w);
+                }
+                qn += __popc(b);
+                if (qn >= 32) {
+                    if (!selected) {
+                        select_warp(du, cand, inv_table, w_ci, w_dinv);
+                        selected = true;
+                    }
+                    __syncwarp();
+                    narrow_drain(wq_mask, wq_word, qn - 32, 32, C, cand, affine, w_ci, w_dinv, d, out);
+                    qn -= 32;
+                }
+            }
+            if (qn) {
+                if (!selected) select_warp(du, cand, inv_table, w_ci, w_dinv);
+                __syncwarp();
+                narrow_drain(wq_mask, wq_word, 0, qn, C, cand, affine, w_ci, w_dinv, d, out);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace dev
+
+// ---------------------------------------------------------------------------
+// Host driver
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+double ms_since(Clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
+template <typename T>
+struct DeviceArray {
+    T *p = nullptr;
+    ~DeviceArray() { cudaFree(p); }
+    void alloc(std::size_t count, const char *what) {
+        cudaFree(p);
+        p = nullptr;
+        check_cuda(cudaMalloc(&p, std::max<std::size_t>(count, 1) * sizeof(T)), what);
+    }
+    void upload(const std::vector<T> &v, cudaStream_t s, unsigned long long &bytes, const char *what) {
+        alloc(v.size(), what);
+        if (!v.empty())
+            check_cuda(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s),
+                       what);
+        bytes += v.size() * sizeof(T);
+    }
+};
+
+// Runs fn(i) for i in [0, n) on the host's threads; rethrows the first exception.
+template <typename F>
+void parallel_for(std::size_t n, F &&fn) {
+    const unsigned threads = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 64));
+    if (n < 2 || threads == 1) {
+        for (std::size_t i = 0; i < n; ++i) fn(i);
+        return;
+    }
+    std::atomic<std::size_t> next{0};
+    std::vector<std::thread> pool;
+    std::exception_ptr error;
+    std::mutex error_mutex;
+    for (unsigned t = 0; t < std::min<std::size_t>(threads, n); ++t) {
+        pool.emplace_back([&] {
+            for (std::size_t i; (i = next.fetch_add(1)) < n;) {
+                try {
+                    fn(i);
+                } catch (...) {
+                    std::lock_guard<std::mutex> lock(error_mutex);
+                    if (!error) error = std::current_exception();
+                }
+            }
+        });
+    }
+    for (auto &th : pool) th.join();
+    if (error) std::rethrow_exception(error);
+}
+
+long long gcd_ll(long long a, long long b) {
+    if (a < 0) a = -a;
+    while (b) {
+        const long long t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+bool is_small_prime(int n) {
+    if (n < 2) return false;
+    for (int f = 2; f * f <= n; ++f)
+        if (n % f == 0) return false;
+    return true;
+}
+
+unsigned long long host_magic(int m) {
+    return m == 1 ? ~0ull : (~0ull) / (unsigned long long)m + 1;
+}
+
+bool lead_is_square(const std::vector<std::string> &coefficients, int q) {
+    const int n = int(coefficients.size()) - 1;
+    if (n % 2) return true;  // odd degree: F(a, d) = d (...) vanishes mod q | d
+    const int lc = decimal_mod(coefficients.back(), q);
+    for (int v = 0; v < q; ++v)
+        if ((v * v) % q == lc) return true;
+    return false;
+}
+
+// 2-adic admissible classes r mod 64 by d mod 64: F(r, d) a square mod 64, r
+// odd when d is even (the fast plan's 2-adic filter).
+void two_adic_classes(const std::vector<std::string> &coefficients, dev::u64 out[64]) {
+    const int n = int(coefficients.size()) - 1;
+    std::vector<int> c64(coefficients.size());
+    for (std::size_t i = 0; i < coefficients.size(); ++i) c64[i] = decimal_mod(coefficients[i], 64);
+    bool square64[64] = {};
+    for (int v = 0; v < 64; ++v) square64[(v * v) & 63] = true;
+    for (int dd = 0; dd < 64; ++dd) {
+        out[dd] = 0;
+        for (int r = 0; r < 64; ++r) {
+            if (dd % 2 == 0 && r % 2 == 0) continue;
+            int value = c64[n], power = 1;
+            for (int i = n - 1; i >= 0; --i) {
+                value = (value * r) & 63;
+                power = (power * dd) & 63;
+                value = (value + c64[i] * power) & 63;
+            }
+            if (n % 2 == 1) value = (value * dd) & 63;
+            if (square64[value]) out[dd] |= dev::u64(1) << r;
+        }
+    }
+}
+
+int round_even(long long v) { return int((v + 1) & ~1LL); }
+
+struct CurveWork {
+    bool ok = false;
+    bool wide = false;
+    std::unique_ptr<ExactPolynomial> poly;
+    FastPlan plan;
+    long long words = 0;       // dense 64-site words per row
+    long long count = 0;       // parameters
+};
+
+// Wide plan: moduli capped so that tables stay small against the curve's
+// work, and the staged rows fit the shared-memory budget.
+FastPlan wide_plan(const std::vector<std::string> &coefficients, long long bound, long double work) {
+    int cap = int(std::min<long double>(kMaxModulus, std::max<long double>(64, std::sqrt(work / 48.0L))));
+    for (;;) {
+        FastPlan plan = choose_fast_plan(coefficients, bound, cap, true);
+        long long smem = 0;
+        for (int sl = 0; sl < dev::kWideSlots; ++sl) {
+            const int m = sl < int(plan.moduli.size()) ? plan.moduli[sl] : 1;
+            smem += round_even(m + dev::kWExt);
+        }
+        if (smem <= dev::kWMaxSmemWords || cap <= 64) return plan;
+        cap = cap * 7 / 8;
+    }
+}
+
+}  // namespace
+
+std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &curves, int device,
+                                           BatchStats *stats_out, bool use_graph) {
+    const auto started = Clock::now();
+    BatchStats stats;
+    std::vector<BatchCurveResult> results(curves.size());
+    if (device >= 0) check_cuda(cudaSetDevice(device), "cudaSetDevice");
+    int dev_id = 0;
+    check_cuda(cudaGetDevice(&dev_id), "cudaGetDevice");
+
+    // ---- validation and per-curve plans, one curve per task ----
+    const auto t_plan = Clock::now();
+    std::vector<CurveWork> work(curves.size());
+    parallel_for(curves.size(), [&](std::size_t i) {
+        const BatchCurveSpec &c = curves[i];
+        BatchCurveResult &r = results[i];
+        CurveWork &cw = work[i];
+        try {
+            if (c.coefficients.size() < 2) throw std::invalid_argument("polynomial must have degree >= 1");
+            if (c.bound < 1) throw std::invalid_argument("numerator bound must be positive");
+            if (c.first < 1) throw std::invalid_argument("denominators start at 1");
+            if (c.last > (c.square ? 46340LL : 2147483647LL))
+                throw std::invalid_argument("denominator range too large for 32-bit denominators");
+            if (c.bound > (1LL << 33))
+                throw std::invalid_argument("numerator bound too large for the batched search");
+            cw.poly.reset(new ExactPolynomial(c.coefficients));
+            if (!cw.poly->is_squarefree()) {
+                r.status = 6;
+                r.error = "polynomial is not squarefree";
+                return;
+            }
+            cw.words = word_count64(c.bound);
+            cw.count = c.last >= c.first ? c.last - c.first + 1 : 0;
+            cw.wide = cw.words >= kBatchWideWords;
+            if (cw.wide) cw.plan = wide_plan(c.coefficients, c.bound, (long double)cw.words * cw.count);
+            else cw.plan = choose_fast_plan(c.coefficients, c.bound, kBatchNarrowModulus, false);
+            r.wide = cw.wide;
+            r.class_prime = cw.plan.class_prime;
+            r.moduli = cw.plan.moduli;
+            cw.ok = true;
+        } catch (const std::exception &e) {
+            r.status = 1;
+            r.error = e.what();
+        }
+    });
+
+    // ---- descriptors, table specs, work items ----
+    std::vector<dev::WideCurve> wide;
+    std::vector<dev::NarrowCurve> narrow;
+    std::vector<dev::AffineSpec> aspecs;
+    std::vector<unsigned short> residues;
+    std::vector<dev::PatternSpec> pspecs;
+    std::vector<dev::CompositeSpec> cspecs;
+    std::vector<dev::BatchItem> wide_items, narrow_items;
+    long long aff_words = 0, pattern_words = 0, row_words = 0;
+    int wide_smem_words = 0;
+    const auto &cands = candidate_primes();
+    auto add_affine = [&](int p, const std::vector<std::string> &coeffs) {
+        dev::AffineSpec A{};
+        A.out = aff_words;
+        A.residues = (long long)residues.size();
+        A.p = p;
+        A.n = int(coeffs.size()) - 1;
+        for (const auto &c : coeffs) residues.push_back((unsigned short)decimal_mod(c, p));
+        aspecs.push_back(A);
+        aff_words += dev::kRefWords;
+        return A.out;
+    };
+    // largest work first, so that the persistent kernels end on small items
+    std::vector<std::size_t> order;
+    for (std::size_t i = 0; i < curves.size(); ++i)
+        if (work[i].ok && work[i].count > 0) order.push_back(i);
+    std::stable_sort(order.begin(), order.end(), [&](std::size_t a, std::size_t b) {
+        return (long double)work[a].words * work[a].count > (long double)work[b].words * work[b].count;
+    });
+    for (std::size_t i : order) {
+        const BatchCurveSpec &c = curves[i];
+        CurveWork &cw = work[i];
+        const FastPlan &plan = cw.plan;
+        const long long H = c.bound;
+        const long long aff_base = aff_words;
+        for (int ci = 0; ci < kCandidatePrimes; ++ci) add_affine(cands[ci], c.coefficients);
+        // per-prime patterns of this curve's stage-1 factors
+        const long long M = cw.wide ? 64LL * plan.class_prime : 1;
+        const long long S = cw.wide ? 64LL * M : 64;
+        std::vector<long long> pattern_of(kFastPrimeLimit, -1);
+        for (const auto &slot : plan.slots)
+            for (int q : slot) {
+                if (pattern_of[q] >= 0) continue;
+                dev::PatternSpec P{};
+                P.offset = pattern_words;
+                P.aff = add_affine(q, c.coefficients);
+                P.q = q;
+                P.lead_ok = lead_is_square(c.coefficients, q) ? 1 : 0;
+                P.s = int(S % q);
+                P.t = int(M % q);
+                pspecs.push_back(P);
+                pattern_of[q] = pattern_words;
+                pattern_words += (long long)q * q;
+            }
+        auto add_composite = [&](int sl, int length) {
+            dev::CompositeSpec T{};
+            T.offset = row_words;
+            if (sl < int(plan.moduli.size())) {
+                T.m = plan.moduli[sl];
+                T.nf = int(plan.slots[sl].size());
+                for (int f = 0; f < T.nf; ++f) {
+                    T.q[f] = plan.slots[sl][f];
+                    T.pattern[f] = pattern_of[T.q[f]];
+                }
+            } else {
+                T.m = 1;  // padding: a row of ones
+                T.nf = 0;
+            }
+            T.length = length < 0 ? T.m : length;
+            cspecs.push_back(T);
+            row_words += (long long)T.m * T.length;
+            return T;
+        };
+        stats.rectangle_sites += (long double)(2 * H + 1) * (long double)cw.count;
+        stats.denominators += (unsigned long long)cw.count;
+        stats.words += (unsigned long long)(cw.words * cw.count);
+        if (cw.wide) {
+            dev::WideCurve C{};
+            const int q = plan.class_prime;
+            C.bound = H;
+            C.stride = S;
+            C.count_q = (2 * H) / M;
+            C.count_r = int((2 * H) % M);
+            C.class_prime = q;
+            C.class_mod = int(M);
+            C.h_mod_m = int(H % M);
+            C.inv64_q = q > 1 ? int(mod_inverse(64 % q, q)) : 0;
+            C.square = c.square ? 1 : 0;
+            C.index = int(i);
+            C.aff = aff_base;
+            if (C.count_q / 64 + 2 >= dev::kMaxClassWords)
+                throw std::invalid_argument("numerator bound too large for the batched search");
+            int smem = 0;
+            for (int sl = 0; sl < dev::kWideSlots; ++sl) {
+                const int m = sl < int(plan.moduli.size()) ? plan.moduli[sl] : 1;
+                const dev::CompositeSpec T = add_composite(sl, round_even(m + dev::kWExt));
+                dev::Modulus &Md = C.mod[sl];
+                Md.offset = T.offset;
+                Md.magic = host_magic(m);
+                Md.m = m;
+                Md.length = T.length;
+                Md.smem_offset = smem;
+                smem += T.length;
+                Md.inv_stride = m > 1 ? dev::u32(mod_inverse(S % m, m)) : 0;
+                Md.neg_h = dev::u32((m - H % m) % m);
+                Md.step = dev::u32((dev::kWarpSize * dev::kWK) % m);
+            }
+            C.smem_words = smem;
+            wide_smem_words = std::max(wide_smem_words, smem);
+            two_adic_classes(c.coefficients, C.admissible);
+            if (q > 1) {
+                const auto aff = affine_mask(q, c.coefficients);
+                const bool lead = lead_is_square(c.coefficients, q);
+                for (int dq = 0; dq < q; ++dq)
+                    for (int r = 0; r < q; ++r) {
+                        const bool ok = dq == 0 ? (r != 0 && lead)
+                                                : aff[(r * mod_inverse(dq, q)) % q] != 0;
+                        if (ok) C.admissible[64 + dq] |= dev::u64(1) << r;
+                    }
+                for (int a = 0; a < q; ++a)
+                    for (int rq = 0; rq < q; ++rq)
+                        C.crt[a * 13 + rq] = (unsigned char)(((rq - a + q) % q) * C.inv64_q % q);
+            }
+            for (int r64 = 0; r64 < 64; ++r64) C.mod_q[r64] = (unsigned char)(q > 1 ? r64 % q : 0);
+            for (int ci = 0; ci < kCandidatePrimes; ++ci) {
+                const int p = cands[ci];
+                C.neg_h[ci] = (unsigned short)((p - H % p) % p);
+                C.s_mod[ci] = (unsigned short)(S % p);
+                C.m_mod[ci] = (unsigned short)(M % p);
+            }
+            // items of about 2^20 row words
+            const long long chunk = std::max(1LL, std::min<long long>(1 << 16, (1LL << 20) / cw.words));
+            for (long long f = c.first; f <= c.last; f += chunk)
+                wide_items.push_back({f, int(wide.size()), int(std::min(chunk, c.last - f + 1))});
+            wide.push_back(C);
+            stats.wide_curves += 1;
+        } else {
+            dev::NarrowCurve C{};
+            C.bound = H;
+            C.words = cw.words;
+            C.square = c.square ? 1 : 0;
+            C.index = int(i);
+            C.aff = aff_base;
+            if (row_words % 2) row_words += 1;  // 16-byte aligned bulk copy
+            C.tables = row_words;
+            int used = 0;
+            for (int sl = 0; sl < dev::kNarrowSlots; ++sl) {
+                const dev::CompositeSpec T = add_composite(sl, -1);
+                const int m = T.m;
+                C.m[sl] = m;
+                C.off[sl] = used;
+                used += m * m;
+                C.magic[sl] = host_magic(m);
+                const long long inv64 = m > 1 ? mod_inverse(64 % m, m) : 0;
+                C.shift[sl] = dev::u32(((m - H % m) % m) * inv64 % m);
+                C.step[sl] = dev::u32(32 % m);
+            }
+            if (used % 2) {
+                row_words += 1;
+                used += 1;
+            }
+            if (used > dev::kNarrowTableWords) throw std::logic_error("narrow tables exceed shared memory");
+            C.table_words = used;
+            // dense layout: bit j of a word holds a = -H + 64 w + j, so a = j - H (mod 64)
+            dev::u64 by_class[64];
+            two_adic_classes(c.coefficients, by_class);
+            const int h64 = int(H % 64);
+            for (int dd = 0; dd < 64; ++dd) {
+                dev::u64 mask = 0;
+                for (int j = 0; j < 64; ++j)
+                    if ((by_class[dd] >> ((j - h64 + 64) % 64)) & 1) mask |= dev::u64(1) << j;
+                C.dense2[dd] = mask;
+            }
+            for (int ci = 0; ci < kCandidatePrimes; ++ci) {
+                const int p = cands[ci];
+                C.neg_h[ci] = (unsigned short)((p - H % p) % p);
+            }
+            // items of about 2^16 words, at least one denominator per warp
+            const long long chunk =
+                std::max<long long>(dev::kNWarps, std::min<long long>(1 << 14, (1LL << 16) / cw.words));
+            for (long long f = c.first; f <= c.last; f += chunk)
+                narrow_items.push_back({f, int(narrow.size()), int(std::min(chunk, c.last - f + 1))});
+            narrow.push_back(C);
+        }
+        stats.curves += 1;
+    }
+    stats.wide_items = wide_items.size();
+    stats.narrow_items = narrow_items.size();
+    stats.table_words = (unsigned long long)row_words;
+    stats.plan_ms = ms_since(t_plan);
+
+    if (!wide.empty() || !narrow.empty()) {
+        std::vector<unsigned short> inv_table(std::size_t(kMaximumPrime) * kMaximumPrime, 0);
+        std::vector<dev::u64> square_masks(std::size_t(kMaximumPrime) * dev::kRefWords, 0);
+        for (int p = 2; p < kMaximumPrime; ++p) {
+            if (!is_small_prime(p)) continue;
+            for (int r = 1; r < p; ++r)
+                inv_table[std::size_t(p) * kMaximumPrime + r] = (unsigned short)mod_inverse(r, p);
+            for (long long v = 0; v < p; ++v) {
+                const int s = int(v * v % p);
+                square_masks[std::size_t(p) * dev::kRefWords + s / 64] |= dev::u64(1) << (s % 64);
+            }
+        }
+        cudaStream_t stream, side;
+        check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking), "cudaStreamCreate");
+        cudaEvent_t ev[6];
+        for (auto &e : ev) check_cuda(cudaEventCreate(&e), "cudaEventCreate");
+        cudaEvent_t fork, join;
+        check_cuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
+        check_cuda(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "cudaEventCreate");
+        unsigned long long *h_counters = nullptr;
+        check_cuda(cudaMallocHost(&h_counters, 8 * sizeof(unsigned long long)), "cudaMallocHost");
+        struct Guard {
+            cudaStream_t a, b;
+            cudaEvent_t *ev;
+            cudaEvent_t f, j;
+            unsigned long long *host;
+            ~Guard() {
+                cudaStreamSynchronize(a);
+                cudaStreamSynchronize(b);
+                for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
+                cudaEventDestroy(f);
+                cudaEventDestroy(j);
+                cudaFreeHost(host);
+                cudaStreamDestroy(a);
+                cudaStreamDestroy(b);
+            }
+        } guard{stream, side, ev, fork, join, h_counters};
+
+        DeviceArray<dev::WideCurve> d_wide;
+        DeviceArray<dev::NarrowCurve> d_narrow;
+        DeviceArray<dev::BatchItem> d_witems, d_nitems;
+        DeviceArray<dev::AffineSpec> d_aspecs;
+        DeviceArray<dev::PatternSpec> d_pspecs;
+        DeviceArray<dev::CompositeSpec> d_cspecs;
+        DeviceArray<unsigned short> d_res, d_inv;
+        DeviceArray<dev::u64> d_sq, d_aff, d_patterns, d_rows;
+        DeviceArray<unsigned long long> d_counters;  // [0] survivors [1] wide work [2] narrow work [3] error
+        d_wide.upload(wide, stream, stats.h2d_bytes, "upload wide curves");
+        d_narrow.upload(narrow, stream, stats.h2d_bytes, "upload narrow curves");
+        d_witems.upload(wide_items, stream, stats.h2d_bytes, "upload work items");
+        d_nitems.upload(narrow_items, stream, stats.h2d_bytes, "upload work items");
+        d_aspecs.upload(aspecs, stream, stats.h2d_bytes, "upload bitmask specs");
+        d_pspecs.upload(pspecs, stream, stats.h2d_bytes, "upload pattern specs");
+        d_cspecs.upload(cspecs, stream, stats.h2d_bytes, "upload table specs");
+        d_res.upload(residues, stream, stats.h2d_bytes, "upload residues");
+        d_inv.upload(inv_table, stream, stats.h2d_bytes, "upload inverses");
+        d_sq.upload(square_masks, stream, stats.h2d_bytes, "upload squares");
+        d_aff.alloc(std::size_t(aff_words), "cudaMalloc(batch bitmasks)");
+        d_patterns.alloc(std::size_t(pattern_words), "cudaMalloc(batch patterns)");
+        d_rows.alloc(std::size_t(row_words), "cudaMalloc(batch tables)");
+        d_counters.alloc(4, "cudaMalloc(batch counters)");
+        // RPG_BATCH_CAPACITY overrides the first survivor capacity (tests use a
+        // small one to exercise the rerun after an overflow)
+        unsigned long long capacity = 1ull << 20;
+        if (const char *env = std::getenv("RPG_BATCH_CAPACITY"))
+            capacity = std::max(1LL, std::atoll(env));
+        DeviceArray<long long> d_a;
+        DeviceArray<int> d_d, d_c;
+        auto alloc_out = [&](unsigned long long cap) {
+            d_a.alloc(cap, "cudaMalloc(batch survivors)");
+            d_d.alloc(cap, "cudaMalloc(batch survivors)");
+            d_c.alloc(cap, "cudaMalloc(batch survivors)");
+        };
+        alloc_out(capacity);
+
+        int sms = 0;
+        check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id),
+                   "cudaDeviceGetAttribute");
+        const std::size_t wide_smem = std::size_t(wide_smem_words) * 8 +
+                                      std::size_t(dev::kWWarps) * dev::kQueue * 12 +
+                                      std::size_t(dev::kMaxClasses) * dev::kWideSlots * 4;
+        const std::size_t narrow_smem =
+            std::size_t(dev::kNarrowTableWords) * 8 + std::size_t(dev::kNWarps) * dev::kQueue * 12;
+        int wide_grid = 0, narrow_grid = 0;
+        if (!wide.empty()) {
+            int per_sm = 0;
+            check_cuda(cudaFuncSetAttribute(dev::wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            int(wide_smem)),
+                       "cudaFuncSetAttribute");
+            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::wide_kernel,
+                                                                     dev::kWThreads, wide_smem),
+                       "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+            wide_grid = std::max(1, std::min<int>(sms * std::max(1, per_sm), int(wide_items.size())));
+        }
+        if (!narrow.empty()) {
+            int per_sm = 0;
+            check_cuda(cudaFuncSetAttribute(dev::narrow_kernel,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, int(narrow_smem)),
+                       "cudaFuncSetAttribute");
+            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::narrow_kernel,
+                                                                     dev::kNThreads, narrow_smem),
+                       "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+            narrow_grid = std::max(1, std::min<int>(sms * std::max(1, per_sm), int(narrow_items.size())));
+        }
+        dev::Candidates cand{};
+        for (int ci = 0; ci < kCandidatePrimes; ++ci) {
+            cand.p[ci] = cands[ci];
+            cand.magic[ci] = dev::magic40(dev::u32(cands[ci]));
+        }
+
+        // ev[0]/ev[1] tables, ev[2]/ev[3] wide kernel, ev[4]/ev[5] narrow kernel;
+        // external records become event nodes when the stream is captured
+        bool capturing = false;
+        auto record = [&](cudaEvent_t e, cudaStream_t s) {
+            check_cuda(capturing ? cudaEventRecordWithFlags(e, s, cudaEventRecordExternal)
+                                 : cudaEventRecord(e, s),
+                       "cudaEventRecord");
+        };
+        auto enqueue_sieve = [&]() {
+            const dev::BatchOut out{d_a.p, d_d.p, d_c.p, d_counters.p, capacity, d_counters.p + 3};
+            check_cuda(cudaMemsetAsync(d_counters.p, 0, 4 * sizeof(unsigned long long), stream),
+                       "cudaMemsetAsync");
+            check_cuda(cudaEventRecord(fork, stream), "cudaEventRecord");
+            check_cuda(cudaStreamWaitEvent(side, fork, 0), "cudaStreamWaitEvent");
+            record(ev[2], stream);
+            if (wide_grid) {
+                dev::wide_kernel<<<wide_grid, dev::kWThreads, wide_smem, stream>>>(
+                    d_wide.p, d_witems.p, int(wide_items.size()), d_rows.p, d_aff.p, d_inv.p, cand,
+                    out, d_counters.p + 1);
+                check_cuda(cudaGetLastError(), "wide_kernel launch");
+            }
+            record(ev[3], stream);
+            record(ev[4], side);
+            if (narrow_grid) {
+                dev::narrow_kernel<<<narrow_grid, dev::kNThreads, narrow_smem, side>>>(
+                    d_narrow.p, d_nitems.p, int(narrow_items.size()), d_rows.p, d_aff.p, d_inv.p,
+                    cand, out, d_counters.p + 2);
+                check_cuda(cudaGetLastError(), "narrow_kernel launch");
+            }
+            record(ev[5], side);
+            check_cuda(cudaEventRecord(join, side), "cudaEventRecord");
+            check_cuda(cudaStreamWaitEvent(stream, join, 0), "cudaStreamWaitEvent");
+            check_cuda(cudaMemcpyAsync(h_counters, d_counters.p, 4 * sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, stream),
+                       "download batch counters");
+        };
+        auto enqueue_all = [&]() {
+            record(ev[0], stream);
+            const long long aff_threads = (long long)aspecs.size() * dev::kRefWords;
+            if (aff_threads) {
+                dev::affine_kernel<<<unsigned((aff_threads + 255) / 256), 256, 0, stream>>>(
+                    d_aspecs.p, (long long)aspecs.size(), d_res.p, d_sq.p, d_aff.p);
+                check_cuda(cudaGetLastError(), "affine_kernel launch");
+            }
+            if (pattern_words) {
+                dev::pattern_kernel<<<unsigned((pattern_words + 255) / 256), 256, 0, stream>>>(
+                    d_pspecs.p, int(pspecs.size()), d_aff.p, d_inv.p, d_patterns.p, pattern_words);
+                check_cuda(cudaGetLastError(), "pattern_kernel launch");
+            }
+            if (row_words) {
+                dev::composite_kernel<<<unsigned((row_words + 255) / 256), 256, 0, stream>>>(
+                    d_cspecs.p, int(cspecs.size()), d_patterns.p, d_rows.p, row_words);
+                check_cuda(cudaGetLastError(), "composite_kernel launch");
+            }
+            record(ev[1], stream);
+            enqueue_sieve();
+        };
+        if (use_graph) {
+            cudaGraph_t graph = nullptr;
+            cudaGraphExec_t exec = nullptr;
+            check_cuda(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal),
+                       "cudaStreamBeginCapture");
+            capturing = true;
+            try {
+                enqueue_all();
+            } catch (...) {
+                cudaStreamEndCapture(stream, &graph);
+                if (graph) cudaGraphDestroy(graph);
+                throw;
+            }
+            capturing = false;
+            check_cuda(cudaStreamEndCapture(stream, &graph), "cudaStreamEndCapture");
+            const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            check_cuda(inst, "cudaGraphInstantiate");
+            const cudaError_t launched = cudaGraphLaunch(exec, stream);
+            const cudaError_t synced = cudaStreamSynchronize(stream);
+            cudaGraphExecDestroy(exec);
+            check_cuda(launched, "cudaGraphLaunch");
+            check_cuda(synced, "batch graph");
+            stats.graph = true;
+        } else {
+            enqueue_all();
+            check_cuda(cudaStreamSynchronize(stream), "batch sieve");
+        }
+        stats.launches += (aspecs.empty() ? 0 : 1) + (pattern_words ? 1 : 0) + (row_words ? 1 : 0) +
+                          (wide_grid ? 1 : 0) + (narrow_grid ? 1 : 0);
+        auto elapsed = [&](int a, int b) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev[a], ev[b]);
+            return double(ms);
+        };
+        stats.table_ms = elapsed(0, 1);
+        stats.wide_ms = elapsed(2, 3);
+        stats.narrow_ms = elapsed(4, 5);
+        stats.sieve_ms = std::max(elapsed(2, 3), elapsed(2, 5));
+        if (h_counters[3]) throw DeviceTimeout("batched sieve: a bounded wait for a table copy timed out");
+        while (h_counters[0] > capacity) {  // survivors did not fit: run again with room for all
+            capacity = h_counters[0] + (h_counters[0] >> 3) + 1024;
+            alloc_out(capacity);
+            enqueue_sieve();
+            check_cuda(cudaStreamSynchronize(stream), "batch sieve");
+            stats.sieve_ms += std::max(elapsed(2, 3), elapsed(2, 5));
+            stats.launches += (wide_grid ? 1 : 0) + (narrow_grid ? 1 : 0);
+            if (h_counters[3]) throw DeviceTimeout("batched sieve: a bounded wait timed out");
+        }
+        const std::size_t n = std::size_t(h_counters[0]);
+        stats.survivors = n;
+        std::vector<long long> ha(n);
+        std::vector<int> hd(n), hc(n);
+        if (n) {
+            check_cuda(cudaMemcpy(ha.data(), d_a.p, n * sizeof(long long), cudaMemcpyDeviceToHost),
+                       "download batch survivors");
+            check_cuda(cudaMemcpy(hd.data(), d_d.p, n * sizeof(int), cudaMemcpyDeviceToHost),
+                       "download batch survivors");
+            check_cuda(cudaMemcpy(hc.data(), d_c.p, n * sizeof(int), cudaMemcpyDeviceToHost),
+                       "download batch survivors");
+        }
+        stats.d2h_bytes += n * (sizeof(long long) + 2 * sizeof(int)) + 4 * sizeof(unsigned long long);
+
+        // ---- exact verification per curve, in single-search order ----
+        const auto t_verify = Clock::now();
+        std::vector<std::vector<std::size_t>> by_curve(curves.size());
+        for (std::size_t s = 0; s < n; ++s) by_curve[std::size_t(hc[s])].push_back(s);
+        parallel_for(curves.size(), [&](std::size_t i) {
+            if (!work[i].ok) return;
+            BatchCurveResult &r = results[i];
+            const ExactPolynomial &poly = *work[i].poly;
+            std::vector<PointPair> found;
+            std::string root;
+            for (std::size_t s : by_curve[i]) {
+                if (gcd_ll(ha[s], hd[s]) != 1) continue;
+                if (poly.square_root(ha[s], hd[s], root)) found.push_back(PointPair{ha[s], root, hd[s]});
+            }
+            std::sort(found.begin(), found.end(), [](const PointPair &a, const PointPair &b) {
+                return a.denominator != b.denominator ? a.denominator < b.denominator
+                                                      : a.numerator < b.numerator;
+            });
+            SearchOptions filter;
+            filter.intervals = curves[i].intervals;
+            for (auto &p : found)
+                if (filter.accepts(p.numerator, p.denominator)) r.points.push_back(std::move(p));
+            r.survivors = by_curve[i].size();
+        });
+        stats.verify_ms = ms_since(t_verify);
+    }
+    // the point at infinity first, as a single search reports it
+    parallel_for(curves.size(), [&](std::size_t i) {
+        if (!work[i].ok || !curves[i].include_infinity) return;
+        std::string root;
+        if (work[i].poly->square_root(1, 0, root))
+            results[i].points.insert(results[i].points.begin(), PointPair{1, root, 0});
+    });
+    for (const auto &r : results) stats.points += r.points.size();
+    stats.wall_ms = ms_since(started);
+    if (stats_out) *stats_out = stats;
+    return results;
+}
+
+}  // namespace rpg

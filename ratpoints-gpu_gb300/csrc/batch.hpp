@@ -1,0 +1,69 @@
+// Batched many-curve search: every curve's tables resident on the device at
+// once and two persistent kernels over device work queues of
+// (curve, denominator range) items, captured in one CUDA graph.
+//
+// No counterpart in the reference, which searches one curve per process
+// (src/main.cpp:48-85); each curve's result here is the result of a
+// single-curve PointSearch of that curve (src/point_search.cpp:171-240): same
+// points, same order, the point at infinity first.
+//
+// Two shapes, chosen per curve by its row length W = ceil((2H + 1) / 64):
+//   - wide rows (W >= kBatchWideWords): the class-strided layout of the
+//     single-curve fast kernel (numerator classes mod 64 q, one CTA per
+//     denominator, stage-1 rows of up to six composite moduli staged into
+//     shared memory by TMA bulk copies), with per-curve descriptors;
+//   - narrow rows: one warp per denominator over dense 64-site words, the
+//     curve's whole stage-1 tables (moduli <= kBatchNarrowModulus, m x m
+//     words each) loaded into shared memory once per work item.
+// Both kernels finish with the reference's 32 selected primes tested bit by
+// bit against per-curve bitmasks of f(x) mod p, then the host verifies each
+// survivor exactly.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "search.hpp"
+
+namespace rpg {
+
+constexpr long long kBatchWideWords = 2048;
+constexpr int kBatchNarrowModulus = 36;
+
+struct BatchCurveSpec {
+    std::vector<std::string> coefficients;
+    long long bound = 0;                       // numerator bound H
+    long long first = 1, last = 0;             // denominators (k in square mode)
+    bool square = false;                       // denominators k^2
+    bool include_infinity = true;
+    std::vector<SearchInterval> intervals;     // empty: all of [-H, H]
+};
+
+struct BatchCurveResult {
+    int status = 0;                    // rpg_status code (0 = ok)
+    std::string error;
+    std::vector<PointPair> points;     // the order of a single-curve search
+    unsigned long long survivors = 0;  // modular survivors of the batched sieve
+    bool wide = false;                 // which kernel swept the curve
+    int class_prime = 1;
+    std::vector<int> moduli;           // stage-1 moduli the autotuner chose
+};
+
+struct BatchStats {
+    unsigned long long curves = 0, wide_curves = 0, denominators = 0, survivors = 0, points = 0;
+    unsigned long long wide_items = 0, narrow_items = 0, launches = 0, words = 0;
+    unsigned long long table_words = 0;
+    long double rectangle_sites = 0;
+    double plan_ms = 0, table_ms = 0, sieve_ms = 0, verify_ms = 0, wall_ms = 0;
+    double wide_ms = 0, narrow_ms = 0;
+    unsigned long long h2d_bytes = 0, d2h_bytes = 0;
+    bool graph = false;
+};
+
+// Runs every valid curve in one batched pass on `device` (-1: current).
+// Curves that fail validation get a nonzero status and no points; the others
+// are searched together.
+std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &curves, int device,
+                                           BatchStats *stats, bool use_graph = true);
+
+}  // namespace rpg

@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "batch.hpp"
 #include "cli.hpp"
 #include "exact.hpp"
 #include "plan.hpp"
@@ -73,6 +74,45 @@ bool coefficients_from(const char *const *c, int32_t n, std::vector<std::string>
         error = "leading coefficient must be nonzero";
         return false;
     }
+    return true;
+}
+
+// rpg_search_options -> SearchOptions with the checks and messages of a search.
+bool options_from(const rpg_search_options &o, rpg::SearchOptions &s, std::string &error) {
+    if (!coefficients_from(o.coefficients, o.coefficient_count, s.coefficients, error)) return false;
+    if (o.numerator_bound < 1) {
+        error = "maximum height must be positive";
+        return false;
+    }
+    if (o.first < 1 || o.first > o.last) {
+        error = "empty denominator range";
+        return false;
+    }
+    if (o.interval_count < 0 || (o.interval_count > 0 && !o.intervals)) {
+        error = "invalid interval list";
+        return false;
+    }
+    s.numerator_bound = o.numerator_bound;
+    s.first = o.first;
+    s.last = o.last;
+    if (o.square_denominators && s.last > 46340) s.last = 46340;
+    for (int32_t i = 0; i < o.interval_count; ++i) {
+        rpg::SearchInterval iv;
+        const rpg_interval &src = o.intervals[i];
+        iv.lower_infinite = src.lower == nullptr;
+        iv.upper_infinite = src.upper == nullptr;
+        if (src.lower && !rpg::parse_real(src.lower, "interval lower bound", iv.lower, error))
+            return false;
+        if (src.upper && !rpg::parse_real(src.upper, "interval upper bound", iv.upper, error))
+            return false;
+        s.intervals.push_back(iv);
+    }
+    s.include_infinity = o.include_infinity != 0;
+    s.batch_size = o.batch_size;
+    s.square = o.square_denominators != 0;
+    s.plan = o.plan == RPG_PLAN_REFERENCE ? rpg::PlanKind::reference : rpg::PlanKind::fast;
+    if (o.device >= 0) s.devices = {o.device};
+    s.verify_threads = o.verify_threads;
     return true;
 }
 
@@ -164,31 +204,7 @@ rpg_status rpg_point_search(const rpg_search_options *o, rpg_point_cb callback, 
         if (!o || !callback) return fail(RPG_E_ARG, "options and callback must not be NULL");
         rpg::SearchOptions s;
         std::string error;
-        if (!coefficients_from(o->coefficients, o->coefficient_count, s.coefficients, error))
-            return fail(RPG_E_ARG, error);
-        if (o->numerator_bound < 1) return fail(RPG_E_ARG, "maximum height must be positive");
-        if (o->first < 1 || o->first > o->last) return fail(RPG_E_ARG, "empty denominator range");
-        s.numerator_bound = o->numerator_bound;
-        s.first = o->first;
-        s.last = o->last;
-        if (o->square_denominators && s.last > 46340) s.last = 46340;
-        for (int32_t i = 0; i < o->interval_count; ++i) {
-            rpg::SearchInterval iv;
-            const rpg_interval &src = o->intervals[i];
-            iv.lower_infinite = src.lower == nullptr;
-            iv.upper_infinite = src.upper == nullptr;
-            if (src.lower && !rpg::parse_real(src.lower, "interval lower bound", iv.lower, error))
-                return fail(RPG_E_ARG, error);
-            if (src.upper && !rpg::parse_real(src.upper, "interval upper bound", iv.upper, error))
-                return fail(RPG_E_ARG, error);
-            s.intervals.push_back(iv);
-        }
-        s.include_infinity = o->include_infinity != 0;
-        s.batch_size = o->batch_size;
-        s.square = o->square_denominators != 0;
-        s.plan = o->plan == RPG_PLAN_REFERENCE ? rpg::PlanKind::reference : rpg::PlanKind::fast;
-        if (o->device >= 0) s.devices = {o->device};
-        s.verify_threads = o->verify_threads;
+        if (!options_from(*o, s, error)) return fail(RPG_E_ARG, error);
         rpg::PointSearch search(s);
         rpg::SearchMetrics m = search.run([&](const rpg::PointPair &p) {
             return callback(p.numerator, p.ordinate.c_str(), p.denominator, user) != 0;
@@ -302,6 +318,84 @@ rpg_status rpg_session_plan(rpg_session *session, int32_t *class_prime, int32_t 
 }
 
 void rpg_session_destroy(rpg_session *session) { delete session; }
+
+rpg_status rpg_batch_search(const rpg_search_options *curves, int32_t curve_count, int32_t device,
+                            uint32_t flags, rpg_batch_point_cb callback, void *user,
+                            int32_t *curve_status, uint64_t *curve_survivors,
+                            rpg_batch_stats *stats) {
+    return guarded([&]() -> rpg_status {
+        if (curve_count < 0 || (curve_count > 0 && !curves) || !callback)
+            return fail(RPG_E_ARG, "curves and callback must not be NULL");
+        const std::size_t count = static_cast<std::size_t>(curve_count);
+        std::vector<rpg::BatchCurveSpec> specs(count);
+        std::vector<int32_t> status(count, RPG_OK);
+        std::vector<std::string> errors(count);
+        for (int32_t i = 0; i < curve_count; ++i) {
+            rpg::SearchOptions s;
+            rpg::BatchCurveSpec &b = specs[std::size_t(i)];
+            if (!options_from(curves[i], s, errors[std::size_t(i)])) {
+                status[std::size_t(i)] = RPG_E_ARG;
+                b.first = 1;
+                b.last = 0;  // no work; the curve is reported as failed
+                continue;
+            }
+            b.coefficients = s.coefficients;
+            b.bound = s.numerator_bound;
+            b.first = s.first;
+            b.last = s.last;
+            b.square = s.square;
+            b.include_infinity = s.include_infinity;
+            b.intervals = s.intervals;
+        }
+        std::vector<std::size_t> valid;
+        std::vector<rpg::BatchCurveSpec> run;
+        for (int32_t i = 0; i < curve_count; ++i)
+            if (status[std::size_t(i)] == RPG_OK) {
+                valid.push_back(std::size_t(i));
+                run.push_back(std::move(specs[std::size_t(i)]));
+            }
+        rpg::BatchStats st;
+        std::vector<rpg::BatchCurveResult> results =
+            rpg::batch_search(run, device, &st, (flags & RPG_BATCH_NO_GRAPH) == 0);
+        std::vector<const rpg::BatchCurveResult *> by_index(count, nullptr);
+        for (std::size_t j = 0; j < valid.size(); ++j) {
+            by_index[valid[j]] = &results[j];
+            if (results[j].status == RPG_E_NOT_SQUAREFREE) status[valid[j]] = RPG_E_NOT_SQUAREFREE;
+            else if (results[j].status != 0) status[valid[j]] = RPG_E_ARG;
+        }
+        for (int32_t i = 0; i < curve_count; ++i) {
+            const rpg::BatchCurveResult *r = by_index[std::size_t(i)];
+            if (curve_status) curve_status[i] = status[std::size_t(i)];
+            if (curve_survivors) curve_survivors[i] = r ? r->survivors : 0;
+            if (!r || status[std::size_t(i)] != RPG_OK) continue;
+            for (const auto &p : r->points)
+                if (callback(i, p.numerator, p.ordinate.c_str(), p.denominator, user) == 0) break;
+        }
+        if (stats) {
+            std::memset(stats, 0, sizeof *stats);
+            stats->curves = st.curves;
+            stats->wide_curves = st.wide_curves;
+            stats->denominators = st.denominators;
+            stats->survivors = st.survivors;
+            stats->points = st.points;
+            stats->launches = st.launches;
+            stats->words = st.words;
+            stats->table_words = st.table_words;
+            stats->rectangle_sites = double(st.rectangle_sites);
+            stats->plan_ms = st.plan_ms;
+            stats->table_ms = st.table_ms;
+            stats->sieve_ms = st.sieve_ms;
+            stats->wide_ms = st.wide_ms;
+            stats->narrow_ms = st.narrow_ms;
+            stats->verify_ms = st.verify_ms;
+            stats->wall_ms = st.wall_ms;
+            stats->h2d_bytes = st.h2d_bytes;
+            stats->d2h_bytes = st.d2h_bytes;
+            stats->graph = st.graph ? 1 : 0;
+        }
+        return RPG_OK;
+    });
+}
 
 int32_t rpg_device_count(void) {
     int n = 0;

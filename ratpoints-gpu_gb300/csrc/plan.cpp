@@ -117,7 +117,8 @@ int max_classes(int q, const std::vector<std::string> &coefficients) {
 }
 }  // namespace
 
-FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long long bound) {
+FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long long bound,
+                          int max_modulus, bool class_layout) {
     FastPlan plan;
     std::vector<std::pair<double, int>> strength;  // (bits, prime)
     for (int q = 3; q < kFastPrimeLimit; q += 2) {
@@ -133,7 +134,7 @@ FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long lon
     double best = 0.45;  // below ~0.45 bits a class prime does not pay for its classes
     for (const auto &s : strength) {
         const int q = s.second;
-        if (q > 13) continue;
+        if (!class_layout || q > 13) continue;
         if (sites / (64.0L * 64.0L * q) < 256.0L) continue;
         if (max_classes(q, coefficients) > kMaxFastClasses) continue;
         if (s.first > best) {
@@ -163,13 +164,13 @@ FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long lon
         out.class_prime = plan.class_prime;
         for (const auto &s : order) {
             const int q = s.second;
-            if (q >= limit || q == plan.class_prime || s.first < 0.3) continue;
+            if (q >= limit || q == plan.class_prime || s.first < 0.3 || q > max_modulus) continue;
             int target = -1;
             long long headroom = -1;
             for (std::size_t i = 0; i < out.moduli.size(); ++i) {
                 const long long product = (long long)out.moduli[i] * q;
-                if (product <= kMaxModulus && kMaxModulus - product > headroom) {
-                    headroom = kMaxModulus - product;
+                if (product <= max_modulus && (long long)max_modulus - product > headroom) {
+                    headroom = max_modulus - product;
                     target = int(i);
                 }
             }
@@ -194,8 +195,12 @@ FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long lon
         }
     plan = best_plan;
     if (plan.moduli.empty()) {  // every small prime is weak: keep one modulus anyway
-        plan.moduli.push_back(5 * 7);
-        plan.slots.push_back({5, 7});
+        // (prime to the class prime, so that the class layout can use it)
+        std::vector<int> pair = plan.class_prime == 5   ? std::vector<int>{3, 7}
+                                : plan.class_prime == 7 ? std::vector<int>{3, 5}
+                                                        : std::vector<int>{5, 7};
+        plan.moduli.push_back(pair[0] * pair[1]);
+        plan.slots.push_back(pair);
     }
     return plan;
 }

@@ -65,6 +65,10 @@ struct FastPlan {
     std::vector<int> moduli;               // their products
     double bits = 0;                       // expected filtering of the stage-1 rows (bits)
 };
-FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long long bound);
+// max_modulus caps each stage-1 modulus (table size grows as its square);
+// class_prime false keeps the plan to 2-adic classes (the dense layout of the
+// batched search, 64 consecutive numerators per word).
+FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long long bound,
+                          int max_modulus = kMaxModulus, bool class_prime = true);
 
 }  // namespace rpg

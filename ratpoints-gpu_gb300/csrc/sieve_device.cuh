@@ -45,6 +45,50 @@ __device__ __forceinline__ u32 mod_small(u32 n, u32 p, u32 magic) {
     return n - q * p;
 }
 
+__device__ __forceinline__ u32 mod_u32(u32 n, u32 m, unsigned long long magic) {
+    u32 q = u32(__umul64hi((unsigned long long)n, magic));
+    u32 r = n - q * m;
+    return r >= m ? r - m : r;
+}
+
+// Shared-memory address, mbarrier and bulk-copy (TMA, non-tensor) helpers.
+__device__ __forceinline__ u32 smem_addr(const void *p) {
+    return u32(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(u32 bar, u32 count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(u32 bar, u32 bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(u32 bar, u32 parity) {
+    u32 done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
+        "selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Bounded wait for the phase with the given parity; false if the limit ran out.
+__device__ __forceinline__ bool mbar_wait(u32 bar, u32 parity) {
+    for (int i = 0; i < (1 << 24); ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_copy_to_shared(u32 dst, const void *src, u32 bytes, u32 bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_shared() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 __device__ __forceinline__ u32 lanemask_lt() {
     u32 m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

@@ -74,10 +74,27 @@ class SearchOptions(ctypes.Structure):
                 ("device", ctypes.c_int32), ("verify_threads", ctypes.c_int32)]
 
 
+class BatchStats(ctypes.Structure):
+    _fields_ = ([(name, ctypes.c_uint64) for name in
+                 ("curves", "wide_curves", "denominators", "survivors", "points", "launches",
+                  "words", "table_words")] +
+                [(name, ctypes.c_double) for name in
+                 ("rectangle_sites", "plan_ms", "table_ms", "sieve_ms", "wide_ms", "narrow_ms",
+                  "verify_ms", "wall_ms")] +
+                [("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+                 ("graph", ctypes.c_int32)])
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 CANDIDATE_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
                                 ctypes.POINTER(ctypes.c_int32), ctypes.c_size_t, ctypes.c_void_p)
 POINT_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int64, ctypes.c_char_p, ctypes.c_int64,
                             ctypes.c_void_p)
+BATCH_POINT_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int32, ctypes.c_int64, ctypes.c_char_p,
+                                  ctypes.c_int64, ctypes.c_void_p)
+RPG_BATCH_NO_GRAPH = 1
 
 _lib = None
 
@@ -99,6 +116,11 @@ def load():
     lib.rpg_point_search.restype = S
     lib.rpg_point_search.argtypes = [ctypes.POINTER(SearchOptions), POINT_CB, ctypes.c_void_p,
                                      ctypes.POINTER(SieveStats)]
+    lib.rpg_batch_search.restype = S
+    lib.rpg_batch_search.argtypes = [ctypes.POINTER(SearchOptions), ctypes.c_int32, ctypes.c_int32,
+                                     ctypes.c_uint32, BATCH_POINT_CB, ctypes.c_void_p,
+                                     ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_uint64),
+                                     ctypes.POINTER(BatchStats)]
     lib.rpg_is_squarefree.restype = S
     lib.rpg_is_squarefree.argtypes = [pp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
     lib.rpg_square_root.restype = S
@@ -191,11 +213,22 @@ def point_search(coefficients, bound, first, last, intervals=(), include_infinit
         points.append((a, int(y.decode()), d))
         return 0 if stop_after is not None and len(points) >= stop_after else 1
 
+    opts = SearchOptions()
+    keep = _fill_options(opts, coeffs, bound, first, last, intervals, include_infinity,
+                         batch_size, square, plan, device, verify_threads)
+    stats = SieveStats()
+    _check(lib.rpg_point_search(ctypes.byref(opts), on_point, None, ctypes.byref(stats)))
+    del keep
+    return points, stats.as_dict()
+
+
+def _fill_options(opts, coeffs, bound, first, last, intervals=(), include_infinity=True,
+                  batch_size=1 << 16, square=False, plan="fast", device=-1, verify_threads=0):
+    """Fill a SearchOptions; returns the ctypes buffers it points into (keep them alive)."""
     ivs = (Interval * max(1, len(intervals)))()
     for i, (lo, hi) in enumerate(intervals):
         ivs[i].lower = None if lo is None else str(lo).encode()
         ivs[i].upper = None if hi is None else str(hi).encode()
-    opts = SearchOptions()
     cstr = _strings(coeffs)
     opts.coefficients = cstr
     opts.coefficient_count = len(coeffs)
@@ -209,9 +242,39 @@ def point_search(coefficients, bound, first, last, intervals=(), include_infinit
     opts.plan = RPG_PLAN_FAST if plan == "fast" else RPG_PLAN_REFERENCE
     opts.device = device
     opts.verify_threads = verify_threads
-    stats = SieveStats()
-    _check(lib.rpg_point_search(ctypes.byref(opts), on_point, None, ctypes.byref(stats)))
-    return points, stats.as_dict()
+    return (ivs, cstr)
+
+
+def batch_search(curves, device=-1, graph=True, stop_after=None):
+    """Search many curves in one batched pass.
+
+    curves: list of dicts with keys coefficients, bound, first, last and
+    optionally intervals, include_infinity, square.  Returns (points, status,
+    survivors, stats): points[i] is curve i's [(a, y, d)] in the order
+    point_search reports them (truncated to stop_after points when given).
+    """
+    lib = load()
+    n = len(curves)
+    arr = (SearchOptions * max(1, n))()
+    keep = []
+    for i, c in enumerate(curves):
+        keep.append(_fill_options(arr[i], coefficients_of(c["coefficients"]), c["bound"],
+                                  c["first"], c["last"], c.get("intervals", ()),
+                                  c.get("include_infinity", True), square=c.get("square", False)))
+    points = [[] for _ in range(n)]
+
+    @BATCH_POINT_CB
+    def on_point(i, a, y, d, _user):
+        points[i].append((a, int(y.decode()), d))
+        return 0 if stop_after is not None and len(points[i]) >= stop_after else 1
+
+    status = (ctypes.c_int32 * max(1, n))()
+    survivors = (ctypes.c_uint64 * max(1, n))()
+    stats = BatchStats()
+    _check(lib.rpg_batch_search(arr, n, device, 0 if graph else RPG_BATCH_NO_GRAPH, on_point, None,
+                                status, survivors, ctypes.byref(stats)))
+    del keep
+    return points, list(status)[:n], list(survivors)[:n], stats.as_dict()
 
 
 def is_squarefree(coefficients):

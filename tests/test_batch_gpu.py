@@ -1,0 +1,160 @@
+"""Batched many-curve search: each curve's points are exactly the points of a
+single-curve search of that curve (same order, infinity first), for curves on
+the narrow (dense, warp per denominator) and the wide (class layout, CTA per
+denominator) kernels, with and without the CUDA graph, with intervals, square
+denominators, a first-point stop, failing curves in the mix, and a survivor
+buffer too small for the first pass."""
+
+import random
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def random_curve(rng, degree, bits):
+    while True:
+        c = [str(rng.choice((-1, 1)) * rng.getrandbits(rng.randint(1, bits))) for _ in range(degree + 1)]
+        if c[-1] == "0":
+            c[-1] = "3"
+        yield c
+
+
+def mixed_curves(rng, n, heights, dens, degrees=(3, 4, 5, 6, 8, 10), bits=64):
+    curves = []
+    for _ in range(n):
+        degree = rng.choice(degrees)
+        coeffs = next(random_curve(rng, degree, rng.randint(min(8, bits), bits)))
+        curves.append({"coefficients": coeffs, "bound": rng.randint(*heights),
+                       "first": 1, "last": rng.randint(*dens)})
+    return curves
+
+
+def single(rpg, c, **kw):
+    points, _ = rpg.point_search(c["coefficients"], c["bound"], c["first"], c["last"],
+                                 intervals=c.get("intervals", ()),
+                                 include_infinity=c.get("include_infinity", True),
+                                 square=c.get("square", False), **kw)
+    return points
+
+
+def squarefree(rpg, curves):
+    return [c for c in curves if rpg.is_squarefree(c["coefficients"])]
+
+
+def test_batch_matches_oracle_small_boxes(rpg, oracle, golden):
+    curves = [{"coefficients": golden["dense"]["coefficients"].split(), "bound": 300,
+               "first": 1, "last": 40}]
+    rng = random.Random(7)
+    for _ in range(8):
+        degree = rng.choice([1, 2, 3, 4, 5, 6])
+        coeffs = [str(rng.randint(-20, 20)) for _ in range(degree + 1)]
+        if coeffs[-1] == "0":
+            coeffs[-1] = "1"
+        curves.append({"coefficients": coeffs, "bound": rng.choice([30, 200, 700]),
+                       "first": rng.randint(1, 20), "last": rng.randint(20, 60)})
+    curves = squarefree(rpg, curves)
+    points, status, _, stats = rpg.batch_search(curves)
+    assert all(s == 0 for s in status)
+    for c, got in zip(curves, points):
+        expected = []
+        o = oracle.Options(coefficients=c["coefficients"], height=c["bound"], first=c["first"],
+                           last=c["last"])
+        oracle.search(o, lambda a, y, d: expected.append((a, int(y), d)) or True)
+        assert got == expected, c
+    assert stats["curves"] == len(curves)
+
+
+def test_batch_matches_single_search_mixed(rpg):
+    rng = random.Random(2024)
+    curves = mixed_curves(rng, 48, (100, 20000), (1, 3000))
+    # wide rows (>= 2048 words of 64 numerators) with a few denominators each
+    curves += mixed_curves(rng, 12, (70000, 400000), (1, 60))
+    curves = squarefree(rpg, curves)
+    points, status, survivors, stats = rpg.batch_search(curves)
+    assert stats["wide_curves"] >= 6 and stats["curves"] - stats["wide_curves"] >= 20
+    assert stats["graph"] == 1
+    for c, got, s, n in zip(curves, points, status, survivors):
+        assert s == 0
+        assert got == single(rpg, c), c
+        assert n >= sum(1 for p in got if p[2] != 0)
+
+
+def test_batch_small_coefficients_many_points(rpg, golden):
+    """Curves with many points on both kernels."""
+    dense = golden["dense"]["coefficients"].split()
+    curves = [{"coefficients": dense, "bound": b, "first": 1, "last": last}
+              for b, last in ((1000, 500), (5000, 50), (150000, 12), (300000, 3))]
+    rng = random.Random(5)
+    for _ in range(10):
+        coeffs = [str(rng.randint(-3, 3)) for _ in range(rng.choice([3, 4, 5, 6]) + 1)]
+        coeffs[-1] = str(rng.choice([1, 4, 9]))
+        curves.append({"coefficients": coeffs, "bound": rng.choice([500, 3000, 100000]),
+                       "first": 1, "last": rng.choice([20, 200])})
+    curves = squarefree(rpg, curves)
+    points, status, _, stats = rpg.batch_search(curves)
+    assert sum(len(p) for p in points) > 30
+    for c, got in zip(curves, points):
+        assert got == single(rpg, c), c
+
+
+def test_graph_and_direct_launch_agree(rpg):
+    rng = random.Random(99)
+    curves = squarefree(rpg, mixed_curves(rng, 24, (50, 100000), (1, 400)))
+    a = rpg.batch_search(curves, graph=True)
+    b = rpg.batch_search(curves, graph=False)
+    assert a[0] == b[0] and a[1] == b[1] and a[2] == b[2]
+    assert a[3]["graph"] == 1 and b[3]["graph"] == 0
+
+
+def test_intervals_square_denominators_and_infinity(rpg, golden):
+    dense = golden["dense"]["coefficients"].split()
+    curves = [
+        {"coefficients": dense, "bound": 4000, "first": 1, "last": 300,
+         "intervals": [("-1.5", "-0.25"), ("0.5", "2e0")]},
+        {"coefficients": dense, "bound": 200000, "first": 1, "last": 8,
+         "intervals": [(None, "-3"), ("0.5", None)]},
+        {"coefficients": dense, "bound": 3000, "first": 1, "last": 60, "square": True},
+        {"coefficients": ["1", "0", "0", "1"], "bound": 100000, "first": 1, "last": 30,
+         "square": True},
+        {"coefficients": dense, "bound": 500, "first": 5, "last": 90, "include_infinity": False},
+    ]
+    points, status, _, _ = rpg.batch_search(curves)
+    assert status == [0] * len(curves)
+    for c, got in zip(curves, points):
+        assert got == single(rpg, c), c
+
+
+def test_failing_curves_do_not_disturb_the_rest(rpg, golden):
+    dense = golden["dense"]["coefficients"].split()
+    curves = [
+        {"coefficients": dense, "bound": 800, "first": 1, "last": 50},
+        {"coefficients": ["1", "2", "1"], "bound": 100, "first": 1, "last": 10},   # (x+1)^2
+        {"coefficients": dense, "bound": 800, "first": 9, "last": 3},              # empty range
+        {"coefficients": ["1", "x", "2"], "bound": 100, "first": 1, "last": 10},   # not an integer
+        {"coefficients": dense, "bound": 90000, "first": 1, "last": 5},
+    ]
+    points, status, _, _ = rpg.batch_search(curves)
+    assert status == [0, 6, 1, 1, 0]
+    assert points[1] == points[2] == points[3] == []
+    assert points[0] == single(rpg, curves[0])
+    assert points[4] == single(rpg, curves[4])
+
+
+def test_first_point_stop(rpg):
+    rng = random.Random(3)
+    curves = squarefree(rpg, mixed_curves(rng, 16, (100, 5000), (1, 200), bits=6))
+    points, _, _, _ = rpg.batch_search(curves, stop_after=1)
+    for c, got in zip(curves, points):
+        assert got == single(rpg, c, stop_after=1)
+
+
+def test_survivor_overflow_rerun(rpg, golden, monkeypatch):
+    dense = golden["dense"]["coefficients"].split()
+    curves = [{"coefficients": dense, "bound": 5000, "first": 1, "last": 100},
+              {"coefficients": dense, "bound": 100000, "first": 1, "last": 6}]
+    full, _, surv_full, _ = rpg.batch_search(curves)
+    monkeypatch.setenv("RPG_BATCH_CAPACITY", "16")
+    small, _, surv_small, stats = rpg.batch_search(curves)
+    assert small == full and surv_small == surv_full
+    assert stats["survivors"] > 16
