@@ -226,6 +226,57 @@ def reference_gpu(coeffs, denominators, rpg):
                     "once (the reference rebuilds it per batch)"}
 
 
+def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2):
+    """Mixed many-curve batch: one batched pass against the plain per-curve
+    loop of single-curve searches, same curves, points compared curve by curve.
+    Both are timed end to end through the C ABI (coefficient strings in,
+    verified points out)."""
+    import workloads
+
+    curves = workloads.mixed_batch(count)
+    mu = workloads.mobius(max(c["last"] for c in curves))
+    reduced = [workloads.reduced_sites(c["bound"], c["first"], c["last"], mu) for c in curves]
+    rect = [(2 * c["bound"] + 1) * (c["last"] - c["first"] + 1) for c in curves]
+    rpg.batch_search(curves[:32])  # warm-up: module load, graph instantiation paths
+    runs = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        points, status, survivors, stats = rpg.batch_search(curves)
+        runs.append((time.perf_counter() - t0, points, stats))
+    wall, points, stats = sorted(runs, key=lambda r: r[0])[len(runs) // 2]
+    n_plain = min(plain_curves, count)
+    t0 = time.perf_counter()
+    plain = [rpg.point_search(c["coefficients"], c["bound"], c["first"], c["last"])[0]
+             for c in curves[:n_plain]]
+    plain_wall = time.perf_counter() - t0
+    identical = all(a == b for a, b in zip(plain, points[:n_plain]))
+    total_reduced, plain_reduced = sum(reduced), sum(reduced[:n_plain])
+    batched = total_reduced / wall / 1e9
+    plain_value = plain_reduced / plain_wall / 1e9
+    return {
+        "workload": f"{count} seeded squarefree curves: degree uniform in {{3,4,5,6,8,10}}, "
+                    "coefficients random sign x random integer of bit length uniform in 8..64, "
+                    "numerator bound A and denominator bound B independent, each log-uniform "
+                    "in [1e3, 1e6]",
+        "curves": count, "seed": 3, "reduced_sites": total_reduced, "rectangle_sites": sum(rect),
+        "denominators": stats["denominators"],
+        "batched": {"value": batched, "unit": UNIT, "wall_s": wall,
+                    "kernel_value": total_reduced / (stats["sieve_ms"] / 1e3) / 1e9,
+                    "sieve_ms": stats["sieve_ms"], "wide_kernel_ms": stats["wide_ms"],
+                    "narrow_kernel_ms": stats["narrow_ms"], "table_ms": stats["table_ms"],
+                    "plan_ms": stats["plan_ms"], "verify_ms": stats["verify_ms"],
+                    "wide_curves": stats["wide_curves"], "survivors": stats["survivors"],
+                    "points": stats["points"], "table_bytes": stats["table_words"] * 8,
+                    "h2d_bytes": stats["h2d_bytes"], "d2h_bytes": stats["d2h_bytes"],
+                    "graph": bool(stats["graph"]), "launches": stats["launches"]},
+        "plain_loop": {"value": plain_value, "unit": UNIT, "wall_s": plain_wall,
+                       "curves": n_plain,
+                       "note": "rpg_point_search (single-curve fast plan) called once per curve"},
+        "speedup_vs_plain": batched / plain_value,
+        "points_identical": identical,
+    }
+
+
 def workload_config():
     rect = (2 * HEIGHT + 1) * DENOMINATORS
     return {"workload": "degree-6 curve, coefficients uniform in [-2^32, 2^32), "
@@ -248,6 +299,10 @@ def main():
     parser.add_argument("--e2e-steps", type=int, default=1, choices=range(1, 100), metavar="N")
     parser.add_argument("--cpu-seconds", type=float, default=12.0)
     parser.add_argument("--no-cpu-baseline", action="store_true")
+    parser.add_argument("--batch-curves", type=int, default=4096,
+                        help="curves of the mixed batch (0: skip the batch measurement)")
+    parser.add_argument("--batch-plain-curves", type=int, default=4096,
+                        help="curves of the batch also run as a plain per-curve loop")
     args = parser.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -360,6 +415,8 @@ def main():
             "ms_per_step": ref["ms"], "modular_survivors": ref["survivors"],
             "note": "same kernel family with the reference's 32-prime plan: survivor set "
                     "identical to the reference implementation's"}
+    if args.batch_curves > 0:
+        line["batch"] = batch_benchmark(rpg, args.batch_curves, args.batch_plain_curves)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(coeffs, seconds=args.cpu_seconds)
     print(json.dumps(line))

@@ -27,7 +27,8 @@ constexpr int kWThreads = kWWarps * kWarpSize;
 constexpr int kWSteps = 4;
 constexpr int kWItemWords = kWarpSize * kWK * kWSteps;  // class words per sweep item
 constexpr int kWExt = kWarpSize * (kWK - 1);            // row extension
-constexpr int kWMaxSmemWords = 5800;                    // staged row words (3 CTAs per SM)
+constexpr int kWMaxSmemWords = 3300;                    // staged row words per buffer (two
+                                                        // buffers, 3 CTAs per SM)
 constexpr int kQueue = 64;
 constexpr int kClassBits = 8;
 constexpr int kMaxClasses = kMaxFastClasses;
@@ -36,7 +37,8 @@ constexpr int kAdmQ = 16;                               // residue words for cla
 constexpr int kNarrowSlots = 6;
 constexpr int kNWarps = 8;
 constexpr int kNThreads = kNWarps * kWarpSize;
-constexpr int kNarrowTableWords = 8192;                 // sum of m^2 (+ padding) per curve
+constexpr int kNarrowTableWords = 7040;                 // sum of m^2 (+ padding) per curve
+constexpr int kAffWords = kCandidatePrimes * 8;         // the 36 candidate bitmasks
 constexpr int kRefWords = 8;                            // u64 words of a bitmask over [0, 512)
 constexpr int kMaxFactors = 4;
 
@@ -243,7 +245,8 @@ __device__ __forceinline__ void select_warp(u32 du, const Candidates &cand,
 
 // Clears the bits j of m whose site a = base + step j fails one of the 32
 // selected primes: f(a/d) mod p must be a square.  residue(ci, p, magic)
-// returns base mod p; step_mod(ci) returns step mod p.
+// returns base mod p; step_mod(ci) returns step mod p; aff holds the curve's
+// 36 candidate bitmasks in shared memory.
 template <typename Residue, typename StepMod>
 __device__ __forceinline__ u64 stage2(u64 m, const int *s_ci, const u32 *s_dinv,
                                       const Candidates &cand, const u64 *aff, Residue residue,
@@ -260,7 +263,7 @@ __device__ __forceinline__ u64 stage2(u64 m, const int *s_ci, const u32 *s_dinv,
             const int j = __ffsll((long long)rest) - 1;
             rest &= rest - 1;
             const u32 x = mod_small(x0 + u32(j) * dx, p, magic);
-            if (!((__ldg(bits + (x >> 6)) >> (x & 63)) & 1)) m &= ~(u64(1) << j);
+            if (!((bits[x >> 6] >> (x & 63)) & 1)) m &= ~(u64(1) << j);
         }
     }
     return m;
@@ -299,7 +302,7 @@ __device__ __forceinline__ void emit(u64 m, long long base, long long step, long
 
 __device__ __forceinline__ void wide_drain(const u64 *qmask, const u32 *qinfo, int start, int n,
                                            const WideCurve &C, const Candidates &cand,
-                                           const u64 *affine, const int *s_ci, const u32 *s_dinv,
+                                           const u64 *s_aff, const int *s_ci, const u32 *s_dinv,
                                            const u32 *s_ofs, long long d, const BatchOut &out) {
     const int lane = threadIdx.x & 31;
     u64 m = 0;
@@ -313,7 +316,7 @@ __device__ __forceinline__ void wide_drain(const u64 *qmask, const u32 *qinfo, i
     const u32 ofs = s_ofs[info & ((1u << kClassBits) - 1)];
     if (m) {
         m = stage2(
-            m, s_ci, s_dinv, cand, affine + C.aff,
+            m, s_ci, s_dinv, cand, s_aff,
             [&](int ci, u32 p, u32 magic) {
                 u32 r = C.neg_h[ci] + mod_small(ofs, p, magic);
                 if (r >= p) r -= p;
@@ -325,13 +328,42 @@ __device__ __forceinline__ void wide_drain(const u64 *qmask, const u32 *qinfo, i
     emit(m, -C.bound + ofs + C.stride * off, C.class_mod, d, C.index, out);
 }
 
+// Position of the n-th set bit (n counted from 0) of a 64-bit mask that has
+// more than n set bits, by halving with population counts.
+__device__ __forceinline__ int nth_bit64(u64 mask, int n) {
+    int pos = 0;
+    int c = __popc(u32(mask));
+    if (n >= c) {
+        n -= c;
+        mask >>= 32;
+        pos = 32;
+    }
+    u32 m = u32(mask);
+    c = __popc(m & 0xFFFFu);
+    if (n >= c) { n -= c; m >>= 16; pos += 16; }
+    c = __popc(m & 0xFFu);
+    if (n >= c) { n -= c; m >>= 8; pos += 8; }
+    c = __popc(m & 0xFu);
+    if (n >= c) { n -= c; m >>= 4; pos += 4; }
+    c = __popc(m & 0x3u);
+    if (n >= c) { n -= c; m >>= 2; pos += 2; }
+    if (n >= int(m & 1u)) pos += 1;
+    return pos;
+}
+
+// Wide rows.  Per denominator: warp 0 selects the 32 reference primes, warp
+// 1 lays out the admissible classes and their sweep items, the other warps
+// wait; then every warp sweeps items.  The stage-1 rows of the next live
+// denominator of the item are copied (TMA bulk copies, one mbarrier per
+// buffer) into the other of two row buffers while this one is swept.
 __global__ void __launch_bounds__(kWThreads, 3)
     wide_kernel(const WideCurve *__restrict__ curves, const BatchItem *__restrict__ items,
                 int nitems, const u64 *__restrict__ pool, const u64 *__restrict__ affine,
                 const unsigned short *__restrict__ inv_table, Candidates cand, BatchOut out,
-                unsigned long long *work) {
+                int row_stride, unsigned long long *work) {
     extern __shared__ __align__(16) u64 smem[];
     __shared__ WideCurve C;
+    __shared__ u64 s_aff[kAffWords];
     __shared__ int s_item;
     __shared__ u32 s_ofs[kMaxClasses];
     __shared__ int s_wtile[kMaxClasses];
@@ -341,15 +373,21 @@ __global__ void __launch_bounds__(kWThreads, 3)
     __shared__ u32 s_dinv[kSelectedPrimes];
     __shared__ int s_next;
     __shared__ int s_abort;
-    __shared__ __align__(8) unsigned long long s_bar;
+    __shared__ __align__(8) unsigned long long s_bar[2];
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const u32 bar = smem_addr(&s_bar);
-    u32 phase = 0;
+    u64 *qmask = smem + 2 * row_stride;
+    u32 *qinfo = reinterpret_cast<u32 *>(qmask + kWWarps * kQueue);
+    u32 *s_start = qinfo + kWWarps * kQueue;  // [kMaxClasses][kWideSlots]
+    u64 *wq_mask = qmask + warp * kQueue;
+    u32 *wq_info = qinfo + warp * kQueue;
+    u32 phase = 0;     // bit b: parity of buffer b's next completion
+    u32 pending = 0;   // bit b: a copy into buffer b is in flight and not yet waited for
     int cur = -1;
     if (threadIdx.x == 0) {
-        mbar_init(bar, 1);
+        mbar_init(smem_addr(&s_bar[0]), 1);
+        mbar_init(smem_addr(&s_bar[1]), 1);
         s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -365,42 +403,51 @@ __global__ void __launch_bounds__(kWThreads, 3)
             const u32 *src = reinterpret_cast<const u32 *>(curves + item.curve);
             u32 *dst = reinterpret_cast<u32 *>(&C);
             for (int i = threadIdx.x; i < int(sizeof(WideCurve) / 4); i += kWThreads) dst[i] = src[i];
+            const u64 *aff_src = affine + curves[item.curve].aff;
+            for (int i = threadIdx.x; i < kAffWords; i += kWThreads) s_aff[i] = __ldg(aff_src + i);
             cur = item.curve;
             __syncthreads();
         }
-        u64 *rows = smem;
-        u64 *qmask = rows + C.smem_words;
-        u32 *qinfo = reinterpret_cast<u32 *>(qmask + kWWarps * kQueue);
-        u32 *s_start = qinfo + kWWarps * kQueue;  // [kMaxClasses][kWideSlots]
-        u64 *wq_mask = qmask + warp * kQueue;
-        u32 *wq_info = qinfo + warp * kQueue;
-        const u32 rows_addr = smem_addr(rows);
-        const unsigned char *sbase = reinterpret_cast<const unsigned char *>(rows);
         const int q = C.class_prime;
         const int M = C.class_mod;
-
-        for (int i = 0; i < item.count; ++i) {
+        // parameters whose denominator has no admissible class are skipped
+        auto live = [&](int i) {
+            const long long k = item.first + i;
+            const u32 du = u32(C.square ? k * k : k);
+            return C.admissible[du & 63] != 0 && (q == 1 || C.admissible[64 + int(du % u32(q))] != 0);
+        };
+        auto stage_rows = [&](int i, int b) {  // thread 0: copy parameter i's rows into buffer b
+            const long long k = item.first + i;
+            const u32 du = u32(C.square ? k * k : k);
+            const u32 bar = smem_addr(&s_bar[b]);
+            const u32 dst = smem_addr(smem + b * row_stride);
+            fence_proxy_async_shared();
+            mbar_arrive_expect_tx(bar, u32(C.smem_words) * 8u);
+#pragma unroll
+            for (int sl = 0; sl < kWideSlots; ++sl) {
+                const Modulus &Md = C.mod[sl];
+                const u32 rho = mod_u32(du, u32(Md.m), Md.magic);
+                bulk_copy_to_shared(dst + u32(Md.smem_offset) * 8u,
+                                    pool + Md.offset + (long long)rho * Md.length,
+                                    u32(Md.length) * 8u, bar);
+            }
+        };
+        int i = 0;
+        while (i < item.count && !live(i)) ++i;
+        int b = 0;
+        if (i < item.count) {
+            if (threadIdx.x == 0) stage_rows(i, b);
+            pending |= 1u << b;
+        }
+        while (i < item.count) {
             const long long k = item.first + i;
             const long long d = C.square ? k * k : k;
             const u32 du = u32(d);
             const u64 classes2 = C.admissible[du & 63];
             const u64 classesq = q > 1 ? C.admissible[64 + int(du % u32(q))] : u64(1);
-            if (!classes2 || !classesq) continue;
             const int nq = __popcll(classesq);
             const int nclass = __popcll(classes2) * nq;
 
-            if (threadIdx.x == 0) {
-                fence_proxy_async_shared();
-                mbar_arrive_expect_tx(bar, u32(C.smem_words) * 8u);
-#pragma unroll
-                for (int sl = 0; sl < kWideSlots; ++sl) {
-                    const Modulus &Md = C.mod[sl];
-                    const u32 rho = mod_u32(du, u32(Md.m), Md.magic);
-                    bulk_copy_to_shared(rows_addr + u32(Md.smem_offset) * 8u,
-                                        pool + Md.offset + (long long)rho * Md.length,
-                                        u32(Md.length) * 8u, bar);
-                }
-            }
             if (warp == 0) {
                 select_warp(du, cand, inv_table, s_ci, s_dinv);
                 if (lane == 0) s_next = 0;
@@ -412,14 +459,10 @@ __global__ void __launch_bounds__(kWThreads, 3)
                     const int c = base + lane;
                     int nitems_c = 0;
                     if (c < nclass) {
-                        u64 b2 = classes2;
-                        for (int t = c / nq; t > 0; --t) b2 &= b2 - 1;
-                        const int r64 = __ffsll((long long)b2) - 1;
+                        const int r64 = nth_bit64(classes2, c / nq);
                         int r = r64;
                         if (q > 1) {
-                            u64 bq = classesq;
-                            for (int t = c % nq; t > 0; --t) bq &= bq - 1;
-                            const int rq = __ffsll((long long)bq) - 1;
+                            const int rq = nth_bit64(classesq, c % nq);
                             r = r64 + 64 * int(C.crt[C.mod_q[r64] * 13 + rq]);
                         }
                         int ofs = r + C.h_mod_m;
@@ -451,12 +494,21 @@ __global__ void __launch_bounds__(kWThreads, 3)
                 if (lane == 0) s_prefix[nclass] = carry;
             }
             __syncthreads();
-            if (!mbar_wait(bar, phase)) {  // rows landed (bounded wait)
+            // every warp is past the previous sweep: the other buffer is free
+            int next = i + 1;
+            while (next < item.count && !live(next)) ++next;
+            if (next < item.count) {
+                if (threadIdx.x == 0) stage_rows(next, b ^ 1);
+                pending |= 1u << (b ^ 1);
+            }
+            if (!mbar_wait(smem_addr(&s_bar[b]), (phase >> b) & 1u)) {  // bounded wait
                 s_abort = 1;
                 if (out.error) atomicOr(out.error, 1ull);
             }
-            phase ^= 1u;
+            phase ^= 1u << b;
+            pending &= ~(1u << b);
 
+            const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
             const int total_items = s_prefix[nclass];
             int qn = 0;
             u32 step8[kWideSlots], mod8[kWideSlots];
@@ -475,9 +527,9 @@ __global__ void __launch_bounds__(kWThreads, 3)
                 int c = 0;
                 for (int base = 0; base < nclass; base += 32) {
                     const int cc = base + lane;
-                    const u32 b = __ballot_sync(kFullMask, cc < nclass && s_prefix[cc] <= sweep);
-                    if (b) c = base + 31 - __clz(b);
-                    if (b != kFullMask) break;
+                    const u32 bb = __ballot_sync(kFullMask, cc < nclass && s_prefix[cc] <= sweep);
+                    if (bb) c = base + 31 - __clz(bb);
+                    if (bb != kFullMask) break;
                 }
                 const int w0 = (sweep - s_prefix[c]) * kWItemWords;
                 const int wt = s_wtile[c];
@@ -515,18 +567,18 @@ __global__ void __launch_bounds__(kWThreads, 3)
                         const int w = ws + kWarpSize * kk + lane;
                         u64 a = acc[kk];
                         if (w == wt - 1) a &= last_mask;
-                        const bool live = a != 0 && w < wt;
-                        const u32 b = __ballot_sync(kFullMask, live);
-                        if (b) {
-                            const int pos = qn + __popc(b & lanemask_lt());
-                            if (live) {
+                        const bool live_word = a != 0 && w < wt;
+                        const u32 bb = __ballot_sync(kFullMask, live_word);
+                        if (bb) {
+                            const int pos = qn + __popc(bb & lanemask_lt());
+                            if (live_word) {
                                 wq_mask[pos] = a;
                                 wq_info[pos] = (u32(w) << kClassBits) | u32(c);
                             }
-                            qn += __popc(b);
+                            qn += __popc(bb);
                             if (qn >= 32) {
                                 __syncwarp();
-                                wide_drain(wq_mask, wq_info, qn - 32, 32, C, cand, affine, s_ci,
+                                wide_drain(wq_mask, wq_info, qn - 32, 32, C, cand, s_aff, s_ci,
                                            s_dinv, s_ofs, d, out);
                                 qn -= 32;
                             }
@@ -535,14 +587,21 @@ __global__ void __launch_bounds__(kWThreads, 3)
                 }
             }
             __syncwarp();
-            wide_drain(wq_mask, wq_info, 0, qn, C, cand, affine, s_ci, s_dinv, s_ofs, d, out);
+            wide_drain(wq_mask, wq_info, 0, qn, C, cand, s_aff, s_ci, s_dinv, s_ofs, d, out);
             __syncthreads();
             if (s_abort) {
-                // a bulk copy did not complete in time: give in-flight copies a
-                // last bounded chance to land, then leave (the host reports it)
-                if (threadIdx.x == 0) mbar_wait(bar, phase ^ 1u);
+                // a bulk copy did not complete in time: give the copies in
+                // flight a last bounded chance to land, then leave (the host
+                // reports the error word)
+                if (threadIdx.x == 0) {
+                    mbar_wait(smem_addr(&s_bar[b]), ((phase >> b) & 1u) ^ 1u);
+                    if (pending & (1u << (b ^ 1)))
+                        mbar_wait(smem_addr(&s_bar[b ^ 1]), (phase >> (b ^ 1)) & 1u);
+                }
                 return;
             }
+            i = next;
+            b ^= 1;
         }
         __syncthreads();
     }
@@ -553,7 +612,7 @@ __global__ void __launch_bounds__(kWThreads, 3)
 
 __device__ __forceinline__ void narrow_drain(const u64 *qmask, const u32 *qword, int start, int n,
                                              const NarrowCurve &C, const Candidates &cand,
-                                             const u64 *affine, const int *s_ci, const u32 *s_dinv,
+                                             const u64 *s_aff, const int *s_ci, const u32 *s_dinv,
                                              long long d, const BatchOut &out) {
     const int lane = threadIdx.x & 31;
     u64 m = 0;
@@ -565,7 +624,7 @@ __device__ __forceinline__ void narrow_drain(const u64 *qmask, const u32 *qword,
     __syncwarp();
     if (m) {
         m = stage2(
-            m, s_ci, s_dinv, cand, affine + C.aff,
+            m, s_ci, s_dinv, cand, s_aff,
             [&](int ci, u32 p, u32 magic) {
                 const u32 r = C.neg_h[ci] + mod_small(64u * mod_small(w, p, magic), p, magic);
                 return r >= p ? r - p : r;
@@ -592,8 +651,10 @@ __global__ void __launch_bounds__(kNThreads, 3)
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const u64 *tab = smem;
-    u64 *wq_mask = smem + kNarrowTableWords + warp * kQueue;
-    u32 *wq_word = reinterpret_cast<u32 *>(smem + kNarrowTableWords + kNWarps * kQueue) + warp * kQueue;
+    const u64 *s_aff = smem + kNarrowTableWords;  // the curve's 36 candidate bitmasks
+    u64 *wq_mask = smem + kNarrowTableWords + kAffWords + warp * kQueue;
+    u32 *wq_word =
+        reinterpret_cast<u32 *>(smem + kNarrowTableWords + kAffWords + kNWarps * kQueue) + warp * kQueue;
     const u32 bar = smem_addr(&s_bar);
     u32 phase = 0;
     int cur = -1;
@@ -621,8 +682,10 @@ __global__ void __launch_bounds__(kNThreads, 3)
             __syncthreads();
             if (threadIdx.x == 0) {
                 fence_proxy_async_shared();
-                mbar_arrive_expect_tx(bar, u32(C.table_words) * 8u);
+                mbar_arrive_expect_tx(bar, u32(C.table_words + kAffWords) * 8u);
                 bulk_copy_to_shared(smem_addr(smem), pool + C.tables, u32(C.table_words) * 8u, bar);
+                bulk_copy_to_shared(smem_addr(smem + kNarrowTableWords), affine + C.aff,
+                                    u32(kAffWords) * 8u, bar);
             }
             if (!mbar_wait(bar, phase)) {
                 s_abort = 1;
@@ -686,14 +749,14 @@ __global__ void __launch_bounds__(kNThreads, 3)
                         selected = true;
                     }
                     __syncwarp();
-                    narrow_drain(wq_mask, wq_word, qn - 32, 32, C, cand, affine, w_ci, w_dinv, d, out);
+                    narrow_drain(wq_mask, wq_word, qn - 32, 32, C, cand, s_aff, w_ci, w_dinv, d, out);
                     qn -= 32;
                 }
             }
             if (qn) {
                 if (!selected) select_warp(du, cand, inv_table, w_ci, w_dinv);
                 __syncwarp();
-                narrow_drain(wq_mask, wq_word, 0, qn, C, cand, affine, w_ci, w_dinv, d, out);
+                narrow_drain(wq_mask, wq_word, 0, qn, C, cand, s_aff, w_ci, w_dinv, d, out);
             }
         }
         __syncthreads();
@@ -1156,11 +1219,11 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
         int sms = 0;
         check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id),
                    "cudaDeviceGetAttribute");
-        const std::size_t wide_smem = std::size_t(wide_smem_words) * 8 +
+        const std::size_t wide_smem = 2 * std::size_t(wide_smem_words) * 8 +
                                       std::size_t(dev::kWWarps) * dev::kQueue * 12 +
                                       std::size_t(dev::kMaxClasses) * dev::kWideSlots * 4;
-        const std::size_t narrow_smem =
-            std::size_t(dev::kNarrowTableWords) * 8 + std::size_t(dev::kNWarps) * dev::kQueue * 12;
+        const std::size_t narrow_smem = std::size_t(dev::kNarrowTableWords + dev::kAffWords) * 8 +
+                                        std::size_t(dev::kNWarps) * dev::kQueue * 12;
         int wide_grid = 0, narrow_grid = 0;
         if (!wide.empty()) {
             int per_sm = 0;
@@ -1206,7 +1269,7 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
             if (wide_grid) {
                 dev::wide_kernel<<<wide_grid, dev::kWThreads, wide_smem, stream>>>(
                     d_wide.p, d_witems.p, int(wide_items.size()), d_rows.p, d_aff.p, d_inv.p, cand,
-                    out, d_counters.p + 1);
+                    out, wide_smem_words, d_counters.p + 1);
                 check_cuda(cudaGetLastError(), "wide_kernel launch");
             }
             record(ev[3], stream);

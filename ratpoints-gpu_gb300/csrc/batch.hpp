@@ -28,7 +28,7 @@
 namespace rpg {
 
 constexpr long long kBatchWideWords = 2048;
-constexpr int kBatchNarrowModulus = 36;
+constexpr int kBatchNarrowModulus = 34;
 
 struct BatchCurveSpec {
     std::vector<std::string> coefficients;
