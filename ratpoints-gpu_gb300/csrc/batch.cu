@@ -41,6 +41,7 @@ constexpr int kNarrowTableWords = 7040;                 // sum of m^2 (+ padding
 constexpr int kAffWords = kCandidatePrimes * 8;         // the 36 candidate bitmasks
 constexpr int kRefWords = 8;                            // u64 words of a bitmask over [0, 512)
 constexpr int kMaxFactors = 4;
+constexpr int kMaxIntervals = 8;                        // more: sweep the whole row
 
 static_assert(kMaxClasses <= (1 << kClassBits), "class index must fit the queue entry");
 
@@ -75,6 +76,9 @@ struct WideCurve {
     unsigned short m_mod[kCandidatePrimes];   // M mod p
     unsigned char crt[13 * 13];    // [r64 mod q][rq] -> t with r = r64 + 64 t (mod 64 q)
     unsigned char mod_q[64];       // r64 mod q
+    int nint;                      // x intervals (0: the whole row)
+    double lo[kMaxIntervals];      // ascending lower bounds (-inf: none)
+    double hi[kMaxIntervals];      // upper bounds (+inf: none)
 };
 
 struct NarrowCurve {
@@ -92,6 +96,9 @@ struct NarrowCurve {
     u32 shift[kNarrowSlots];       // (-H) 64^-1 mod m: table word of row word 0
     u32 step[kNarrowSlots];        // 32 mod m
     unsigned short neg_h[kCandidatePrimes];
+    int nint;
+    double lo[kMaxIntervals];
+    double hi[kMaxIntervals];
 };
 
 static_assert(sizeof(WideCurve) % 4 == 0 && sizeof(NarrowCurve) % 4 == 0, "u32 copies");
@@ -100,7 +107,46 @@ struct BatchItem {
     long long first;               // first parameter k
     int curve;                     // descriptor index
     int count;                     // parameters in this item
+    int range;                     // which numerator range of each denominator (see x_ranges)
+    int pad;
 };
+
+// Numerator ranges of denominator d for x in the curve's intervals: each
+// interval [lo, hi] gives a in [floor(lo d) - 1, ceil(hi d) + 1] (widened by
+// one so that double rounding never drops a site; the host applies the exact
+// interval test), clipped to [-H, H]; overlapping ranges are merged.  Sets
+// [L, U] to the want-th of the disjoint ascending ranges and returns false if
+// there are not that many.  Without intervals the one range is [-H, H].
+__device__ __forceinline__ bool x_range(const double *lo, const double *hi, int nint, long long H,
+                                        long long d, int want, long long &L, long long &U) {
+    if (nint == 0) {
+        L = -H;
+        U = H;
+        return want == 0;
+    }
+    const double dd = double(d), h = double(H);
+    int n = -1;
+    long long cl = 0, cu = -1;
+    for (int i = 0; i < nint; ++i) {
+        const double x = floor(lo[i] * dd) - 1.0;
+        const double y = ceil(hi[i] * dd) + 1.0;
+        const long long l = !(x > -h) ? -H : (x > h ? H + 1 : (long long)x);
+        const long long u = !(y < h) ? H : (y < -h ? -H - 1 : (long long)y);
+        if (l > u) continue;
+        if (n >= 0 && l <= cu + 1) {
+            if (u > cu) cu = u;
+            continue;
+        }
+        if (n == want) break;
+        ++n;
+        cl = l;
+        cu = u;
+    }
+    if (n != want) return false;
+    L = cl;
+    U = cu;
+    return true;
+}
 
 struct AffineSpec {                // bitmask of x in [0, p) with f(x) a square mod p
     long long out;                 // u64 offset of the 8-word output
@@ -300,10 +346,21 @@ __device__ __forceinline__ void emit(u64 m, long long base, long long step, long
 // ---------------------------------------------------------------------------
 // Wide rows: class layout, one CTA per denominator.
 
+// One admissible class of one denominator: words [wbase, wbase + words) of
+// the class hold its sites in the numerator range being swept; the first
+// word drops its `first` low bits, the last keeps its `last` low bits.
+struct ClassRun {
+    int wbase;
+    int words;
+    unsigned short ofs;            // (r + H) mod M: the class's least a is -H + ofs
+    unsigned char first;
+    unsigned char last;
+};
+
 __device__ __forceinline__ void wide_drain(const u64 *qmask, const u32 *qinfo, int start, int n,
                                            const WideCurve &C, const Candidates &cand,
                                            const u64 *s_aff, const int *s_ci, const u32 *s_dinv,
-                                           const u32 *s_ofs, long long d, const BatchOut &out) {
+                                           const ClassRun *s_run, long long d, const BatchOut &out) {
     const int lane = threadIdx.x & 31;
     u64 m = 0;
     u32 info = 0;
@@ -313,7 +370,7 @@ __device__ __forceinline__ void wide_drain(const u64 *qmask, const u32 *qinfo, i
     }
     __syncwarp();
     const u32 off = info >> kClassBits;
-    const u32 ofs = s_ofs[info & ((1u << kClassBits) - 1)];
+    const u32 ofs = s_run[info & ((1u << kClassBits) - 1)].ofs;
     if (m) {
         m = stage2(
             m, s_ci, s_dinv, cand, s_aff,
@@ -365,9 +422,7 @@ __global__ void __launch_bounds__(kWThreads, 3)
     __shared__ WideCurve C;
     __shared__ u64 s_aff[kAffWords];
     __shared__ int s_item;
-    __shared__ u32 s_ofs[kMaxClasses];
-    __shared__ int s_wtile[kMaxClasses];
-    __shared__ int s_last_bits[kMaxClasses];
+    __shared__ ClassRun s_run[kMaxClasses];
     __shared__ int s_prefix[kMaxClasses + 1];
     __shared__ int s_ci[kSelectedPrimes];
     __shared__ u32 s_dinv[kSelectedPrimes];
@@ -410,11 +465,17 @@ __global__ void __launch_bounds__(kWThreads, 3)
         }
         const int q = C.class_prime;
         const int M = C.class_mod;
-        // parameters whose denominator has no admissible class are skipped
+        // parameters whose denominator has no admissible class, or no
+        // numerator range of this item's index, are skipped
         auto live = [&](int i) {
             const long long k = item.first + i;
-            const u32 du = u32(C.square ? k * k : k);
-            return C.admissible[du & 63] != 0 && (q == 1 || C.admissible[64 + int(du % u32(q))] != 0);
+            const long long d = C.square ? k * k : k;
+            const u32 du = u32(d);
+            if (C.admissible[du & 63] == 0 || (q > 1 && C.admissible[64 + int(du % u32(q))] == 0))
+                return false;
+            if (C.nint == 0) return true;
+            long long L, U;
+            return x_range(C.lo, C.hi, C.nint, C.bound, d, item.range, L, U);
         };
         auto stage_rows = [&](int i, int b) {  // thread 0: copy parameter i's rows into buffer b
             const long long k = item.first + i;
@@ -452,6 +513,9 @@ __global__ void __launch_bounds__(kWThreads, 3)
                 select_warp(du, cand, inv_table, s_ci, s_dinv);
                 if (lane == 0) s_next = 0;
             } else if (warp == 1) {
+                // the numerator range [lo_a, hi_a] of this item for d
+                long long lo_a = -C.bound, hi_a = C.bound;
+                if (C.nint > 0) x_range(C.lo, C.hi, C.nint, C.bound, d, item.range, lo_a, hi_a);
                 // classes, 32 per pass: class c = (c / nq)-th 2-adic class crossed
                 // with the (c % nq)-th admissible residue mod q; item prefix by scan
                 int carry = 0;
@@ -467,12 +531,31 @@ __global__ void __launch_bounds__(kWThreads, 3)
                         }
                         int ofs = r + C.h_mod_m;
                         if (ofs >= M) ofs -= M;
-                        // sites of class r: a = -H + ofs + M t, t in [0, count)
+                        // sites of class r: a = -H + ofs + M t, t in [0, count); those
+                        // in [lo_a, hi_a] are t in [t_lo, t_hi]
                         const long long count = C.count_q + (ofs <= C.count_r ? 1 : 0);
-                        const long long words = (count + 63) >> 6;
-                        s_ofs[c] = u32(ofs);
-                        s_wtile[c] = int(words);
-                        s_last_bits[c] = words > 0 ? int(count - 64 * (words - 1)) : 64;
+                        long long t_lo = 0, t_hi = count - 1;
+                        if (C.nint > 0) {
+                            const long long a0 = -C.bound + ofs;
+                            const long long below = lo_a - a0;
+                            t_lo = below <= 0 ? 0 : (below + M - 1) / M;
+                            const long long above = hi_a - a0;
+                            t_hi = above < 0 ? -1 : min(count - 1, above / M);
+                        }
+                        ClassRun run;
+                        run.ofs = (unsigned short)ofs;
+                        if (t_lo <= t_hi) {
+                            run.wbase = int(t_lo >> 6);
+                            run.words = int((t_hi >> 6) - (t_lo >> 6) + 1);
+                            run.first = (unsigned char)(t_lo & 63);
+                            run.last = (unsigned char)((t_hi & 63) + 1);
+                        } else {
+                            run.wbase = 0;
+                            run.words = 0;
+                            run.first = 0;
+                            run.last = 64;
+                        }
+                        s_run[c] = run;
 #pragma unroll
                         for (int sl = 0; sl < kWideSlots; ++sl) {
                             const Modulus &Md = C.mod[sl];
@@ -480,7 +563,7 @@ __global__ void __launch_bounds__(kWThreads, 3)
                             s_start[c * kWideSlots + sl] =
                                 mod_u32(a0m * Md.inv_stride, u32(Md.m), Md.magic);
                         }
-                        nitems_c = int((words + kWItemWords - 1) / kWItemWords);
+                        nitems_c = (run.words + kWItemWords - 1) / kWItemWords;
                     }
                     int incl = nitems_c;
 #pragma unroll
@@ -532,13 +615,14 @@ __global__ void __launch_bounds__(kWThreads, 3)
                     if (bb != kFullMask) break;
                 }
                 const int w0 = (sweep - s_prefix[c]) * kWItemWords;
-                const int wt = s_wtile[c];
-                const u64 last_mask =
-                    s_last_bits[c] >= 64 ? ~u64(0) : ((u64(1) << s_last_bits[c]) - 1);
+                const ClassRun run = s_run[c];
+                const int wt = run.words;
+                const u64 first_mask = ~u64(0) << run.first;
+                const u64 last_mask = run.last >= 64 ? ~u64(0) : ((u64(1) << run.last) - 1);
                 u32 o[kWideSlots];
 #pragma unroll
                 for (int sl = 0; sl < kWideSlots; ++sl)
-                    o[sl] = 8u * mod_u32(s_start[c * kWideSlots + sl] + u32(w0 + lane),
+                    o[sl] = 8u * mod_u32(s_start[c * kWideSlots + sl] + u32(run.wbase + w0 + lane),
                                          u32(C.mod[sl].m), C.mod[sl].magic);
 #pragma unroll 1
                 for (int step = 0; step < kWSteps; ++step) {
@@ -566,6 +650,7 @@ __global__ void __launch_bounds__(kWThreads, 3)
                     for (int kk = 0; kk < kWK; ++kk) {
                         const int w = ws + kWarpSize * kk + lane;
                         u64 a = acc[kk];
+                        if (w == 0) a &= first_mask;
                         if (w == wt - 1) a &= last_mask;
                         const bool live_word = a != 0 && w < wt;
                         const u32 bb = __ballot_sync(kFullMask, live_word);
@@ -573,13 +658,13 @@ __global__ void __launch_bounds__(kWThreads, 3)
                             const int pos = qn + __popc(bb & lanemask_lt());
                             if (live_word) {
                                 wq_mask[pos] = a;
-                                wq_info[pos] = (u32(w) << kClassBits) | u32(c);
+                                wq_info[pos] = (u32(run.wbase + w) << kClassBits) | u32(c);
                             }
                             qn += __popc(bb);
                             if (qn >= 32) {
                                 __syncwarp();
                                 wide_drain(wq_mask, wq_info, qn - 32, 32, C, cand, s_aff, s_ci,
-                                           s_dinv, s_ofs, d, out);
+                                           s_dinv, s_run, d, out);
                                 qn -= 32;
                             }
                         }
@@ -587,7 +672,7 @@ __global__ void __launch_bounds__(kWThreads, 3)
                 }
             }
             __syncwarp();
-            wide_drain(wq_mask, wq_info, 0, qn, C, cand, s_aff, s_ci, s_dinv, s_ofs, d, out);
+            wide_drain(wq_mask, wq_info, 0, qn, C, cand, s_aff, s_ci, s_dinv, s_run, d, out);
             __syncthreads();
             if (s_abort) {
                 // a bulk copy did not complete in time: give the copies in
@@ -698,9 +783,6 @@ __global__ void __launch_bounds__(kNThreads, 3)
                 return;
             }
         }
-        const long long W = C.words;
-        const int last_bits = int(2 * C.bound + 1 - 64 * (W - 1));
-        const u64 last_mask = last_bits >= 64 ? ~u64(0) : ((u64(1) << last_bits) - 1);
         int *w_ci = s_ci[warp];
         u32 *w_dinv = s_dinv[warp];
         for (;;) {
@@ -713,6 +795,13 @@ __global__ void __launch_bounds__(kNThreads, 3)
             const u32 du = u32(d);
             const u64 mask2 = C.dense2[du & 63];
             if (!mask2) continue;
+            // words [w_lo, w_hi] hold the numerator range of this item: a in [L, U]
+            long long L = -C.bound, U = C.bound;
+            if (C.nint > 0 && !x_range(C.lo, C.hi, C.nint, C.bound, d, item.range, L, U)) continue;
+            const int w_lo = int((L + C.bound) >> 6), w_hi = int((U + C.bound) >> 6);
+            const u64 first_mask = ~u64(0) << ((L + C.bound) & 63);
+            const int last_bits = int((U + C.bound) & 63) + 1;
+            const u64 last_mask = last_bits >= 64 ? ~u64(0) : ((u64(1) << last_bits) - 1);
             u32 base[kNarrowSlots], at[kNarrowSlots], mods[kNarrowSlots], steps[kNarrowSlots];
 #pragma unroll
             for (int s = 0; s < kNarrowSlots; ++s) {
@@ -720,12 +809,12 @@ __global__ void __launch_bounds__(kNThreads, 3)
                 mods[s] = m;
                 steps[s] = C.step[s];
                 base[s] = u32(C.off[s]) + mod_u32(du, m, C.magic[s]) * m;
-                at[s] = mod_u32(C.shift[s] + u32(lane), m, C.magic[s]);
+                at[s] = mod_u32(C.shift[s] + u32(w_lo + lane), m, C.magic[s]);
             }
             bool selected = false;
             int qn = 0;
-            for (long long w0 = 0; w0 < W; w0 += kWarpSize) {
-                const long long w = w0 + lane;
+            for (int w0 = w_lo; w0 <= w_hi; w0 += kWarpSize) {
+                const int w = w0 + lane;
                 u64 acc = mask2;
 #pragma unroll
                 for (int s = 0; s < kNarrowSlots; ++s) {
@@ -733,8 +822,9 @@ __global__ void __launch_bounds__(kNThreads, 3)
                     const u32 t = at[s] + steps[s];  // advance 32 words mod m
                     at[s] = min(t, t - mods[s]);
                 }
-                if (w >= W) acc = 0;
-                else if (w == W - 1) acc &= last_mask;
+                if (w > w_hi) acc = 0;
+                if (w == w_lo) acc &= first_mask;
+                if (w == w_hi) acc &= last_mask;
                 const u32 b = __ballot_sync(kFullMask, acc != 0);
                 if (!b) continue;
                 const int pos = qn + __popc(b & lanemask_lt());
@@ -876,6 +966,48 @@ void two_adic_classes(const std::vector<std::string> &coefficients, dev::u64 out
 }
 
 int round_even(long long v) { return int((v + 1) & ~1LL); }
+
+// A rational bound as a double (leading 18 digits of numerator and
+// denominator), +-inf beyond 1e300: the device widens every range by one site,
+// far more than this rounding can move a bound that matters (|x d| <= 2^36).
+double approx_value(const Rational &r) {
+    auto split = [](const BigInt &v, double &mant, long &exp10) {
+        std::string t = v.to_string();
+        const bool neg = !t.empty() && t[0] == '-';
+        if (neg) t.erase(0, 1);
+        const std::size_t keep = std::min<std::size_t>(t.size(), 18);
+        mant = std::stod(t.substr(0, keep));
+        exp10 = long(t.size() - keep);
+        if (neg) mant = -mant;
+    };
+    double mn, md;
+    long en, ed;
+    split(r.num, mn, en);
+    split(r.den, md, ed);
+    if (mn == 0) return 0.0;
+    const long e = en - ed;
+    if (e > 300) return mn > 0 ? HUGE_VAL : -HUGE_VAL;
+    if (e < -300) return 0.0;
+    return mn / md * std::pow(10.0, double(e));
+}
+
+// The intervals as ascending (lo, hi) doubles for the device ranges; false
+// when there are none or more than the device takes (then rows are swept whole).
+bool device_intervals(const std::vector<SearchInterval> &intervals, int &nint, double *lo, double *hi) {
+    nint = 0;
+    if (intervals.empty() || intervals.size() > std::size_t(dev::kMaxIntervals)) return false;
+    std::vector<std::pair<double, double>> v;
+    for (const auto &iv : intervals)
+        v.push_back({iv.lower_infinite ? -HUGE_VAL : approx_value(iv.lower),
+                     iv.upper_infinite ? HUGE_VAL : approx_value(iv.upper)});
+    std::sort(v.begin(), v.end());
+    for (const auto &p : v) {
+        lo[nint] = p.first;
+        hi[nint] = p.second;
+        ++nint;
+    }
+    return true;
+}
 
 struct CurveWork {
     bool ok = false;
@@ -1079,10 +1211,13 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
                 C.s_mod[ci] = (unsigned short)(S % p);
                 C.m_mod[ci] = (unsigned short)(M % p);
             }
-            // items of about 2^20 row words
+            device_intervals(c.intervals, C.nint, C.lo, C.hi);
+            // items of about 2^20 row words, one set per numerator range
             const long long chunk = std::max(1LL, std::min<long long>(1 << 16, (1LL << 20) / cw.words));
-            for (long long f = c.first; f <= c.last; f += chunk)
-                wide_items.push_back({f, int(wide.size()), int(std::min(chunk, c.last - f + 1))});
+            for (int range = 0; range < std::max(1, C.nint); ++range)
+                for (long long f = c.first; f <= c.last; f += chunk)
+                    wide_items.push_back({f, int(wide.size()), int(std::min(chunk, c.last - f + 1)),
+                                          range, 0});
             wide.push_back(C);
             stats.wide_curves += 1;
         } else {
@@ -1126,11 +1261,14 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
                 const int p = cands[ci];
                 C.neg_h[ci] = (unsigned short)((p - H % p) % p);
             }
+            device_intervals(c.intervals, C.nint, C.lo, C.hi);
             // items of about 2^16 words, at least one denominator per warp
             const long long chunk =
                 std::max<long long>(dev::kNWarps, std::min<long long>(1 << 14, (1LL << 16) / cw.words));
-            for (long long f = c.first; f <= c.last; f += chunk)
-                narrow_items.push_back({f, int(narrow.size()), int(std::min(chunk, c.last - f + 1))});
+            for (int range = 0; range < std::max(1, C.nint); ++range)
+                for (long long f = c.first; f <= c.last; f += chunk)
+                    narrow_items.push_back({f, int(narrow.size()),
+                                            int(std::min(chunk, c.last - f + 1)), range, 0});
             narrow.push_back(C);
         }
         stats.curves += 1;

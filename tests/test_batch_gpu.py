@@ -158,3 +158,57 @@ def test_survivor_overflow_rerun(rpg, golden, monkeypatch):
     small, _, surv_small, stats = rpg.batch_search(curves)
     assert small == full and surv_small == surv_full
     assert stats["survivors"] > 16
+
+
+def _decimal(a, d):
+    """a/d as an exact decimal string when d divides a power of ten, else None."""
+    k = 0
+    while (10**k) % d and k < 12:
+        k += 1
+    if (10**k) % d:
+        return None
+    n = a * (10**k // d)
+    sign = "-" if n < 0 else ""
+    digits = str(abs(n)).rjust(k + 1, "0")
+    return sign + (digits[:-k] + "." + digits[-k:] if k else digits)
+
+
+def test_interval_narrowing_matches_single_search(rpg, golden):
+    """Each denominator sweeps only the numerators of the x intervals: random
+    unions of intervals, exact one-point intervals at known points, infinite
+    and huge-exponent bounds, overlapping and unsorted intervals, and more
+    intervals than the device narrows (whole rows, host filter only)."""
+    dense = golden["dense"]["coefficients"].split()
+    mordell = ["17", "0", "0", "1"]  # y^2 = x^3 + 17: many points with small denominators
+    rng = random.Random(17)
+    known = [p for p in single(rpg, {"coefficients": mordell, "bound": 6000, "first": 1, "last": 400})
+             if p[2] != 0]
+    exact = [s for s in (_decimal(a, d) for a, _, d in known) if s is not None]
+    assert len(exact) >= 4
+    curves = []
+    for bound, last in ((6000, 400), (150000, 10)):
+        curves.append({"coefficients": mordell, "bound": bound, "first": 1, "last": last,
+                       "intervals": [(x, x) for x in exact[:4]]})
+        curves.append({"coefficients": dense, "bound": bound, "first": 1, "last": last,
+                       "intervals": [(None, "-2.5"), ("-3", "-1e0"), ("4e-1", "1e400"),
+                                     ("-1e-400", "0")]})
+        curves.append({"coefficients": dense, "bound": bound, "first": 1, "last": last,
+                       "intervals": [(str(-i - 0.5), str(-i)) for i in range(10)]})
+    for _ in range(24):
+        c = mixed_curves(rng, 1, (200, 120000), (1, 300), bits=10)[0]
+        ivs = []
+        for _ in range(3):
+            lo = rng.uniform(-8, 8)
+            ivs.append((f"{lo:.4f}", f"{lo + rng.uniform(0, 3):.4f}"))
+        c["intervals"] = ivs
+        curves.append(c)
+    curves = squarefree(rpg, curves)
+    points, status, survivors, stats = rpg.batch_search(curves)
+    assert all(s == 0 for s in status)
+    assert stats["wide_curves"] >= 4
+    for c, got in zip(curves, points):
+        assert got == single(rpg, c), c
+    full, _, full_survivors, _ = rpg.batch_search([dict(c, intervals=()) for c in curves[:2]])
+    # one-point intervals sweep a few numerators per denominator: what survives
+    # there is the points themselves and their unreduced multiples
+    assert survivors[0] < full_survivors[0] and survivors[1] < full_survivors[1]
