@@ -232,6 +232,55 @@ rpg_status rpg_batch_search(const rpg_search_options *curves, int32_t curve_coun
                             int32_t *curve_status, uint64_t *curve_survivors,
                             rpg_batch_stats *stats);
 
+/*
+ * Serving: searches submitted at any time, answered in batches that overlap
+ * on the device (continuous batching).  No counterpart in the reference,
+ * which runs one search per process (src/main.cpp:48-85).
+ *
+ * `lanes` batch engines, each with its own CUDA streams and device buffers
+ * kept resident across batches, take batches from one dispatcher: whenever a
+ * lane is free and requests wait, waiting requests are admitted in arrival
+ * order while their estimated device bytes (tables, bitmasks, work items)
+ * fit the lane's share of memory_budget_bytes.  Each answer is what
+ * rpg_point_search reports for the same options: all points in order, or
+ * with first_point_only only the first (the -1 option).  First-point
+ * requests are searched in denominator waves of growing size and stop at the
+ * first wave holding an accepted point.
+ */
+typedef struct rpg_server rpg_server;
+
+typedef struct rpg_server_options {
+    int32_t device;                 /* CUDA device ordinal, -1: current */
+    int32_t lanes;                  /* concurrent batches, 1..16 */
+    uint64_t memory_budget_bytes;   /* device bytes for all lanes' batches */
+    int32_t max_batch_curves;       /* requests per batch */
+} rpg_server_options;
+
+typedef struct rpg_request_stats {
+    double latency_ms;              /* submit -> answer */
+    double queue_ms;                /* submit -> first batch start */
+    double rectangle_sites;         /* (2H + 1) x denominators searched */
+    uint64_t survivors;             /* modular survivors of the request */
+    uint64_t points;                /* points in the answer */
+    int32_t waves;                  /* batch entries the request took */
+} rpg_request_stats;
+
+rpg_status rpg_server_create(const rpg_server_options *options, rpg_server **server);
+/* Fails with RPG_E_ARG for invalid options (as rpg_point_search would);
+ * batch_size, plan, device and verify_threads of the request are ignored. */
+rpg_status rpg_server_submit(rpg_server *server, const rpg_search_options *request,
+                             int32_t first_point_only, uint64_t *request_id);
+/* Waits up to timeout_ms (negative: no limit).  *done = 0 on timeout (RPG_OK).
+ * When the request is done, *done = 1, its points go to callback in order
+ * (returning 0 stops the delivery), the request is retired, and the call
+ * returns the request's own status (RPG_OK, RPG_E_NOT_SQUAREFREE, ...).
+ * One waiter per request. */
+rpg_status rpg_server_wait(rpg_server *server, uint64_t request_id, double timeout_ms,
+                           rpg_point_cb callback, void *user, int32_t *done,
+                           rpg_request_stats *stats);
+/* Finishes the admitted work, then releases the server. */
+void rpg_server_destroy(rpg_server *server);
+
 int32_t rpg_device_count(void);
 int32_t rpg_abi_version(void);
 const char *rpg_last_error(void);

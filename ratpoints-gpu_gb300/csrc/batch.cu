@@ -865,17 +865,27 @@ double ms_since(Clock::time_point t0) {
     return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
 }
 
+// Grow-only device array: kept across runs, reallocated only when a run
+// needs more room than it has.
 template <typename T>
 struct DeviceArray {
     T *p = nullptr;
+    std::size_t cap = 0;
+    DeviceArray() = default;
+    DeviceArray(const DeviceArray &) = delete;
+    DeviceArray &operator=(const DeviceArray &) = delete;
     ~DeviceArray() { cudaFree(p); }
-    void alloc(std::size_t count, const char *what) {
+    void ensure(std::size_t count, const char *what) {
+        count = std::max<std::size_t>(count, 1);
+        if (count <= cap) return;
         cudaFree(p);
         p = nullptr;
-        check_cuda(cudaMalloc(&p, std::max<std::size_t>(count, 1) * sizeof(T)), what);
+        cap = 0;
+        check_cuda(cudaMalloc(&p, count * sizeof(T)), what);
+        cap = count;
     }
     void upload(const std::vector<T> &v, cudaStream_t s, unsigned long long &bytes, const char *what) {
-        alloc(v.size(), what);
+        ensure(v.size(), what);
         if (!v.empty())
             check_cuda(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s),
                        what);
@@ -1036,22 +1046,32 @@ FastPlan wide_plan(const std::vector<std::string> &coefficients, long long bound
 
 }  // namespace
 
-std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &curves, int device,
-                                           BatchStats *stats_out, bool use_graph) {
-    const auto started = Clock::now();
-    BatchStats stats;
-    std::vector<BatchCurveResult> results(curves.size());
-    if (device >= 0) check_cuda(cudaSetDevice(device), "cudaSetDevice");
-    int dev_id = 0;
-    check_cuda(cudaGetDevice(&dev_id), "cudaGetDevice");
+namespace {
 
-    // ---- validation and per-curve plans, one curve per task ----
-    const auto t_plan = Clock::now();
-    std::vector<CurveWork> work(curves.size());
+// Everything one batched run launches: per-curve descriptors, table specs
+// and work items, built on the host from the curves' plans.
+struct BatchPlan {
+    std::vector<CurveWork> work;
+    std::vector<dev::WideCurve> wide;
+    std::vector<dev::NarrowCurve> narrow;
+    std::vector<dev::AffineSpec> aspecs;
+    std::vector<unsigned short> residues;
+    std::vector<dev::PatternSpec> pspecs;
+    std::vector<dev::CompositeSpec> cspecs;
+    std::vector<dev::BatchItem> wide_items, narrow_items;
+    long long aff_words = 0, pattern_words = 0, row_words = 0;
+    int wide_smem_words = 0;
+};
+
+// Validation and per-curve plans (one curve per task), then descriptors,
+// table specs and work items in the order the kernels take them.
+void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurveResult> &results,
+                BatchPlan &P, BatchStats &stats) {
+    P.work.resize(curves.size());
     parallel_for(curves.size(), [&](std::size_t i) {
         const BatchCurveSpec &c = curves[i];
         BatchCurveResult &r = results[i];
-        CurveWork &cw = work[i];
+        CurveWork &cw = P.work[i];
         try {
             if (c.coefficients.size() < 2) throw std::invalid_argument("polynomial must have degree >= 1");
             if (c.bound < 1) throw std::invalid_argument("numerator bound must be positive");
@@ -1081,41 +1101,32 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
         }
     });
 
-    // ---- descriptors, table specs, work items ----
-    std::vector<dev::WideCurve> wide;
-    std::vector<dev::NarrowCurve> narrow;
-    std::vector<dev::AffineSpec> aspecs;
-    std::vector<unsigned short> residues;
-    std::vector<dev::PatternSpec> pspecs;
-    std::vector<dev::CompositeSpec> cspecs;
-    std::vector<dev::BatchItem> wide_items, narrow_items;
-    long long aff_words = 0, pattern_words = 0, row_words = 0;
-    int wide_smem_words = 0;
     const auto &cands = candidate_primes();
     auto add_affine = [&](int p, const std::vector<std::string> &coeffs) {
         dev::AffineSpec A{};
-        A.out = aff_words;
-        A.residues = (long long)residues.size();
+        A.out = P.aff_words;
+        A.residues = (long long)P.residues.size();
         A.p = p;
         A.n = int(coeffs.size()) - 1;
-        for (const auto &c : coeffs) residues.push_back((unsigned short)decimal_mod(c, p));
-        aspecs.push_back(A);
-        aff_words += dev::kRefWords;
+        for (const auto &c : coeffs) P.residues.push_back((unsigned short)decimal_mod(c, p));
+        P.aspecs.push_back(A);
+        P.aff_words += dev::kRefWords;
         return A.out;
     };
     // largest work first, so that the persistent kernels end on small items
     std::vector<std::size_t> order;
     for (std::size_t i = 0; i < curves.size(); ++i)
-        if (work[i].ok && work[i].count > 0) order.push_back(i);
+        if (P.work[i].ok && P.work[i].count > 0) order.push_back(i);
     std::stable_sort(order.begin(), order.end(), [&](std::size_t a, std::size_t b) {
-        return (long double)work[a].words * work[a].count > (long double)work[b].words * work[b].count;
+        return (long double)P.work[a].words * P.work[a].count >
+               (long double)P.work[b].words * P.work[b].count;
     });
     for (std::size_t i : order) {
         const BatchCurveSpec &c = curves[i];
-        CurveWork &cw = work[i];
+        CurveWork &cw = P.work[i];
         const FastPlan &plan = cw.plan;
         const long long H = c.bound;
-        const long long aff_base = aff_words;
+        const long long aff_base = P.aff_words;
         for (int ci = 0; ci < kCandidatePrimes; ++ci) add_affine(cands[ci], c.coefficients);
         // per-prime patterns of this curve's stage-1 factors
         const long long M = cw.wide ? 64LL * plan.class_prime : 1;
@@ -1124,20 +1135,20 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
         for (const auto &slot : plan.slots)
             for (int q : slot) {
                 if (pattern_of[q] >= 0) continue;
-                dev::PatternSpec P{};
-                P.offset = pattern_words;
-                P.aff = add_affine(q, c.coefficients);
-                P.q = q;
-                P.lead_ok = lead_is_square(c.coefficients, q) ? 1 : 0;
-                P.s = int(S % q);
-                P.t = int(M % q);
-                pspecs.push_back(P);
-                pattern_of[q] = pattern_words;
-                pattern_words += (long long)q * q;
+                dev::PatternSpec Q{};
+                Q.offset = P.pattern_words;
+                Q.aff = add_affine(q, c.coefficients);
+                Q.q = q;
+                Q.lead_ok = lead_is_square(c.coefficients, q) ? 1 : 0;
+                Q.s = int(S % q);
+                Q.t = int(M % q);
+                P.pspecs.push_back(Q);
+                pattern_of[q] = P.pattern_words;
+                P.pattern_words += (long long)q * q;
             }
         auto add_composite = [&](int sl, int length) {
             dev::CompositeSpec T{};
-            T.offset = row_words;
+            T.offset = P.row_words;
             if (sl < int(plan.moduli.size())) {
                 T.m = plan.moduli[sl];
                 T.nf = int(plan.slots[sl].size());
@@ -1150,8 +1161,8 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
                 T.nf = 0;
             }
             T.length = length < 0 ? T.m : length;
-            cspecs.push_back(T);
-            row_words += (long long)T.m * T.length;
+            P.cspecs.push_back(T);
+            P.row_words += (long long)T.m * T.length;
             return T;
         };
         stats.rectangle_sites += (long double)(2 * H + 1) * (long double)cw.count;
@@ -1189,7 +1200,7 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
                 Md.step = dev::u32((dev::kWarpSize * dev::kWK) % m);
             }
             C.smem_words = smem;
-            wide_smem_words = std::max(wide_smem_words, smem);
+            P.wide_smem_words = std::max(P.wide_smem_words, smem);
             two_adic_classes(c.coefficients, C.admissible);
             if (q > 1) {
                 const auto aff = affine_mask(q, c.coefficients);
@@ -1216,9 +1227,9 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
             const long long chunk = std::max(1LL, std::min<long long>(1 << 16, (1LL << 20) / cw.words));
             for (int range = 0; range < std::max(1, C.nint); ++range)
                 for (long long f = c.first; f <= c.last; f += chunk)
-                    wide_items.push_back({f, int(wide.size()), int(std::min(chunk, c.last - f + 1)),
-                                          range, 0});
-            wide.push_back(C);
+                    P.wide_items.push_back({f, int(P.wide.size()), int(std::min(chunk, c.last - f + 1)),
+                                            range, 0});
+            P.wide.push_back(C);
             stats.wide_curves += 1;
         } else {
             dev::NarrowCurve C{};
@@ -1227,8 +1238,8 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
             C.square = c.square ? 1 : 0;
             C.index = int(i);
             C.aff = aff_base;
-            if (row_words % 2) row_words += 1;  // 16-byte aligned bulk copy
-            C.tables = row_words;
+            if (P.row_words % 2) P.row_words += 1;  // 16-byte aligned bulk copy
+            C.tables = P.row_words;
             int used = 0;
             for (int sl = 0; sl < dev::kNarrowSlots; ++sl) {
                 const dev::CompositeSpec T = add_composite(sl, -1);
@@ -1242,7 +1253,7 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
                 C.step[sl] = dev::u32(32 % m);
             }
             if (used % 2) {
-                row_words += 1;
+                P.row_words += 1;
                 used += 1;
             }
             if (used > dev::kNarrowTableWords) throw std::logic_error("narrow tables exceed shared memory");
@@ -1267,18 +1278,61 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
                 std::max<long long>(dev::kNWarps, std::min<long long>(1 << 14, (1LL << 16) / cw.words));
             for (int range = 0; range < std::max(1, C.nint); ++range)
                 for (long long f = c.first; f <= c.last; f += chunk)
-                    narrow_items.push_back({f, int(narrow.size()),
-                                            int(std::min(chunk, c.last - f + 1)), range, 0});
-            narrow.push_back(C);
+                    P.narrow_items.push_back({f, int(P.narrow.size()),
+                                              int(std::min(chunk, c.last - f + 1)), range, 0});
+            P.narrow.push_back(C);
         }
         stats.curves += 1;
     }
-    stats.wide_items = wide_items.size();
-    stats.narrow_items = narrow_items.size();
-    stats.table_words = (unsigned long long)row_words;
-    stats.plan_ms = ms_since(t_plan);
+    stats.wide_items = P.wide_items.size();
+    stats.narrow_items = P.narrow_items.size();
+    stats.table_words = (unsigned long long)P.row_words;
+}
 
-    if (!wide.empty() || !narrow.empty()) {
+}  // namespace
+
+struct BatchEngine::Impl {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr, side = nullptr;
+    cudaEvent_t ev[6] = {};    // tables, wide kernel, narrow kernel (start, end)
+    cudaEvent_t fork = nullptr, join = nullptr;
+    unsigned long long *h_counters = nullptr;
+    unsigned long long capacity = 1ull << 20;
+    dev::Candidates cand{};
+    DeviceArray<dev::WideCurve> d_wide;
+    DeviceArray<dev::NarrowCurve> d_narrow;
+    DeviceArray<dev::BatchItem> d_witems, d_nitems;
+    DeviceArray<dev::AffineSpec> d_aspecs;
+    DeviceArray<dev::PatternSpec> d_pspecs;
+    DeviceArray<dev::CompositeSpec> d_cspecs;
+    DeviceArray<unsigned short> d_res, d_inv;
+    DeviceArray<dev::u64> d_sq, d_aff, d_patterns, d_rows;
+    DeviceArray<unsigned long long> d_counters;  // [0] survivors [1] wide work [2] narrow work [3] error
+    DeviceArray<long long> d_a;
+    DeviceArray<int> d_d, d_c;
+
+    explicit Impl(int dev_ordinal) {
+        if (dev_ordinal >= 0) check_cuda(cudaSetDevice(dev_ordinal), "cudaSetDevice");
+        check_cuda(cudaGetDevice(&device), "cudaGetDevice");
+        check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device),
+                   "cudaDeviceGetAttribute");
+        check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (auto &e : ev) check_cuda(cudaEventCreate(&e), "cudaEventCreate");
+        check_cuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
+        check_cuda(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "cudaEventCreate");
+        check_cuda(cudaMallocHost(&h_counters, 8 * sizeof(unsigned long long)), "cudaMallocHost");
+        // RPG_BATCH_CAPACITY overrides the first survivor capacity (tests use a
+        // small one to exercise the rerun after an overflow)
+        if (const char *env = std::getenv("RPG_BATCH_CAPACITY"))
+            capacity = (unsigned long long)std::max(1LL, std::atoll(env));
+        const auto &cands = candidate_primes();
+        for (int ci = 0; ci < kCandidatePrimes; ++ci) {
+            cand.p[ci] = cands[ci];
+            cand.magic[ci] = dev::magic40(dev::u32(cands[ci]));
+        }
+        // curve-independent tables: inverses and squares modulo every prime below 512
         std::vector<unsigned short> inv_table(std::size_t(kMaximumPrime) * kMaximumPrime, 0);
         std::vector<dev::u64> square_masks(std::size_t(kMaximumPrime) * dev::kRefWords, 0);
         for (int p = 2; p < kMaximumPrime; ++p) {
@@ -1286,84 +1340,73 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
             for (int r = 1; r < p; ++r)
                 inv_table[std::size_t(p) * kMaximumPrime + r] = (unsigned short)mod_inverse(r, p);
             for (long long v = 0; v < p; ++v) {
-                const int s = int(v * v % p);
-                square_masks[std::size_t(p) * dev::kRefWords + s / 64] |= dev::u64(1) << (s % 64);
+                const int sq = int(v * v % p);
+                square_masks[std::size_t(p) * dev::kRefWords + sq / 64] |= dev::u64(1) << (sq % 64);
             }
         }
-        cudaStream_t stream, side;
-        check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        check_cuda(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking), "cudaStreamCreate");
-        cudaEvent_t ev[6];
-        for (auto &e : ev) check_cuda(cudaEventCreate(&e), "cudaEventCreate");
-        cudaEvent_t fork, join;
-        check_cuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
-        check_cuda(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "cudaEventCreate");
-        unsigned long long *h_counters = nullptr;
-        check_cuda(cudaMallocHost(&h_counters, 8 * sizeof(unsigned long long)), "cudaMallocHost");
-        struct Guard {
-            cudaStream_t a, b;
-            cudaEvent_t *ev;
-            cudaEvent_t f, j;
-            unsigned long long *host;
-            ~Guard() {
-                cudaStreamSynchronize(a);
-                cudaStreamSynchronize(b);
-                for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
-                cudaEventDestroy(f);
-                cudaEventDestroy(j);
-                cudaFreeHost(host);
-                cudaStreamDestroy(a);
-                cudaStreamDestroy(b);
-            }
-        } guard{stream, side, ev, fork, join, h_counters};
+        unsigned long long bytes = 0;
+        d_inv.upload(inv_table, stream, bytes, "upload inverses");
+        d_sq.upload(square_masks, stream, bytes, "upload squares");
+        d_counters.ensure(4, "cudaMalloc(batch counters)");
+        ensure_output(capacity);
+        check_cuda(cudaStreamSynchronize(stream), "batch engine setup");
+    }
 
-        DeviceArray<dev::WideCurve> d_wide;
-        DeviceArray<dev::NarrowCurve> d_narrow;
-        DeviceArray<dev::BatchItem> d_witems, d_nitems;
-        DeviceArray<dev::AffineSpec> d_aspecs;
-        DeviceArray<dev::PatternSpec> d_pspecs;
-        DeviceArray<dev::CompositeSpec> d_cspecs;
-        DeviceArray<unsigned short> d_res, d_inv;
-        DeviceArray<dev::u64> d_sq, d_aff, d_patterns, d_rows;
-        DeviceArray<unsigned long long> d_counters;  // [0] survivors [1] wide work [2] narrow work [3] error
-        d_wide.upload(wide, stream, stats.h2d_bytes, "upload wide curves");
-        d_narrow.upload(narrow, stream, stats.h2d_bytes, "upload narrow curves");
-        d_witems.upload(wide_items, stream, stats.h2d_bytes, "upload work items");
-        d_nitems.upload(narrow_items, stream, stats.h2d_bytes, "upload work items");
-        d_aspecs.upload(aspecs, stream, stats.h2d_bytes, "upload bitmask specs");
-        d_pspecs.upload(pspecs, stream, stats.h2d_bytes, "upload pattern specs");
-        d_cspecs.upload(cspecs, stream, stats.h2d_bytes, "upload table specs");
-        d_res.upload(residues, stream, stats.h2d_bytes, "upload residues");
-        d_inv.upload(inv_table, stream, stats.h2d_bytes, "upload inverses");
-        d_sq.upload(square_masks, stream, stats.h2d_bytes, "upload squares");
-        d_aff.alloc(std::size_t(aff_words), "cudaMalloc(batch bitmasks)");
-        d_patterns.alloc(std::size_t(pattern_words), "cudaMalloc(batch patterns)");
-        d_rows.alloc(std::size_t(row_words), "cudaMalloc(batch tables)");
-        d_counters.alloc(4, "cudaMalloc(batch counters)");
-        // RPG_BATCH_CAPACITY overrides the first survivor capacity (tests use a
-        // small one to exercise the rerun after an overflow)
-        unsigned long long capacity = 1ull << 20;
-        if (const char *env = std::getenv("RPG_BATCH_CAPACITY"))
-            capacity = std::max(1LL, std::atoll(env));
-        DeviceArray<long long> d_a;
-        DeviceArray<int> d_d, d_c;
-        auto alloc_out = [&](unsigned long long cap) {
-            d_a.alloc(cap, "cudaMalloc(batch survivors)");
-            d_d.alloc(cap, "cudaMalloc(batch survivors)");
-            d_c.alloc(cap, "cudaMalloc(batch survivors)");
-        };
-        alloc_out(capacity);
+    ~Impl() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (side) cudaStreamSynchronize(side);
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (h_counters) cudaFreeHost(h_counters);
+        if (stream) cudaStreamDestroy(stream);
+        if (side) cudaStreamDestroy(side);
+    }
 
-        int sms = 0;
-        check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id),
-                   "cudaDeviceGetAttribute");
+    void ensure_output(unsigned long long cap) {
+        d_a.ensure(cap, "cudaMalloc(batch survivors)");
+        d_d.ensure(cap, "cudaMalloc(batch survivors)");
+        d_c.ensure(cap, "cudaMalloc(batch survivors)");
+    }
+
+    std::vector<BatchCurveResult> run(const std::vector<BatchCurveSpec> &curves, BatchStats *stats_out,
+                                      bool use_graph);
+};
+
+std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurveSpec> &curves,
+                                                     BatchStats *stats_out, bool use_graph) {
+    const auto started = Clock::now();
+    BatchStats stats;
+    std::vector<BatchCurveResult> results(curves.size());
+    check_cuda(cudaSetDevice(device), "cudaSetDevice");
+    BatchPlan P;
+    const auto t_plan = Clock::now();
+    build_plan(curves, results, P, stats);
+    stats.plan_ms = ms_since(t_plan);
+    const std::vector<CurveWork> &work = P.work;
+
+    if (!P.wide.empty() || !P.narrow.empty()) {
+        d_wide.upload(P.wide, stream, stats.h2d_bytes, "upload wide curves");
+        d_narrow.upload(P.narrow, stream, stats.h2d_bytes, "upload narrow curves");
+        d_witems.upload(P.wide_items, stream, stats.h2d_bytes, "upload work items");
+        d_nitems.upload(P.narrow_items, stream, stats.h2d_bytes, "upload work items");
+        d_aspecs.upload(P.aspecs, stream, stats.h2d_bytes, "upload bitmask specs");
+        d_pspecs.upload(P.pspecs, stream, stats.h2d_bytes, "upload pattern specs");
+        d_cspecs.upload(P.cspecs, stream, stats.h2d_bytes, "upload table specs");
+        d_res.upload(P.residues, stream, stats.h2d_bytes, "upload residues");
+        d_aff.ensure(std::size_t(P.aff_words), "cudaMalloc(batch bitmasks)");
+        d_patterns.ensure(std::size_t(P.pattern_words), "cudaMalloc(batch patterns)");
+        d_rows.ensure(std::size_t(P.row_words), "cudaMalloc(batch tables)");
+
+        const int wide_smem_words = P.wide_smem_words;
         const std::size_t wide_smem = 2 * std::size_t(wide_smem_words) * 8 +
                                       std::size_t(dev::kWWarps) * dev::kQueue * 12 +
                                       std::size_t(dev::kMaxClasses) * dev::kWideSlots * 4;
         const std::size_t narrow_smem = std::size_t(dev::kNarrowTableWords + dev::kAffWords) * 8 +
                                         std::size_t(dev::kNWarps) * dev::kQueue * 12;
         int wide_grid = 0, narrow_grid = 0;
-        if (!wide.empty()) {
+        if (!P.wide.empty()) {
             int per_sm = 0;
             check_cuda(cudaFuncSetAttribute(dev::wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             int(wide_smem)),
@@ -1371,9 +1414,9 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
             check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::wide_kernel,
                                                                      dev::kWThreads, wide_smem),
                        "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-            wide_grid = std::max(1, std::min<int>(sms * std::max(1, per_sm), int(wide_items.size())));
+            wide_grid = std::max(1, std::min<int>(sms * std::max(1, per_sm), int(P.wide_items.size())));
         }
-        if (!narrow.empty()) {
+        if (!P.narrow.empty()) {
             int per_sm = 0;
             check_cuda(cudaFuncSetAttribute(dev::narrow_kernel,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(narrow_smem)),
@@ -1381,15 +1424,9 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
             check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::narrow_kernel,
                                                                      dev::kNThreads, narrow_smem),
                        "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-            narrow_grid = std::max(1, std::min<int>(sms * std::max(1, per_sm), int(narrow_items.size())));
-        }
-        dev::Candidates cand{};
-        for (int ci = 0; ci < kCandidatePrimes; ++ci) {
-            cand.p[ci] = cands[ci];
-            cand.magic[ci] = dev::magic40(dev::u32(cands[ci]));
+            narrow_grid = std::max(1, std::min<int>(sms * std::max(1, per_sm), int(P.narrow_items.size())));
         }
 
-        // ev[0]/ev[1] tables, ev[2]/ev[3] wide kernel, ev[4]/ev[5] narrow kernel;
         // external records become event nodes when the stream is captured
         bool capturing = false;
         auto record = [&](cudaEvent_t e, cudaStream_t s) {
@@ -1406,7 +1443,7 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
             record(ev[2], stream);
             if (wide_grid) {
                 dev::wide_kernel<<<wide_grid, dev::kWThreads, wide_smem, stream>>>(
-                    d_wide.p, d_witems.p, int(wide_items.size()), d_rows.p, d_aff.p, d_inv.p, cand,
+                    d_wide.p, d_witems.p, int(P.wide_items.size()), d_rows.p, d_aff.p, d_inv.p, cand,
                     out, wide_smem_words, d_counters.p + 1);
                 check_cuda(cudaGetLastError(), "wide_kernel launch");
             }
@@ -1414,7 +1451,7 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
             record(ev[4], side);
             if (narrow_grid) {
                 dev::narrow_kernel<<<narrow_grid, dev::kNThreads, narrow_smem, side>>>(
-                    d_narrow.p, d_nitems.p, int(narrow_items.size()), d_rows.p, d_aff.p, d_inv.p,
+                    d_narrow.p, d_nitems.p, int(P.narrow_items.size()), d_rows.p, d_aff.p, d_inv.p,
                     cand, out, d_counters.p + 2);
                 check_cuda(cudaGetLastError(), "narrow_kernel launch");
             }
@@ -1427,20 +1464,20 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
         };
         auto enqueue_all = [&]() {
             record(ev[0], stream);
-            const long long aff_threads = (long long)aspecs.size() * dev::kRefWords;
+            const long long aff_threads = (long long)P.aspecs.size() * dev::kRefWords;
             if (aff_threads) {
                 dev::affine_kernel<<<unsigned((aff_threads + 255) / 256), 256, 0, stream>>>(
-                    d_aspecs.p, (long long)aspecs.size(), d_res.p, d_sq.p, d_aff.p);
+                    d_aspecs.p, (long long)P.aspecs.size(), d_res.p, d_sq.p, d_aff.p);
                 check_cuda(cudaGetLastError(), "affine_kernel launch");
             }
-            if (pattern_words) {
-                dev::pattern_kernel<<<unsigned((pattern_words + 255) / 256), 256, 0, stream>>>(
-                    d_pspecs.p, int(pspecs.size()), d_aff.p, d_inv.p, d_patterns.p, pattern_words);
+            if (P.pattern_words) {
+                dev::pattern_kernel<<<unsigned((P.pattern_words + 255) / 256), 256, 0, stream>>>(
+                    d_pspecs.p, int(P.pspecs.size()), d_aff.p, d_inv.p, d_patterns.p, P.pattern_words);
                 check_cuda(cudaGetLastError(), "pattern_kernel launch");
             }
-            if (row_words) {
-                dev::composite_kernel<<<unsigned((row_words + 255) / 256), 256, 0, stream>>>(
-                    d_cspecs.p, int(cspecs.size()), d_patterns.p, d_rows.p, row_words);
+            if (P.row_words) {
+                dev::composite_kernel<<<unsigned((P.row_words + 255) / 256), 256, 0, stream>>>(
+                    d_cspecs.p, int(P.cspecs.size()), d_patterns.p, d_rows.p, P.row_words);
                 check_cuda(cudaGetLastError(), "composite_kernel launch");
             }
             record(ev[1], stream);
@@ -1455,6 +1492,7 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
             try {
                 enqueue_all();
             } catch (...) {
+                capturing = false;
                 cudaStreamEndCapture(stream, &graph);
                 if (graph) cudaGraphDestroy(graph);
                 throw;
@@ -1474,7 +1512,7 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
             enqueue_all();
             check_cuda(cudaStreamSynchronize(stream), "batch sieve");
         }
-        stats.launches += (aspecs.empty() ? 0 : 1) + (pattern_words ? 1 : 0) + (row_words ? 1 : 0) +
+        stats.launches += (P.aspecs.empty() ? 0 : 1) + (P.pattern_words ? 1 : 0) + (P.row_words ? 1 : 0) +
                           (wide_grid ? 1 : 0) + (narrow_grid ? 1 : 0);
         auto elapsed = [&](int a, int b) {
             float ms = 0;
@@ -1488,7 +1526,7 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
         if (h_counters[3]) throw DeviceTimeout("batched sieve: a bounded wait for a table copy timed out");
         while (h_counters[0] > capacity) {  // survivors did not fit: run again with room for all
             capacity = h_counters[0] + (h_counters[0] >> 3) + 1024;
-            alloc_out(capacity);
+            ensure_output(capacity);
             enqueue_sieve();
             check_cuda(cudaStreamSynchronize(stream), "batch sieve");
             stats.sieve_ms += std::max(elapsed(2, 3), elapsed(2, 5));
@@ -1500,12 +1538,14 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
         std::vector<long long> ha(n);
         std::vector<int> hd(n), hc(n);
         if (n) {
-            check_cuda(cudaMemcpy(ha.data(), d_a.p, n * sizeof(long long), cudaMemcpyDeviceToHost),
+            check_cuda(cudaMemcpyAsync(ha.data(), d_a.p, n * sizeof(long long), cudaMemcpyDeviceToHost,
+                                       stream),
                        "download batch survivors");
-            check_cuda(cudaMemcpy(hd.data(), d_d.p, n * sizeof(int), cudaMemcpyDeviceToHost),
+            check_cuda(cudaMemcpyAsync(hd.data(), d_d.p, n * sizeof(int), cudaMemcpyDeviceToHost, stream),
                        "download batch survivors");
-            check_cuda(cudaMemcpy(hc.data(), d_c.p, n * sizeof(int), cudaMemcpyDeviceToHost),
+            check_cuda(cudaMemcpyAsync(hc.data(), d_c.p, n * sizeof(int), cudaMemcpyDeviceToHost, stream),
                        "download batch survivors");
+            check_cuda(cudaStreamSynchronize(stream), "download batch survivors");
         }
         stats.d2h_bytes += n * (sizeof(long long) + 2 * sizeof(int)) + 4 * sizeof(unsigned long long);
 
@@ -1546,6 +1586,38 @@ std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &cu
     stats.wall_ms = ms_since(started);
     if (stats_out) *stats_out = stats;
     return results;
+}
+
+BatchEngine::BatchEngine(int device) : impl_(new Impl(device)) {}
+BatchEngine::~BatchEngine() = default;
+
+std::vector<BatchCurveResult> BatchEngine::run(const std::vector<BatchCurveSpec> &curves,
+                                               BatchStats *stats, bool use_graph) {
+    return impl_->run(curves, stats, use_graph);
+}
+
+int BatchEngine::device() const { return impl_->device; }
+
+unsigned long long BatchEngine::estimate_bytes(const BatchCurveSpec &c) {
+    const long long words = word_count64(std::max(1LL, c.bound));
+    const long long count = c.last >= c.first ? c.last - c.first + 1 : 0;
+    long long table;
+    if (words >= kBatchWideWords) {
+        const double cap = std::min<double>(kMaxModulus, std::max(64.0, std::sqrt(double(words) * count / 48.0)));
+        table = (long long)(6.0 * cap * (cap + dev::kWExt));
+    } else {
+        table = dev::kNarrowTableWords;
+    }
+    // tables, bitmasks, patterns, descriptor and items (8-byte words)
+    return (unsigned long long)(table + 2 * dev::kAffWords + 6 * 127 * 127 + 1024 +
+                                std::max(1LL, count * std::max(1LL, (long long)c.intervals.size()) /
+                                                  64)) * 8ull;
+}
+
+std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &curves, int device,
+                                           BatchStats *stats, bool use_graph) {
+    BatchEngine engine(device);
+    return engine.run(curves, stats, use_graph);
 }
 
 }  // namespace rpg

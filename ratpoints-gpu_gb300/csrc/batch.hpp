@@ -20,6 +20,7 @@
 // survivor exactly.
 #pragma once
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -60,9 +61,34 @@ struct BatchStats {
     bool graph = false;
 };
 
-// Runs every valid curve in one batched pass on `device` (-1: current).
-// Curves that fail validation get a nonzero status and no points; the others
-// are searched together.
+// Device resources of batched runs kept across runs: streams, events, the
+// curve-independent tables and grow-only device buffers (tables, bitmasks,
+// descriptors, work items, survivors), so that a run allocates nothing once
+// the buffers are large enough.  One engine serves one thread at a time.
+class BatchEngine {
+public:
+    explicit BatchEngine(int device);  // -1: the calling thread's current device
+    ~BatchEngine();
+    BatchEngine(const BatchEngine &) = delete;
+    BatchEngine &operator=(const BatchEngine &) = delete;
+
+    // Runs every valid curve in one batched pass.  Curves that fail
+    // validation get a nonzero status and no points; the others are searched
+    // together.  The table build and sieve launches are captured in one CUDA
+    // graph when use_graph is set.
+    std::vector<BatchCurveResult> run(const std::vector<BatchCurveSpec> &curves, BatchStats *stats,
+                                      bool use_graph = true);
+    int device() const;
+
+    // Upper estimate of the device bytes a curve adds to a run (admission).
+    static unsigned long long estimate_bytes(const BatchCurveSpec &curve);
+
+private:
+    struct Impl;
+    std::unique_ptr<Impl> impl_;
+};
+
+// One batched pass on a fresh engine on `device` (-1: current).
 std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &curves, int device,
                                            BatchStats *stats, bool use_graph = true);
 

@@ -13,6 +13,7 @@
 #include "exact.hpp"
 #include "plan.hpp"
 #include "search.hpp"
+#include "serve.hpp"
 #include "session.hpp"
 #include "sieve.hpp"
 
@@ -396,6 +397,75 @@ rpg_status rpg_batch_search(const rpg_search_options *curves, int32_t curve_coun
         return RPG_OK;
     });
 }
+
+struct rpg_server {
+    std::unique_ptr<rpg::SearchServer> server;
+};
+
+rpg_status rpg_server_create(const rpg_server_options *options, rpg_server **server) {
+    return guarded([&]() -> rpg_status {
+        if (!options || !server) return fail(RPG_E_ARG, "options and server must not be NULL");
+        rpg::ServeOptions o;
+        o.device = options->device;
+        o.lanes = options->lanes;
+        o.memory_budget = options->memory_budget_bytes;
+        o.max_batch_curves = options->max_batch_curves;
+        if (o.memory_budget == 0) return fail(RPG_E_ARG, "memory budget must be positive");
+        auto s = std::make_unique<rpg_server>();
+        s->server = std::make_unique<rpg::SearchServer>(o);
+        *server = s.release();
+        return RPG_OK;
+    });
+}
+
+rpg_status rpg_server_submit(rpg_server *server, const rpg_search_options *request,
+                             int32_t first_point_only, uint64_t *request_id) {
+    return guarded([&]() -> rpg_status {
+        if (!server || !request || !request_id)
+            return fail(RPG_E_ARG, "server, request and request_id must not be NULL");
+        rpg::SearchOptions s;
+        std::string error;
+        if (!options_from(*request, s, error)) return fail(RPG_E_ARG, error);
+        rpg::BatchCurveSpec b;
+        b.coefficients = s.coefficients;
+        b.bound = s.numerator_bound;
+        b.first = s.first;
+        b.last = s.last;
+        b.square = s.square;
+        b.include_infinity = s.include_infinity;
+        b.intervals = s.intervals;
+        *request_id = server->server->submit(b, first_point_only != 0);
+        return RPG_OK;
+    });
+}
+
+rpg_status rpg_server_wait(rpg_server *server, uint64_t request_id, double timeout_ms,
+                           rpg_point_cb callback, void *user, int32_t *done,
+                           rpg_request_stats *stats) {
+    return guarded([&]() -> rpg_status {
+        if (!server || !done) return fail(RPG_E_ARG, "server and done must not be NULL");
+        *done = 0;
+        rpg::ServeResult r;
+        if (!server->server->wait(request_id, timeout_ms, r)) return RPG_OK;
+        *done = 1;
+        if (stats) {
+            std::memset(stats, 0, sizeof *stats);
+            stats->latency_ms = r.latency_ms;
+            stats->queue_ms = r.queue_ms;
+            stats->rectangle_sites = double(r.rectangle_sites);
+            stats->survivors = r.survivors;
+            stats->points = r.points.size();
+            stats->waves = r.waves;
+        }
+        if (r.status != 0) return fail(rpg_status(r.status), r.error);
+        if (callback)
+            for (const auto &p : r.points)
+                if (callback(p.numerator, p.ordinate.c_str(), p.denominator, user) == 0) break;
+        return RPG_OK;
+    });
+}
+
+void rpg_server_destroy(rpg_server *server) { delete server; }
 
 int32_t rpg_device_count(void) {
     int n = 0;

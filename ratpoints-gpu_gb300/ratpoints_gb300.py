@@ -88,6 +88,20 @@ class BatchStats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("lanes", ctypes.c_int32),
+                ("memory_budget_bytes", ctypes.c_uint64), ("max_batch_curves", ctypes.c_int32)]
+
+
+class RequestStats(ctypes.Structure):
+    _fields_ = [("latency_ms", ctypes.c_double), ("queue_ms", ctypes.c_double),
+                ("rectangle_sites", ctypes.c_double), ("survivors", ctypes.c_uint64),
+                ("points", ctypes.c_uint64), ("waves", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 CANDIDATE_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
                                 ctypes.POINTER(ctypes.c_int32), ctypes.c_size_t, ctypes.c_void_p)
 POINT_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int64, ctypes.c_char_p, ctypes.c_int64,
@@ -121,6 +135,17 @@ def load():
                                      ctypes.c_uint32, BATCH_POINT_CB, ctypes.c_void_p,
                                      ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_uint64),
                                      ctypes.POINTER(BatchStats)]
+    lib.rpg_server_create.restype = S
+    lib.rpg_server_create.argtypes = [ctypes.POINTER(ServerOptions), ctypes.POINTER(ctypes.c_void_p)]
+    lib.rpg_server_submit.restype = S
+    lib.rpg_server_submit.argtypes = [ctypes.c_void_p, ctypes.POINTER(SearchOptions), ctypes.c_int32,
+                                      ctypes.POINTER(ctypes.c_uint64)]
+    lib.rpg_server_wait.restype = S
+    lib.rpg_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double, POINT_CB,
+                                    ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                    ctypes.POINTER(RequestStats)]
+    lib.rpg_server_destroy.restype = None
+    lib.rpg_server_destroy.argtypes = [ctypes.c_void_p]
     lib.rpg_is_squarefree.restype = S
     lib.rpg_is_squarefree.argtypes = [pp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
     lib.rpg_square_root.restype = S
@@ -275,6 +300,67 @@ def batch_search(curves, device=-1, graph=True, stop_after=None):
                                 status, survivors, ctypes.byref(stats)))
     del keep
     return points, list(status)[:n], list(survivors)[:n], stats.as_dict()
+
+
+class Server:
+    """Serving loop (rpg_server_*): submit searches at any time, wait for answers.
+
+    A request is a dict like batch_search's curves; wait() returns None on
+    timeout, else (status, points, stats) with status the request's rpg_status
+    (0, or e.g. 6 for a polynomial that is not squarefree).
+    """
+
+    def __init__(self, device=-1, lanes=2, memory_budget=8 << 30, max_batch_curves=1024):
+        self._lib = load()
+        opts = ServerOptions(device, lanes, memory_budget, max_batch_curves)
+        handle = ctypes.c_void_p()
+        _check(self._lib.rpg_server_create(ctypes.byref(opts), ctypes.byref(handle)))
+        self._handle = handle
+
+    def submit(self, curve, first_point_only=False):
+        opts = SearchOptions()
+        keep = _fill_options(opts, coefficients_of(curve["coefficients"]), curve["bound"],
+                             curve["first"], curve["last"], curve.get("intervals", ()),
+                             curve.get("include_infinity", True), square=curve.get("square", False))
+        rid = ctypes.c_uint64()
+        _check(self._lib.rpg_server_submit(self._handle, ctypes.byref(opts), int(first_point_only),
+                                           ctypes.byref(rid)))
+        del keep
+        return rid.value
+
+    def wait(self, request_id, timeout_ms=-1.0):
+        points = []
+
+        @POINT_CB
+        def on_point(a, y, d, _user):
+            points.append((a, int(y.decode()), d))
+            return 1
+
+        done = ctypes.c_int32(0)
+        stats = RequestStats()
+        status = self._lib.rpg_server_wait(self._handle, request_id, float(timeout_ms), on_point,
+                                           None, ctypes.byref(done), ctypes.byref(stats))
+        if not done.value:
+            _check(status)
+            return None
+        return status, points, stats.as_dict()
+
+    def close(self):
+        if self._handle:
+            self._lib.rpg_server_destroy(self._handle)
+            self._handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def is_squarefree(coefficients):

@@ -8,6 +8,16 @@ lists c0 .. cn; sizes and distributions follow the benchmark definitions:
                  coefficient a random sign times a random integer of bit length
                  uniform in [8, 64]; numerator bound A and denominator bound B
                  independent, each log-uniform in [10^3, 10^6]
+  wide_degree    degree uniform in 12..40, coefficients of bit length uniform
+                 in [100, 256] with a random sign, box A = B = 10^5, x in a
+                 union of 3 random closed intervals (lower bound uniform in
+                 [-4, 4], length uniform in [0.05, 1], four decimals)
+  square_cubics  x^3 + alpha x + beta with alpha, beta uniform in [-10^12, 10^12],
+                 square denominators k^2 for k in [1, 46340], |a| <= 10^9
+  serving_stream Poisson arrivals (200 per second): degree uniform in 2..12,
+                 coefficient bit length uniform in [16, 128] with a random sign,
+                 box a in [-H, H], b in [1, H] with H log-uniform in [10^2, 10^6],
+                 30 % asking for the first point only
 """
 
 from __future__ import annotations
@@ -43,17 +53,68 @@ def mixed_batch(count=4096, seed=3, degrees=(3, 4, 5, 6, 8, 10), bits=(8, 64),
     rng = random.Random(seed)
     curves = []
     while len(curves) < count:
-        degree = rng.choice(degrees)
-        coeffs = []
-        for i in range(degree + 1):
-            b = rng.randint(*bits)
-            value = rng.getrandbits(b) | (1 << (b - 1))  # bit length exactly b
-            coeffs.append(str(rng.choice((-1, 1)) * value))
+        coeffs = _random_coefficients(rng, rng.choice(degrees), bits)
         if not _squarefree(coeffs):
             continue
         curves.append({"coefficients": coeffs, "bound": _log_uniform(rng, *heights),
                        "first": 1, "last": _log_uniform(rng, *denominators)})
     return curves
+
+
+def _random_coefficients(rng, degree, bits):
+    coeffs = []
+    for _ in range(degree + 1):
+        b = rng.randint(*bits)
+        value = rng.getrandbits(b) | (1 << (b - 1))
+        coeffs.append(str(rng.choice((-1, 1)) * value))
+    return coeffs
+
+
+def wide_degree(count=256, seed=11, bound=10**5):
+    """[{coefficients, bound, first, last, intervals}] of high degree with big coefficients."""
+    rng = random.Random(seed)
+    curves = []
+    while len(curves) < count:
+        coeffs = _random_coefficients(rng, rng.randint(12, 40), (100, 256))
+        if not _squarefree(coeffs):
+            continue
+        intervals = []
+        for _ in range(3):
+            lo = rng.uniform(-4, 4)
+            intervals.append((f"{lo:.4f}", f"{lo + rng.uniform(0.05, 1):.4f}"))
+        curves.append({"coefficients": coeffs, "bound": bound, "first": 1, "last": bound,
+                       "intervals": intervals})
+    return curves
+
+
+def square_cubics(count=256, seed=13, bound=10**9, last=46340):
+    """[{coefficients, bound, first, last, square}]: x^3 + alpha x + beta, square denominators."""
+    rng = random.Random(seed)
+    curves = []
+    while len(curves) < count:
+        alpha, beta = rng.randint(-10**12, 10**12), rng.randint(-10**12, 10**12)
+        coeffs = [str(beta), str(alpha), "0", "1"]
+        if not _squarefree(coeffs):
+            continue
+        curves.append({"coefficients": coeffs, "bound": bound, "first": 1, "last": last,
+                       "square": True})
+    return curves
+
+
+def serving_stream(count=1000, rate=200.0, seed=5, first_fraction=0.3):
+    """[(arrival seconds, request dict, first_point_only)] of a Poisson stream."""
+    rng = random.Random(seed)
+    t = 0.0
+    stream = []
+    while len(stream) < count:
+        coeffs = _random_coefficients(rng, rng.randint(2, 12), (16, 128))
+        if not _squarefree(coeffs):
+            continue
+        t += rng.expovariate(rate)
+        h = _log_uniform(rng, 10**2, 10**6)
+        stream.append((t, {"coefficients": coeffs, "bound": h, "first": 1, "last": h},
+                       rng.random() < first_fraction))
+    return stream
 
 
 def mobius(limit):
