@@ -277,6 +277,119 @@ def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2):
     }
 
 
+def _loop(rpg, curves):
+    """The plain per-curve loop: one single-curve search per curve."""
+    t0 = time.perf_counter()
+    pts = [rpg.point_search(c["coefficients"], c["bound"], c["first"], c["last"],
+                            intervals=c.get("intervals", ()), square=c.get("square", False))[0]
+           for c in curves]
+    return time.perf_counter() - t0, pts
+
+
+def restricted_benchmark(rpg, high_degree=256, cubics=32, plain_cubics=8):
+    """High-degree curves with big coefficients restricted to x intervals, and
+    cubics with square denominators: batched pass against the plain loop.
+    Sites are those of the search boxes ((2A + 1) x denominators), whether or
+    not the sieve sweeps them (interval narrowing skips rows' other numerators)."""
+    import workloads
+
+    out = {}
+    curves = workloads.wide_degree(high_degree)
+    box = sum((2 * c["bound"] + 1) * c["last"] for c in curves)
+    rpg.batch_search(curves[:4])
+    t0 = time.perf_counter()
+    points, _, _, stats = rpg.batch_search(curves)
+    wall = time.perf_counter() - t0
+    plain_wall, plain = _loop(rpg, curves)
+    out["high_degree_intervals"] = {
+        "workload": f"{high_degree} curves, degree uniform in 12..40, coefficients of 100..256 bits, "
+                    "A = B = 1e5, x in 3 random closed intervals",
+        "box_sites": box, "batched": {"value": box / wall / 1e9, "unit": "rectangle Gsites/s",
+                                      "wall_s": wall, "sieve_ms": stats["sieve_ms"],
+                                      "points": stats["points"], "survivors": stats["survivors"]},
+        "plain_loop": {"value": box / plain_wall / 1e9, "unit": "rectangle Gsites/s",
+                       "wall_s": plain_wall, "note": "single-curve search of each curve: whole "
+                                                     "rows swept, interval test on the host"},
+        "speedup_vs_plain": plain_wall / wall,
+        "points_identical": plain == points}
+    if cubics > 0:
+        cs = workloads.square_cubics(cubics)
+        box = sum((2 * c["bound"] + 1) * c["last"] for c in cs)
+        t0 = time.perf_counter()
+        points, _, _, stats = rpg.batch_search(cs)
+        wall = time.perf_counter() - t0
+        n_plain = min(plain_cubics, cubics)
+        plain_wall, plain = _loop(rpg, cs[:n_plain])
+        plain_box = sum((2 * c["bound"] + 1) * c["last"] for c in cs[:n_plain])
+        out["square_cubics"] = {
+            "workload": f"{cubics} of the 256 cubics x^3 + alpha x + beta, alpha, beta uniform in "
+                        "[-1e12, 1e12], denominators k^2 for k in [1, 46340], |a| <= 1e9",
+            "box_sites": box,
+            "batched": {"value": box / wall / 1e9, "unit": "rectangle Gsites/s", "wall_s": wall,
+                        "sieve_ms": stats["sieve_ms"], "points": stats["points"],
+                        "survivors": stats["survivors"]},
+            "plain_loop": {"value": plain_box / plain_wall / 1e9, "unit": "rectangle Gsites/s",
+                           "wall_s": plain_wall, "curves": n_plain},
+            "points_identical": plain == points[:n_plain]}
+    return out
+
+
+def serving_benchmark(rpg, count=1000, rate=200.0, lanes=2, check=40):
+    """Poisson stream of requests into the serving loop: per-request latency
+    (submit -> answer) percentiles and aggregate throughput over the stream."""
+    import statistics
+    import workloads
+
+    stream = workloads.serving_stream(count, rate)
+    mu = workloads.mobius(max(r["last"] for _, r, _ in stream))
+    results = [None] * len(stream)
+    with rpg.Server(lanes=lanes) as server:
+        warm = server.submit(stream[0][1])
+        server.wait(warm)
+        ids = [None] * len(stream)
+        t0 = time.perf_counter()
+
+        def feed():
+            for i, (at, req, first) in enumerate(stream):
+                delay = at - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                ids[i] = server.submit(req, first)
+
+        feeder = threading.Thread(target=feed)
+        feeder.start()
+        feeder.join()
+        for i, rid in enumerate(ids):
+            results[i] = server.wait(rid)
+        wall = time.perf_counter() - t0
+    lat = sorted(r[2]["latency_ms"] for r in results)
+    pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))]
+    rect = sum(r[2]["rectangle_sites"] for r in results)
+    reduced = 0
+    for (_, req, _), r in zip(stream, results):
+        searched = int(round(r[2]["rectangle_sites"] / (2 * req["bound"] + 1)))
+        if searched:
+            reduced += workloads.reduced_sites(req["bound"], req["first"], req["first"] + searched - 1, mu)
+    rng = random.Random(1)
+    sample = rng.sample(range(len(stream)), min(check, len(stream)))
+    identical = all(
+        results[i][1] == rpg.point_search(stream[i][1]["coefficients"], stream[i][1]["bound"],
+                                          stream[i][1]["first"], stream[i][1]["last"],
+                                          stop_after=1 if stream[i][2] else None)[0]
+        for i in sample)
+    return {"workload": f"{count} requests, Poisson arrivals at {rate:g}/s: degree uniform in 2..12, "
+                        "coefficients of 16..128 bits, a in [-H, H], b in [1, H], H log-uniform in "
+                        "[1e2, 1e6], 30% first point only",
+            "lanes": lanes, "requests": count, "wall_s": wall,
+            "p50_ms": pct(0.50), "p99_ms": pct(0.99), "mean_ms": statistics.fmean(lat),
+            "max_ms": lat[-1], "value": reduced / wall / 1e9, "unit": UNIT,
+            "rectangle_gsites_per_s": rect / wall / 1e9,
+            "note": "throughput = reduced sites searched (first-point requests count the "
+                    "denominators their waves covered) / stream wall time; the offered load is "
+                    "the arrival rate, not the device's capacity",
+            "identical_to_single_search": {"checked": len(sample), "all": identical}}
+
+
 def workload_config():
     rect = (2 * HEIGHT + 1) * DENOMINATORS
     return {"workload": "degree-6 curve, coefficients uniform in [-2^32, 2^32), "
@@ -303,6 +416,12 @@ def main():
                         help="curves of the mixed batch (0: skip the batch measurement)")
     parser.add_argument("--batch-plain-curves", type=int, default=4096,
                         help="curves of the batch also run as a plain per-curve loop")
+    parser.add_argument("--restricted", type=int, default=256,
+                        help="high-degree interval-restricted curves (0: skip)")
+    parser.add_argument("--square-cubics", type=int, default=32,
+                        help="square-denominator cubics of the restricted searches (0: skip)")
+    parser.add_argument("--serving-requests", type=int, default=1000,
+                        help="requests of the serving stream (0: skip)")
     args = parser.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -417,6 +536,10 @@ def main():
                     "identical to the reference implementation's"}
     if args.batch_curves > 0:
         line["batch"] = batch_benchmark(rpg, args.batch_curves, args.batch_plain_curves)
+    if args.restricted > 0:
+        line["restricted"] = restricted_benchmark(rpg, args.restricted, args.square_cubics)
+    if args.serving_requests > 0:
+        line["serving"] = serving_benchmark(rpg, args.serving_requests)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(coeffs, seconds=args.cpu_seconds)
     print(json.dumps(line))

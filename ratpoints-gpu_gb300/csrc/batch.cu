@@ -29,6 +29,8 @@ constexpr int kWItemWords = kWarpSize * kWK * kWSteps;  // class words per sweep
 constexpr int kWExt = kWarpSize * (kWK - 1);            // row extension
 constexpr int kWMaxSmemWords = 3300;                    // staged row words per buffer (two
                                                         // buffers, 3 CTAs per SM)
+constexpr long long kWHugeWords = 1LL << 17;            // rows this long use one buffer of
+                                                        // twice the size (stronger moduli)
 constexpr int kQueue = 64;
 constexpr int kClassBits = 8;
 constexpr int kMaxClasses = kMaxFastClasses;
@@ -69,6 +71,7 @@ struct WideCurve {
     int h_mod_m;                   // H mod M
     int inv64_q;                   // 64^-1 mod q (CRT)
     int smem_words;
+    int nbuf;                      // row buffers: 2 (the next row copied during a sweep) or 1
     int square;
     int index;                     // position in the caller's curve list
     unsigned short neg_h[kCandidatePrimes];   // (-H) mod p
@@ -580,7 +583,7 @@ __global__ void __launch_bounds__(kWThreads, 3)
             // every warp is past the previous sweep: the other buffer is free
             int next = i + 1;
             while (next < item.count && !live(next)) ++next;
-            if (next < item.count) {
+            if (C.nbuf == 2 && next < item.count) {
                 if (threadIdx.x == 0) stage_rows(next, b ^ 1);
                 pending |= 1u << (b ^ 1);
             }
@@ -686,7 +689,12 @@ __global__ void __launch_bounds__(kWThreads, 3)
                 return;
             }
             i = next;
-            b ^= 1;
+            if (C.nbuf == 2) {
+                b ^= 1;
+            } else if (i < item.count) {  // one buffer: copy the next row now that it is free
+                if (threadIdx.x == 0) stage_rows(i, b);
+                pending |= 1u << b;
+            }
         }
         __syncthreads();
     }
@@ -1030,7 +1038,8 @@ struct CurveWork {
 
 // Wide plan: moduli capped so that tables stay small against the curve's
 // work, and the staged rows fit the shared-memory budget.
-FastPlan wide_plan(const std::vector<std::string> &coefficients, long long bound, long double work) {
+FastPlan wide_plan(const std::vector<std::string> &coefficients, long long bound, long double work,
+                   int smem_budget) {
     int cap = int(std::min<long double>(kMaxModulus, std::max<long double>(64, std::sqrt(work / 48.0L))));
     for (;;) {
         FastPlan plan = choose_fast_plan(coefficients, bound, cap, true);
@@ -1039,7 +1048,7 @@ FastPlan wide_plan(const std::vector<std::string> &coefficients, long long bound
             const int m = sl < int(plan.moduli.size()) ? plan.moduli[sl] : 1;
             smem += round_even(m + dev::kWExt);
         }
-        if (smem <= dev::kWMaxSmemWords || cap <= 64) return plan;
+        if (smem <= smem_budget || cap <= 64) return plan;
         cap = cap * 7 / 8;
     }
 }
@@ -1089,7 +1098,10 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             cw.words = word_count64(c.bound);
             cw.count = c.last >= c.first ? c.last - c.first + 1 : 0;
             cw.wide = cw.words >= kBatchWideWords;
-            if (cw.wide) cw.plan = wide_plan(c.coefficients, c.bound, (long double)cw.words * cw.count);
+            if (cw.wide)
+                cw.plan = wide_plan(c.coefficients, c.bound, (long double)cw.words * cw.count,
+                                    cw.words >= dev::kWHugeWords ? 2 * dev::kWMaxSmemWords
+                                                                 : dev::kWMaxSmemWords);
             else cw.plan = choose_fast_plan(c.coefficients, c.bound, kBatchNarrowModulus, false);
             r.wide = cw.wide;
             r.class_prime = cw.plan.class_prime;
@@ -1200,7 +1212,10 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 Md.step = dev::u32((dev::kWarpSize * dev::kWK) % m);
             }
             C.smem_words = smem;
-            P.wide_smem_words = std::max(P.wide_smem_words, smem);
+            C.nbuf = cw.words >= dev::kWHugeWords ? 1 : 2;
+            // row buffers are row_stride words apart; a one-buffer curve spans both
+            P.wide_smem_words =
+                std::max(P.wide_smem_words, round_even(C.nbuf == 2 ? smem : (smem + 1) / 2));
             two_adic_classes(c.coefficients, C.admissible);
             if (q > 1) {
                 const auto aff = affine_mask(q, c.coefficients);
