@@ -237,6 +237,8 @@ T *device_alloc(std::size_t count, const char *what) {
 
 }  // namespace
 
+constexpr long long kInitialSurvivors = 1 << 16;  // survivors per buffer before any growth
+
 struct Sieve::Impl {
     SieveOptions opt;
     long long bound = 0, words = 0;
@@ -252,12 +254,14 @@ struct Sieve::Impl {
     std::vector<dev::u64> fast_adm_host;
     FastPlan fast_plan;
     long long max_tile = dev::kMaxTileWords;
-    long long capacity = 0;
+    long long capacity = 0;       // most survivors a buffer may grow to hold
+    long long host_capacity = 0;  // entries of the pinned host arrays
     SieveTimings timings;
 
     struct Buffer {
         long long *a = nullptr;
         int *d = nullptr;
+        long long cap = 0;        // entries of a and d
         unsigned long long *count = nullptr;  // [0] survivors, [1] work counter, [2] error word
         cudaEvent_t begin = nullptr, end = nullptr;
         long long first = 0, last = 0;
@@ -387,21 +391,27 @@ struct Sieve::Impl {
                                                                  dev::kThreads, dev::kRefSmem),
                    "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
         grid = std::max(1, sms * std::max(1, per_sm));
-        // RPG_SURVIVOR_CAPACITY overrides the per-buffer survivor capacity (at
-        // least 64, one word's worth); tests use it to drive the split path.
+        // Survivor buffers start small (most searches have few survivors) and
+        // grow on overflow up to the per-buffer capacity; past it a batch is
+        // split.  RPG_SURVIVOR_CAPACITY fixes both at its value (at least 64,
+        // one word's worth); tests use it to drive the split path.
         capacity = opt.capacity;
-        if (const char *env = std::getenv("RPG_SURVIVOR_CAPACITY")) capacity = std::atoll(env);
+        long long initial = std::min<long long>(capacity, kInitialSurvivors);
+        if (const char *env = std::getenv("RPG_SURVIVOR_CAPACITY")) initial = capacity = std::atoll(env);
         capacity = std::max<long long>(capacity, 64);
+        initial = std::max<long long>(initial, 64);
         for (auto &b : buf) {
-            b.a = device_alloc<long long>(std::size_t(capacity), "cudaMalloc(survivors)");
-            b.d = device_alloc<int>(std::size_t(capacity), "cudaMalloc(survivors)");
+            b.a = device_alloc<long long>(std::size_t(initial), "cudaMalloc(survivors)");
+            b.d = device_alloc<int>(std::size_t(initial), "cudaMalloc(survivors)");
+            b.cap = initial;
             b.count = device_alloc<unsigned long long>(3, "cudaMalloc(count)");
             check_cuda(cudaEventCreate(&b.begin), "cudaEventCreate");
             check_cuda(cudaEventCreate(&b.end), "cudaEventCreate");
         }
         check_cuda(cudaMallocHost(&h_count, 2 * sizeof(unsigned long long)), "cudaMallocHost");
-        check_cuda(cudaMallocHost(&h_a, std::size_t(capacity) * sizeof(long long)), "cudaMallocHost");
-        check_cuda(cudaMallocHost(&h_d, std::size_t(capacity) * sizeof(int)), "cudaMallocHost");
+        check_cuda(cudaMallocHost(&h_a, std::size_t(initial) * sizeof(long long)), "cudaMallocHost");
+        check_cuda(cudaMallocHost(&h_d, std::size_t(initial) * sizeof(int)), "cudaMallocHost");
+        host_capacity = initial;
         timings.workspace_ms += ms_since(t0);
         if (opt.plan == PlanKind::fast) build_fast_tables(coefficients);
         else build_tables(coefficients);
@@ -636,7 +646,7 @@ struct Sieve::Impl {
         A.out_a = buf[which].a;
         A.out_d = buf[which].d;
         A.out_count = buf[which].count;
-        A.capacity = (unsigned long long)capacity;
+        A.capacity = (unsigned long long)buf[which].cap;
         A.error = buf[which].count + 2;
         return A;
     }
@@ -736,6 +746,36 @@ struct Sieve::Impl {
         out.complete = complete;
     }
 
+    // Grow buffer `which` (idle) to hold n survivors if the capacity allows;
+    // false if it is already as large as it may get.
+    bool grow(int which, unsigned long long n) {
+        Buffer &b = buf[which];
+        if (b.cap >= capacity) return false;
+        const long long cap = std::min<long long>(capacity, (long long)(n + n / 4 + 1024));
+        const auto t0 = Clock::now();
+        check_cuda(cudaStreamSynchronize(stream), "sieve stream");
+        cudaFree(b.a);
+        cudaFree(b.d);
+        b.a = nullptr;
+        b.d = nullptr;
+        b.cap = 0;
+        b.a = device_alloc<long long>(std::size_t(cap), "cudaMalloc(survivors)");
+        b.d = device_alloc<int>(std::size_t(cap), "cudaMalloc(survivors)");
+        b.cap = cap;
+        if (host_capacity < cap) {
+            cudaFreeHost(h_a);
+            cudaFreeHost(h_d);
+            h_a = nullptr;
+            h_d = nullptr;
+            host_capacity = 0;
+            check_cuda(cudaMallocHost(&h_a, std::size_t(cap) * sizeof(long long)), "cudaMallocHost");
+            check_cuda(cudaMallocHost(&h_d, std::size_t(cap) * sizeof(int)), "cudaMallocHost");
+            host_capacity = cap;
+        }
+        timings.workspace_ms += ms_since(t0);
+        return true;
+    }
+
     // Queue a batch as pieces: word tiles of at most kMaxTileWords.
     void queue_pieces(long long first, long long last) {
         piece_batch_first = first;
@@ -773,9 +813,10 @@ struct Sieve::Impl {
             const unsigned long long n = h_count[which];
             const float ms = elapsed(buf[which]);
             timings.sieve_ms += ms;
-            if (n > (unsigned long long)capacity) {
+            if (n > (unsigned long long)buf[which].cap) {
                 ++timings.reruns;
-                split_front(p);
+                if (!grow(which, n)) split_front(p);
+                else pieces.push_front(p);
                 continue;
             }
             deliver(out, which, std::size_t(n), ms, piece_batch_first, piece_batch_last,
@@ -810,12 +851,13 @@ struct Sieve::Impl {
         check_error_word(which);
         const float ms = elapsed(b);
         timings.sieve_ms += ms;
-        if (n > (unsigned long long)capacity) {
+        if (n > (unsigned long long)b.cap) {
             ++timings.reruns;
             b.busy = false;
             piece_batch_first = b.first;
             piece_batch_last = b.last;
-            split_front(Piece{b.first, b.last, 0, words});
+            if (grow(which, n)) pieces.push_front(Piece{b.first, b.last, 0, words});
+            else split_front(Piece{b.first, b.last, 0, words});
             return next_piece(out);
         }
         deliver(out, which, std::size_t(n), ms, b.first, b.last, true);
