@@ -226,14 +226,20 @@ def reference_gpu(coeffs, denominators, rpg):
                     "once (the reference rebuilds it per batch)"}
 
 
-def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2):
+def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2, shape="all"):
     """Mixed many-curve batch: one batched pass against the plain per-curve
     loop of single-curve searches, same curves, points compared curve by curve.
     Both are timed end to end through the C ABI (coefficient strings in,
-    verified points out)."""
+    verified points out).  shape "wide" / "narrow" keeps only the curves whose
+    rows have at least / fewer than 2,048 words of 64 numerators (the two
+    batch kernels), for per-kernel measurements."""
     import workloads
 
     curves = workloads.mixed_batch(count)
+    if shape != "all":
+        wide = lambda c: (2 * c["bound"] + 64) // 64 >= 2048
+        curves = [c for c in curves if wide(c) == (shape == "wide")]
+        count = len(curves)
     mu = workloads.mobius(max(c["last"] for c in curves))
     reduced = [workloads.reduced_sites(c["bound"], c["first"], c["last"], mu) for c in curves]
     rect = [(2 * c["bound"] + 1) * (c["last"] - c["first"] + 1) for c in curves]
@@ -249,11 +255,12 @@ def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2):
     plain = [rpg.point_search(c["coefficients"], c["bound"], c["first"], c["last"])[0]
              for c in curves[:n_plain]]
     plain_wall = time.perf_counter() - t0
-    identical = all(a == b for a, b in zip(plain, points[:n_plain]))
+    identical = all(a == b for a, b in zip(plain, points[:n_plain])) if n_plain else None
     total_reduced, plain_reduced = sum(reduced), sum(reduced[:n_plain])
     batched = total_reduced / wall / 1e9
-    plain_value = plain_reduced / plain_wall / 1e9
+    plain_value = plain_reduced / plain_wall / 1e9 if n_plain else None
     return {
+        "shape": shape,
         "workload": f"{count} seeded squarefree curves: degree uniform in {{3,4,5,6,8,10}}, "
                     "coefficients random sign x random integer of bit length uniform in 8..64, "
                     "numerator bound A and denominator bound B independent, each log-uniform "
@@ -272,7 +279,7 @@ def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2):
         "plain_loop": {"value": plain_value, "unit": UNIT, "wall_s": plain_wall,
                        "curves": n_plain,
                        "note": "rpg_point_search (single-curve fast plan) called once per curve"},
-        "speedup_vs_plain": batched / plain_value,
+        "speedup_vs_plain": batched / plain_value if plain_value else None,
         "points_identical": identical,
     }
 
@@ -416,6 +423,8 @@ def main():
                         help="curves of the mixed batch (0: skip the batch measurement)")
     parser.add_argument("--batch-plain-curves", type=int, default=4096,
                         help="curves of the batch also run as a plain per-curve loop")
+    parser.add_argument("--batch-shape", choices=["all", "wide", "narrow"], default="all",
+                        help="keep only the batch curves of one kernel")
     parser.add_argument("--restricted", type=int, default=256,
                         help="high-degree interval-restricted curves (0: skip)")
     parser.add_argument("--square-cubics", type=int, default=32,
@@ -535,7 +544,8 @@ def main():
             "note": "same kernel family with the reference's 32-prime plan: survivor set "
                     "identical to the reference implementation's"}
     if args.batch_curves > 0:
-        line["batch"] = batch_benchmark(rpg, args.batch_curves, args.batch_plain_curves)
+        line["batch"] = batch_benchmark(rpg, args.batch_curves, args.batch_plain_curves,
+                                        shape=args.batch_shape)
     if args.restricted > 0:
         line["restricted"] = restricted_benchmark(rpg, args.restricted, args.square_cubics)
     if args.serving_requests > 0:
