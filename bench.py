@@ -226,7 +226,7 @@ def reference_gpu(coeffs, denominators, rpg):
                     "once (the reference rebuilds it per batch)"}
 
 
-def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2, shape="all"):
+def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2, shape="all", smem_peak_gbs=None):
     """Mixed many-curve batch: one batched pass against the plain per-curve
     loop of single-curve searches, same curves, points compared curve by curve.
     Both are timed end to end through the C ABI (coefficient strings in,
@@ -280,6 +280,15 @@ def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2, shape="all"):
                        "curves": n_plain,
                        "note": "rpg_point_search (single-curve fast plan) called once per curve"},
         "speedup_vs_plain": batched / plain_value if plain_value else None,
+        "roofline": None if not smem_peak_gbs else {
+            "bound": "smem", "unit": "GB/s",
+            "achieved": stats["smem_bytes"] / (stats["sieve_ms"] / 1e3) / 1e9,
+            "peak": smem_peak_gbs,
+            "frac": stats["smem_bytes"] / (stats["sieve_ms"] / 1e3) / 1e9 / smem_peak_gbs,
+            "swept_words": stats["swept_words"], "smem_bytes": stats["smem_bytes"],
+            "algorithmic": "8 B per stage-1 modulus of each curve's plan per swept 64-site word "
+                           "(class words on the wide kernel, row words on the narrow one), both "
+                           "kernels' time"},
         "points_identical": identical,
     }
 
@@ -545,7 +554,7 @@ def main():
                     "identical to the reference implementation's"}
     if args.batch_curves > 0:
         line["batch"] = batch_benchmark(rpg, args.batch_curves, args.batch_plain_curves,
-                                        shape=args.batch_shape)
+                                        shape=args.batch_shape, smem_peak_gbs=peak)
     if args.restricted > 0:
         line["restricted"] = restricted_benchmark(rpg, args.restricted, args.square_cubics)
     if args.serving_requests > 0:

@@ -211,6 +211,8 @@ typedef struct rpg_batch_stats {
     uint64_t launches;         /* kernel launches (table build and sieve) */
     uint64_t words;            /* 64-site row words of all denominators */
     uint64_t table_words;      /* stage-1 table words resident on the device */
+    uint64_t swept_words;      /* 64-site words the sieve kernels sweep (whole rows) */
+    uint64_t smem_bytes;       /* stage-1 shared-memory bytes those sweeps read */
     double rectangle_sites;    /* sum over curves of (2H + 1) x denominators */
     double plan_ms;            /* host: validation, plans, descriptors */
     double table_ms;           /* device table build, CUDA events */

@@ -36,10 +36,12 @@ constexpr int kClassBits = 8;
 constexpr int kMaxClasses = kMaxFastClasses;
 constexpr long long kMaxClassWords = 1LL << 23;         // class word index fits 24 bits
 constexpr int kAdmQ = 16;                               // residue words for class primes <= 13
-constexpr int kNarrowSlots = 6;
+constexpr int kNarrowSlots = 8;
+constexpr int kNK = 4;                                  // consecutive row words per lane
+constexpr int kND = 4;                                  // consecutive parameters per warp fetch
 constexpr int kNWarps = 8;
 constexpr int kNThreads = kNWarps * kWarpSize;
-constexpr int kNarrowTableWords = 7040;                 // sum of m^2 (+ padding) per curve
+constexpr int kNarrowTableWords = 7680;                 // sum of m (m + kNK - 1) per curve
 constexpr int kAffWords = kCandidatePrimes * 8;         // the 36 candidate bitmasks
 constexpr int kRefWords = 8;                            // u64 words of a bitmask over [0, 512)
 constexpr int kMaxFactors = 4;
@@ -63,6 +65,7 @@ struct WideCurve {
     long long stride;              // S = 64 M: numerator step between words of a class
     long long count_q;             // 2H = count_q M + count_r
     long long aff;                 // u64 offset of the 36 candidate bitmasks
+    long long cls;                 // index of the curve's ClassStart[M] block
     Modulus mod[kWideSlots];
     u64 admissible[64 + kAdmQ];    // 2-adic classes by d mod 64, residues mod q by d mod q
     int count_r;
@@ -96,8 +99,9 @@ struct NarrowCurve {
     int index;
     int m[kNarrowSlots];           // moduli (1: padding)
     int off[kNarrowSlots];         // word offset of each table inside the block
+    int len[kNarrowSlots];         // row length m + kNK - 1 (rows repeat their first words)
     u32 shift[kNarrowSlots];       // (-H) 64^-1 mod m: table word of row word 0
-    u32 step[kNarrowSlots];        // 32 mod m
+    u32 step[kNarrowSlots];        // (32 kNK) mod m
     unsigned short neg_h[kCandidatePrimes];
     int nint;
     double lo[kMaxIntervals];
@@ -355,10 +359,21 @@ __device__ __forceinline__ void emit(u64 m, long long base, long long step, long
 struct ClassRun {
     int wbase;
     int words;
+    unsigned short r;              // class residue mod M
     unsigned short ofs;            // (r + H) mod M: the class's least a is -H + ofs
     unsigned char first;
     unsigned char last;
+    unsigned short pad;
 };
+
+// Per curve and class residue r mod M (precomputed on the host): the row
+// index of class word 0 for each modulus, (a0 S^-1) mod m with a0 = -H + ofs.
+struct ClassStart {
+    unsigned short start[kWideSlots];
+    unsigned short ofs;            // (r + H) mod M
+    unsigned short pad;
+};
+static_assert(sizeof(ClassStart) == 16, "one 16-byte load per class");
 
 __device__ __forceinline__ void wide_drain(const u64 *qmask, const u32 *qinfo, int start, int n,
                                            const WideCurve &C, const Candidates &cand,
@@ -411,25 +426,30 @@ __device__ __forceinline__ int nth_bit64(u64 mask, int n) {
     return pos;
 }
 
-// Wide rows.  Per denominator: warp 0 selects the 32 reference primes, warp
-// 1 lays out the admissible classes and their sweep items, the other warps
-// wait; then every warp sweeps items.  The stage-1 rows of the next live
-// denominator of the item are copied (TMA bulk copies, one mbarrier per
-// buffer) into the other of two row buffers while this one is swept.
+// Wide rows, one CTA per denominator, software-pipelined over the
+// denominators of an item: while every warp sweeps denominator d_i (rows in
+// buffer b, class runs and prime selection in set s), warp 0 selects the
+// reference primes of the next live denominator d_j and warp 1 lays out its
+// classes into set s ^ 1, and thread 0 copies its rows into buffer b ^ 1
+// (TMA bulk copies, one mbarrier per buffer); one barrier per denominator.
+// Curves with huge rows use one row buffer of twice the size: their next
+// rows are copied after the barrier.
 __global__ void __launch_bounds__(kWThreads, 3)
     wide_kernel(const WideCurve *__restrict__ curves, const BatchItem *__restrict__ items,
                 int nitems, const u64 *__restrict__ pool, const u64 *__restrict__ affine,
+                const ClassStart *__restrict__ class_starts,
                 const unsigned short *__restrict__ inv_table, Candidates cand, BatchOut out,
                 int row_stride, unsigned long long *work) {
     extern __shared__ __align__(16) u64 smem[];
     __shared__ WideCurve C;
     __shared__ u64 s_aff[kAffWords];
+    __shared__ ClassRun s_run[2][kMaxClasses];
+    __shared__ int s_prefix[2][kMaxClasses + 1];
+    __shared__ int s_nclass[2];
+    __shared__ int s_ci[2][kSelectedPrimes];
+    __shared__ u32 s_dinv[2][kSelectedPrimes];
+    __shared__ int s_next[2];
     __shared__ int s_item;
-    __shared__ ClassRun s_run[kMaxClasses];
-    __shared__ int s_prefix[kMaxClasses + 1];
-    __shared__ int s_ci[kSelectedPrimes];
-    __shared__ u32 s_dinv[kSelectedPrimes];
-    __shared__ int s_next;
     __shared__ int s_abort;
     __shared__ __align__(8) unsigned long long s_bar[2];
 
@@ -437,7 +457,6 @@ __global__ void __launch_bounds__(kWThreads, 3)
     const int warp = threadIdx.x >> 5;
     u64 *qmask = smem + 2 * row_stride;
     u32 *qinfo = reinterpret_cast<u32 *>(qmask + kWWarps * kQueue);
-    u32 *s_start = qinfo + kWWarps * kQueue;  // [kMaxClasses][kWideSlots]
     u64 *wq_mask = qmask + warp * kQueue;
     u32 *wq_info = qinfo + warp * kQueue;
     u32 phase = 0;     // bit b: parity of buffer b's next completion
@@ -468,11 +487,15 @@ __global__ void __launch_bounds__(kWThreads, 3)
         }
         const int q = C.class_prime;
         const int M = C.class_mod;
+        const ClassStart *cstart = class_starts + C.cls;
+        auto param = [&](int i) {
+            const long long k = item.first + i;
+            return C.square ? k * k : k;
+        };
         // parameters whose denominator has no admissible class, or no
         // numerator range of this item's index, are skipped
         auto live = [&](int i) {
-            const long long k = item.first + i;
-            const long long d = C.square ? k * k : k;
+            const long long d = param(i);
             const u32 du = u32(d);
             if (C.admissible[du & 63] == 0 || (q > 1 && C.admissible[64 + int(du % u32(q))] == 0))
                 return false;
@@ -480,9 +503,12 @@ __global__ void __launch_bounds__(kWThreads, 3)
             long long L, U;
             return x_range(C.lo, C.hi, C.nint, C.bound, d, item.range, L, U);
         };
+        auto next_live = [&](int i) {
+            while (i < item.count && !live(i)) ++i;
+            return i;
+        };
         auto stage_rows = [&](int i, int b) {  // thread 0: copy parameter i's rows into buffer b
-            const long long k = item.first + i;
-            const u32 du = u32(C.square ? k * k : k);
+            const u32 du = u32(param(i));
             const u32 bar = smem_addr(&s_bar[b]);
             const u32 dst = smem_addr(smem + b * row_stride);
             fence_proxy_async_shared();
@@ -496,27 +522,18 @@ __global__ void __launch_bounds__(kWThreads, 3)
                                     u32(Md.length) * 8u, bar);
             }
         };
-        int i = 0;
-        while (i < item.count && !live(i)) ++i;
-        int b = 0;
-        if (i < item.count) {
-            if (threadIdx.x == 0) stage_rows(i, b);
-            pending |= 1u << b;
-        }
-        while (i < item.count) {
-            const long long k = item.first + i;
-            const long long d = C.square ? k * k : k;
+        // warps 0 and 1: prime selection and class runs of parameter i into set st
+        auto setup = [&](int i, int st) {
+            const long long d = param(i);
             const u32 du = u32(d);
-            const u64 classes2 = C.admissible[du & 63];
-            const u64 classesq = q > 1 ? C.admissible[64 + int(du % u32(q))] : u64(1);
-            const int nq = __popcll(classesq);
-            const int nclass = __popcll(classes2) * nq;
-
             if (warp == 0) {
-                select_warp(du, cand, inv_table, s_ci, s_dinv);
-                if (lane == 0) s_next = 0;
+                select_warp(du, cand, inv_table, s_ci[st], s_dinv[st]);
+                if (lane == 0) s_next[st] = 0;
             } else if (warp == 1) {
-                // the numerator range [lo_a, hi_a] of this item for d
+                const u64 classes2 = C.admissible[du & 63];
+                const u64 classesq = q > 1 ? C.admissible[64 + int(du % u32(q))] : u64(1);
+                const int nq = __popcll(classesq);
+                const int nclass = __popcll(classes2) * nq;
                 long long lo_a = -C.bound, hi_a = C.bound;
                 if (C.nint > 0) x_range(C.lo, C.hi, C.nint, C.bound, d, item.range, lo_a, hi_a);
                 // classes, 32 per pass: class c = (c / nq)-th 2-adic class crossed
@@ -532,8 +549,7 @@ __global__ void __launch_bounds__(kWThreads, 3)
                             const int rq = nth_bit64(classesq, c % nq);
                             r = r64 + 64 * int(C.crt[C.mod_q[r64] * 13 + rq]);
                         }
-                        int ofs = r + C.h_mod_m;
-                        if (ofs >= M) ofs -= M;
+                        const int ofs = cstart[r].ofs;
                         // sites of class r: a = -H + ofs + M t, t in [0, count); those
                         // in [lo_a, hi_a] are t in [t_lo, t_hi]
                         const long long count = C.count_q + (ofs <= C.count_r ? 1 : 0);
@@ -546,7 +562,9 @@ __global__ void __launch_bounds__(kWThreads, 3)
                             t_hi = above < 0 ? -1 : min(count - 1, above / M);
                         }
                         ClassRun run;
+                        run.r = (unsigned short)r;
                         run.ofs = (unsigned short)ofs;
+                        run.pad = 0;
                         if (t_lo <= t_hi) {
                             run.wbase = int(t_lo >> 6);
                             run.words = int((t_hi >> 6) - (t_lo >> 6) + 1);
@@ -558,14 +576,7 @@ __global__ void __launch_bounds__(kWThreads, 3)
                             run.first = 0;
                             run.last = 64;
                         }
-                        s_run[c] = run;
-#pragma unroll
-                        for (int sl = 0; sl < kWideSlots; ++sl) {
-                            const Modulus &Md = C.mod[sl];
-                            const u32 a0m = mod_u32(Md.neg_h + u32(ofs), u32(Md.m), Md.magic);
-                            s_start[c * kWideSlots + sl] =
-                                mod_u32(a0m * Md.inv_stride, u32(Md.m), Md.magic);
-                        }
+                        s_run[st][c] = run;
                         nitems_c = (run.words + kWItemWords - 1) / kWItemWords;
                     }
                     int incl = nitems_c;
@@ -574,18 +585,33 @@ __global__ void __launch_bounds__(kWThreads, 3)
                         const int v = __shfl_up_sync(kFullMask, incl, o);
                         if (lane >= o) incl += v;
                     }
-                    if (c < nclass) s_prefix[c] = carry + incl - nitems_c;
+                    if (c < nclass) s_prefix[st][c] = carry + incl - nitems_c;
                     carry += __shfl_sync(kFullMask, incl, 31);
                 }
-                if (lane == 0) s_prefix[nclass] = carry;
+                if (lane == 0) {
+                    s_prefix[st][nclass] = carry;
+                    s_nclass[st] = nclass;
+                }
             }
-            __syncthreads();
-            // every warp is past the previous sweep: the other buffer is free
-            int next = i + 1;
-            while (next < item.count && !live(next)) ++next;
-            if (C.nbuf == 2 && next < item.count) {
-                if (threadIdx.x == 0) stage_rows(next, b ^ 1);
-                pending |= 1u << (b ^ 1);
+        };
+
+        int i = next_live(0);
+        int b = 0, st = 0;
+        if (i < item.count) {
+            if (threadIdx.x == 0) stage_rows(i, b);
+            pending |= 1u << b;
+            setup(i, st);
+        }
+        __syncthreads();
+        while (i < item.count) {
+            const long long d = param(i);
+            const int next = next_live(i + 1);
+            if (next < item.count) {
+                setup(next, st ^ 1);
+                if (C.nbuf == 2) {
+                    if (threadIdx.x == 0) stage_rows(next, b ^ 1);
+                    pending |= 1u << (b ^ 1);
+                }
             }
             if (!mbar_wait(smem_addr(&s_bar[b]), (phase >> b) & 1u)) {  // bounded wait
                 s_abort = 1;
@@ -595,7 +621,10 @@ __global__ void __launch_bounds__(kWThreads, 3)
             pending &= ~(1u << b);
 
             const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
-            const int total_items = s_prefix[nclass];
+            const int nclass = s_nclass[st];
+            const int *prefix = s_prefix[st];
+            const ClassRun *runs = s_run[st];
+            const int total_items = prefix[nclass];
             int qn = 0;
             u32 step8[kWideSlots], mod8[kWideSlots];
             const unsigned char *slot_base[kWideSlots];
@@ -607,25 +636,26 @@ __global__ void __launch_bounds__(kWThreads, 3)
             }
             for (;;) {
                 int sweep = 0;
-                if (lane == 0) sweep = atomicAdd(&s_next, 1);
+                if (lane == 0) sweep = atomicAdd(&s_next[st], 1);
                 sweep = __shfl_sync(kFullMask, sweep, 0);
                 if (sweep >= total_items) break;
                 int c = 0;
                 for (int base = 0; base < nclass; base += 32) {
                     const int cc = base + lane;
-                    const u32 bb = __ballot_sync(kFullMask, cc < nclass && s_prefix[cc] <= sweep);
+                    const u32 bb = __ballot_sync(kFullMask, cc < nclass && prefix[cc] <= sweep);
                     if (bb) c = base + 31 - __clz(bb);
                     if (bb != kFullMask) break;
                 }
-                const int w0 = (sweep - s_prefix[c]) * kWItemWords;
-                const ClassRun run = s_run[c];
+                const int w0 = (sweep - prefix[c]) * kWItemWords;
+                const ClassRun run = runs[c];
+                const ClassStart cs = cstart[run.r];
                 const int wt = run.words;
                 const u64 first_mask = ~u64(0) << run.first;
                 const u64 last_mask = run.last >= 64 ? ~u64(0) : ((u64(1) << run.last) - 1);
                 u32 o[kWideSlots];
 #pragma unroll
                 for (int sl = 0; sl < kWideSlots; ++sl)
-                    o[sl] = 8u * mod_u32(s_start[c * kWideSlots + sl] + u32(run.wbase + w0 + lane),
+                    o[sl] = 8u * mod_u32(u32(cs.start[sl]) + u32(run.wbase + w0 + lane),
                                          u32(C.mod[sl].m), C.mod[sl].magic);
 #pragma unroll 1
                 for (int step = 0; step < kWSteps; ++step) {
@@ -666,8 +696,8 @@ __global__ void __launch_bounds__(kWThreads, 3)
                             qn += __popc(bb);
                             if (qn >= 32) {
                                 __syncwarp();
-                                wide_drain(wq_mask, wq_info, qn - 32, 32, C, cand, s_aff, s_ci,
-                                           s_dinv, s_run, d, out);
+                                wide_drain(wq_mask, wq_info, qn - 32, 32, C, cand, s_aff, s_ci[st],
+                                           s_dinv[st], runs, d, out);
                                 qn -= 32;
                             }
                         }
@@ -675,7 +705,7 @@ __global__ void __launch_bounds__(kWThreads, 3)
                 }
             }
             __syncwarp();
-            wide_drain(wq_mask, wq_info, 0, qn, C, cand, s_aff, s_ci, s_dinv, s_run, d, out);
+            wide_drain(wq_mask, wq_info, 0, qn, C, cand, s_aff, s_ci[st], s_dinv[st], runs, d, out);
             __syncthreads();
             if (s_abort) {
                 // a bulk copy did not complete in time: give the copies in
@@ -689,6 +719,7 @@ __global__ void __launch_bounds__(kWThreads, 3)
                 return;
             }
             i = next;
+            st ^= 1;
             if (C.nbuf == 2) {
                 b ^= 1;
             } else if (i < item.count) {  // one buffer: copy the next row now that it is free
@@ -794,13 +825,27 @@ __global__ void __launch_bounds__(kNThreads, 3)
         int *w_ci = s_ci[warp];
         u32 *w_dinv = s_dinv[warp];
         for (;;) {
-            int idx = 0;
-            if (lane == 0) idx = atomicAdd(&s_next, 1);
-            idx = __shfl_sync(kFullMask, idx, 0);
-            if (idx >= item.count) break;
-            const long long k = item.first + idx;
+            int idx0 = 0;
+            if (lane == 0) idx0 = atomicAdd(&s_next, kND);
+            idx0 = __shfl_sync(kFullMask, idx0, 0);
+            if (idx0 >= item.count) break;
+            const int jn = min(kND, item.count - idx0);
+            u32 rho[kNarrowSlots];
+            for (int j = 0; j < jn; ++j) {
+            const long long k = item.first + idx0 + j;
             const long long d = C.square ? k * k : k;
             const u32 du = u32(d);
+            // d mod m for every modulus: reduced for the first parameter of the
+            // fetch (and for square denominators), else advanced by one
+#pragma unroll
+            for (int s = 0; s < kNarrowSlots; ++s) {
+                if (j == 0 || C.square) {
+                    rho[s] = mod_u32(du, u32(C.m[s]), C.magic[s]);
+                } else {
+                    rho[s] += 1;
+                    if (rho[s] == u32(C.m[s])) rho[s] = 0;
+                }
+            }
             const u64 mask2 = C.dense2[du & 63];
             if (!mask2) continue;
             // words [w_lo, w_hi] hold the numerator range of this item: a in [L, U]
@@ -810,51 +855,68 @@ __global__ void __launch_bounds__(kNThreads, 3)
             const u64 first_mask = ~u64(0) << ((L + C.bound) & 63);
             const int last_bits = int((U + C.bound) & 63) + 1;
             const u64 last_mask = last_bits >= 64 ? ~u64(0) : ((u64(1) << last_bits) - 1);
+            // lane l takes words w0 + kNK l .. w0 + kNK l + kNK - 1 of each
+            // 128-word step: rows repeat their first kNK - 1 words, so the kNK
+            // words of a lane never wrap and one index per modulus advances
             u32 base[kNarrowSlots], at[kNarrowSlots], mods[kNarrowSlots], steps[kNarrowSlots];
 #pragma unroll
             for (int s = 0; s < kNarrowSlots; ++s) {
                 const u32 m = u32(C.m[s]);
                 mods[s] = m;
                 steps[s] = C.step[s];
-                base[s] = u32(C.off[s]) + mod_u32(du, m, C.magic[s]) * m;
-                at[s] = mod_u32(C.shift[s] + u32(w_lo + lane), m, C.magic[s]);
+                base[s] = u32(C.off[s]) + rho[s] * u32(C.len[s]);
+                at[s] = mod_u32(C.shift[s] + u32(w_lo + kNK * lane), m, C.magic[s]);
             }
             bool selected = false;
             int qn = 0;
-            for (int w0 = w_lo; w0 <= w_hi; w0 += kWarpSize) {
-                const int w = w0 + lane;
-                u64 acc = mask2;
+            for (int w0 = w_lo; w0 <= w_hi; w0 += kWarpSize * kNK) {
+                u64 acc[kNK];
+#pragma unroll
+                for (int k = 0; k < kNK; ++k) acc[k] = mask2;
 #pragma unroll
                 for (int s = 0; s < kNarrowSlots; ++s) {
-                    acc &= tab[base[s] + at[s]];
-                    const u32 t = at[s] + steps[s];  // advance 32 words mod m
+                    const u64 *row = tab + base[s] + at[s];
+#pragma unroll
+                    for (int k = 0; k < kNK; ++k) acc[k] &= row[k];
+                    const u32 t = at[s] + steps[s];  // advance 32 kNK words mod m
                     at[s] = min(t, t - mods[s]);
                 }
-                if (w > w_hi) acc = 0;
-                if (w == w_lo) acc &= first_mask;
-                if (w == w_hi) acc &= last_mask;
-                const u32 b = __ballot_sync(kFullMask, acc != 0);
-                if (!b) continue;
-                const int pos = qn + __popc(b & lanemask_lt());
-                if (acc) {
-                    wq_mask[pos] = acc;
-                    wq_word[pos] = u32(w);
+                const int wl = w0 + kNK * lane;
+#pragma unroll
+                for (int k = 0; k < kNK; ++k) {
+                    const int w = wl + k;
+                    if (w > w_hi) acc[k] = 0;
+                    if (w == w_lo) acc[k] &= first_mask;
+                    if (w == w_hi) acc[k] &= last_mask;
                 }
-                qn += __popc(b);
-                if (qn >= 32) {
-                    if (!selected) {
-                        select_warp(du, cand, inv_table, w_ci, w_dinv);
-                        selected = true;
+                if (!__ballot_sync(kFullMask, (acc[0] | acc[1] | acc[2] | acc[3]) != 0)) continue;
+#pragma unroll
+                for (int k = 0; k < kNK; ++k) {
+                    const u32 b = __ballot_sync(kFullMask, acc[k] != 0);
+                    if (!b) continue;
+                    const int pos = qn + __popc(b & lanemask_lt());
+                    if (acc[k]) {
+                        wq_mask[pos] = acc[k];
+                        wq_word[pos] = u32(wl + k);
                     }
-                    __syncwarp();
-                    narrow_drain(wq_mask, wq_word, qn - 32, 32, C, cand, s_aff, w_ci, w_dinv, d, out);
-                    qn -= 32;
+                    qn += __popc(b);
+                    if (qn >= 32) {
+                        if (!selected) {
+                            select_warp(du, cand, inv_table, w_ci, w_dinv);
+                            selected = true;
+                        }
+                        __syncwarp();
+                        narrow_drain(wq_mask, wq_word, qn - 32, 32, C, cand, s_aff, w_ci, w_dinv, d,
+                                     out);
+                        qn -= 32;
+                    }
                 }
             }
             if (qn) {
                 if (!selected) select_warp(du, cand, inv_table, w_ci, w_dinv);
                 __syncwarp();
                 narrow_drain(wq_mask, wq_word, 0, qn, C, cand, s_aff, w_ci, w_dinv, d, out);
+            }
             }
         }
         __syncthreads();
@@ -1036,6 +1098,55 @@ struct CurveWork {
     long long count = 0;       // parameters
 };
 
+// Narrow plan: every odd prime up to kBatchNarrowModulus that filters at
+// least 0.15 bit, strongest first, each joining the slot whose product stays
+// within the cap (smallest product first) or opening a new slot, while the
+// tables (m rows of m + kNK - 1 words per slot) fit shared memory.
+FastPlan narrow_plan(const std::vector<std::string> &coefficients) {
+    std::vector<std::pair<double, int>> strength;
+    for (int q = 3; q <= kBatchNarrowModulus; q += 2) {
+        if (!is_small_prime(q)) continue;
+        const double rate = pass_rate(q, coefficients);
+        const double bits = rate > 0 ? -std::log2(rate) : 8.0;
+        if (bits >= 0.15) strength.push_back({bits, q});
+    }
+    std::sort(strength.begin(), strength.end(), [](const auto &a, const auto &b) {
+        return a.first != b.first ? a.first > b.first : a.second < b.second;
+    });
+    auto words = [](long long m) { return m * (m + dev::kNK - 1); };
+    FastPlan plan;
+    long long used = 0;
+    for (const auto &sq : strength) {
+        const int q = sq.second;
+        int join = -1;
+        for (std::size_t i = 0; i < plan.moduli.size(); ++i)
+            if (plan.moduli[i] * q <= kBatchNarrowModulus &&
+                (join < 0 || plan.moduli[i] < plan.moduli[std::size_t(join)]))
+                join = int(i);
+        if (join >= 0) {
+            const long long m = plan.moduli[std::size_t(join)];
+            const long long grown = used - words(m) + words(m * q);
+            if (grown + dev::kNK * (dev::kNarrowSlots - long(plan.moduli.size())) >
+                dev::kNarrowTableWords - 1)  // one word may pad the block to an even length
+                continue;
+            used = grown;
+            plan.moduli[std::size_t(join)] *= q;
+            plan.slots[std::size_t(join)].push_back(q);
+        } else {
+            if (int(plan.moduli.size()) == dev::kNarrowSlots) continue;
+            const long long grown = used + words(q);
+            if (grown + dev::kNK * (dev::kNarrowSlots - long(plan.moduli.size()) - 1) >
+                dev::kNarrowTableWords - 1)
+                continue;
+            used = grown;
+            plan.moduli.push_back(q);
+            plan.slots.push_back({q});
+        }
+        plan.bits += sq.first;
+    }
+    return plan;
+}
+
 // Wide plan: moduli capped so that tables stay small against the curve's
 // work, and the staged rows fit the shared-memory budget.
 FastPlan wide_plan(const std::vector<std::string> &coefficients, long long bound, long double work,
@@ -1068,6 +1179,7 @@ struct BatchPlan {
     std::vector<dev::PatternSpec> pspecs;
     std::vector<dev::CompositeSpec> cspecs;
     std::vector<dev::BatchItem> wide_items, narrow_items;
+    std::vector<dev::ClassStart> class_starts;
     long long aff_words = 0, pattern_words = 0, row_words = 0;
     int wide_smem_words = 0;
 };
@@ -1102,7 +1214,7 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 cw.plan = wide_plan(c.coefficients, c.bound, (long double)cw.words * cw.count,
                                     cw.words >= dev::kWHugeWords ? 2 * dev::kWMaxSmemWords
                                                                  : dev::kWMaxSmemWords);
-            else cw.plan = choose_fast_plan(c.coefficients, c.bound, kBatchNarrowModulus, false);
+            else cw.plan = narrow_plan(c.coefficients);
             r.wide = cw.wide;
             r.class_prime = cw.plan.class_prime;
             r.moduli = cw.plan.moduli;
@@ -1231,6 +1343,20 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                         C.crt[a * 13 + rq] = (unsigned char)(((rq - a + q) % q) * C.inv64_q % q);
             }
             for (int r64 = 0; r64 < 64; ++r64) C.mod_q[r64] = (unsigned char)(q > 1 ? r64 % q : 0);
+            // class starts for every residue r mod M: ofs = (r + H) mod M, and per
+            // modulus the row index ((-H + ofs) S^-1) mod m of class word 0
+            C.cls = (long long)P.class_starts.size();
+            for (long long r = 0; r < M; ++r) {
+                dev::ClassStart cs{};
+                const long long ofs = (r + H % M) % M;
+                cs.ofs = (unsigned short)ofs;
+                for (int sl = 0; sl < dev::kWideSlots; ++sl) {
+                    const dev::Modulus &Md = C.mod[sl];
+                    const long long m = Md.m;
+                    cs.start[sl] = (unsigned short)((Md.neg_h + ofs) % m * Md.inv_stride % m);
+                }
+                P.class_starts.push_back(cs);
+            }
             for (int ci = 0; ci < kCandidatePrimes; ++ci) {
                 const int p = cands[ci];
                 C.neg_h[ci] = (unsigned short)((p - H % p) % p);
@@ -1244,6 +1370,32 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 for (long long f = c.first; f <= c.last; f += chunk)
                     P.wide_items.push_back({f, int(P.wide.size()), int(std::min(chunk, c.last - f + 1)),
                                             range, 0});
+            {
+                // class words swept: admissible classes of each d (by d mod 64 and
+                // d mod q), each of about 2H / (64 M) words
+                const long long per_class = (2 * H / M + 64) / 64;
+                long double classes = 0;
+                const long long qq = q > 1 ? q : 1;
+                const long long period = 64 * qq;
+                for (long long res = 0; res < period; ++res) {
+                    // parameters k in [first, last] with d(k) = res (mod 64 q)
+                    long long n = 0;
+                    if (!c.square) {
+                        const long long lo = c.first, hi = c.last;
+                        const long long base = (res - lo % period + period) % period + lo;
+                        n = base > hi ? 0 : (hi - base) / period + 1;
+                    } else {
+                        for (long long k = c.first; k <= std::min(c.last, c.first + period - 1); ++k)
+                            if ((k * k) % period == res) n += (c.last - k) / period + 1;
+                    }
+                    if (!n) continue;
+                    const int c2 = __builtin_popcountll(C.admissible[res & 63]);
+                    const int cq = q > 1 ? __builtin_popcountll(C.admissible[64 + res % q]) : 1;
+                    classes += (long double)n * c2 * cq;
+                }
+                stats.swept_words += (unsigned long long)(classes * per_class);
+                stats.smem_bytes += (unsigned long long)(classes * per_class) * 8ull * plan.moduli.size();
+            }
             P.wide.push_back(C);
             stats.wide_curves += 1;
         } else {
@@ -1257,15 +1409,16 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             C.tables = P.row_words;
             int used = 0;
             for (int sl = 0; sl < dev::kNarrowSlots; ++sl) {
-                const dev::CompositeSpec T = add_composite(sl, -1);
-                const int m = T.m;
+                const int m = sl < int(plan.moduli.size()) ? plan.moduli[sl] : 1;
+                const dev::CompositeSpec T = add_composite(sl, m + dev::kNK - 1);
                 C.m[sl] = m;
                 C.off[sl] = used;
-                used += m * m;
+                C.len[sl] = T.length;
+                used += m * T.length;
                 C.magic[sl] = host_magic(m);
                 const long long inv64 = m > 1 ? mod_inverse(64 % m, m) : 0;
                 C.shift[sl] = dev::u32(((m - H % m) % m) * inv64 % m);
-                C.step[sl] = dev::u32(32 % m);
+                C.step[sl] = dev::u32((dev::kWarpSize * dev::kNK) % m);
             }
             if (used % 2) {
                 P.row_words += 1;
@@ -1295,6 +1448,23 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 for (long long f = c.first; f <= c.last; f += chunk)
                     P.narrow_items.push_back({f, int(P.narrow.size()),
                                               int(std::min(chunk, c.last - f + 1)), range, 0});
+            {
+                long double live = 0;  // parameters whose d mod 64 admits a class
+                for (int res = 0; res < 64; ++res) {
+                    if (!C.dense2[res]) continue;
+                    long long n = 0;
+                    if (!c.square) {
+                        const long long base = (res - c.first % 64 + 64) % 64 + c.first;
+                        n = base > c.last ? 0 : (c.last - base) / 64 + 1;
+                    } else {
+                        for (long long k = c.first; k <= std::min(c.last, c.first + 63); ++k)
+                            if ((k * k) % 64 == res) n += (c.last - k) / 64 + 1;
+                    }
+                    live += n;
+                }
+                stats.swept_words += (unsigned long long)(live * cw.words);
+                stats.smem_bytes += (unsigned long long)(live * cw.words) * 8ull * plan.moduli.size();
+            }
             P.narrow.push_back(C);
         }
         stats.curves += 1;
@@ -1321,6 +1491,7 @@ struct BatchEngine::Impl {
     DeviceArray<dev::AffineSpec> d_aspecs;
     DeviceArray<dev::PatternSpec> d_pspecs;
     DeviceArray<dev::CompositeSpec> d_cspecs;
+    DeviceArray<dev::ClassStart> d_cls;
     DeviceArray<unsigned short> d_res, d_inv;
     DeviceArray<dev::u64> d_sq, d_aff, d_patterns, d_rows;
     DeviceArray<unsigned long long> d_counters;  // [0] survivors [1] wide work [2] narrow work [3] error
@@ -1410,14 +1581,14 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
         d_pspecs.upload(P.pspecs, stream, stats.h2d_bytes, "upload pattern specs");
         d_cspecs.upload(P.cspecs, stream, stats.h2d_bytes, "upload table specs");
         d_res.upload(P.residues, stream, stats.h2d_bytes, "upload residues");
+        d_cls.upload(P.class_starts, stream, stats.h2d_bytes, "upload class starts");
         d_aff.ensure(std::size_t(P.aff_words), "cudaMalloc(batch bitmasks)");
         d_patterns.ensure(std::size_t(P.pattern_words), "cudaMalloc(batch patterns)");
         d_rows.ensure(std::size_t(P.row_words), "cudaMalloc(batch tables)");
 
         const int wide_smem_words = P.wide_smem_words;
-        const std::size_t wide_smem = 2 * std::size_t(wide_smem_words) * 8 +
-                                      std::size_t(dev::kWWarps) * dev::kQueue * 12 +
-                                      std::size_t(dev::kMaxClasses) * dev::kWideSlots * 4;
+        const std::size_t wide_smem =
+            2 * std::size_t(wide_smem_words) * 8 + std::size_t(dev::kWWarps) * dev::kQueue * 12;
         const std::size_t narrow_smem = std::size_t(dev::kNarrowTableWords + dev::kAffWords) * 8 +
                                         std::size_t(dev::kNWarps) * dev::kQueue * 12;
         int wide_grid = 0, narrow_grid = 0;
@@ -1458,8 +1629,8 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
             record(ev[2], stream);
             if (wide_grid) {
                 dev::wide_kernel<<<wide_grid, dev::kWThreads, wide_smem, stream>>>(
-                    d_wide.p, d_witems.p, int(P.wide_items.size()), d_rows.p, d_aff.p, d_inv.p, cand,
-                    out, wide_smem_words, d_counters.p + 1);
+                    d_wide.p, d_witems.p, int(P.wide_items.size()), d_rows.p, d_aff.p, d_cls.p,
+                    d_inv.p, cand, out, wide_smem_words, d_counters.p + 1);
                 check_cuda(cudaGetLastError(), "wide_kernel launch");
             }
             record(ev[3], stream);

@@ -54,6 +54,8 @@ struct BatchStats {
     unsigned long long curves = 0, wide_curves = 0, denominators = 0, survivors = 0, points = 0;
     unsigned long long wide_items = 0, narrow_items = 0, launches = 0, words = 0;
     unsigned long long table_words = 0;
+    unsigned long long swept_words = 0;       // 64-site words the sieve kernels sweep (no intervals)
+    unsigned long long smem_bytes = 0;        // stage-1 shared-memory bytes those sweeps read
     long double rectangle_sites = 0;
     double plan_ms = 0, table_ms = 0, sieve_ms = 0, verify_ms = 0, wall_ms = 0;
     double wide_ms = 0, narrow_ms = 0;

@@ -382,6 +382,8 @@ rpg_status rpg_batch_search(const rpg_search_options *curves, int32_t curve_coun
             stats->launches = st.launches;
             stats->words = st.words;
             stats->table_words = st.table_words;
+            stats->swept_words = st.swept_words;
+            stats->smem_bytes = st.smem_bytes;
             stats->rectangle_sites = double(st.rectangle_sites);
             stats->plan_ms = st.plan_ms;
             stats->table_ms = st.table_ms;

@@ -77,7 +77,7 @@ class SearchOptions(ctypes.Structure):
 class BatchStats(ctypes.Structure):
     _fields_ = ([(name, ctypes.c_uint64) for name in
                  ("curves", "wide_curves", "denominators", "survivors", "points", "launches",
-                  "words", "table_words")] +
+                  "words", "table_words", "swept_words", "smem_bytes")] +
                 [(name, ctypes.c_double) for name in
                  ("rectangle_sites", "plan_ms", "table_ms", "sieve_ms", "wide_ms", "narrow_ms",
                   "verify_ms", "wall_ms")] +
