@@ -1095,8 +1095,26 @@ struct CurveWork {
     std::unique_ptr<ExactPolynomial> poly;
     FastPlan plan;
     long long words = 0;       // dense 64-site words per row
+    long long swept = 0;       // words a denominator sweeps after interval narrowing (estimate)
     long long count = 0;       // parameters
 };
+
+// Words of one denominator's row that the sieve sweeps: the whole row, or with
+// x intervals the interval numerators at a middle denominator (each interval
+// [lo, hi] covers about (hi - lo) d / 64 words).  Picks the kernel shape.
+long long swept_row_words(const BatchCurveSpec &c, long long words) {
+    if (c.intervals.empty() || c.intervals.size() > std::size_t(dev::kMaxIntervals)) return words;
+    const double dmid = 0.5 * double(c.first) + 0.5 * double(std::max(c.first, c.last));
+    const double d = c.square ? dmid * dmid : dmid;
+    double total = 0;
+    for (const auto &iv : c.intervals) {
+        if (iv.lower_infinite || iv.upper_infinite) return words;
+        const double len = approx_value(iv.upper) - approx_value(iv.lower);
+        if (len < 0) continue;
+        total += std::min(double(words), len * d / 64.0 + 2.0);
+    }
+    return std::min(words, (long long)std::ceil(total));
+}
 
 // Narrow plan: every odd prime up to kBatchNarrowModulus that filters at
 // least 0.15 bit, strongest first, each joining the slot whose product stays
@@ -1209,7 +1227,8 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             }
             cw.words = word_count64(c.bound);
             cw.count = c.last >= c.first ? c.last - c.first + 1 : 0;
-            cw.wide = cw.words >= kBatchWideWords;
+            cw.swept = swept_row_words(c, cw.words);
+            cw.wide = cw.swept >= kBatchWideWords;
             if (cw.wide)
                 cw.plan = wide_plan(c.coefficients, c.bound, (long double)cw.words * cw.count,
                                     cw.words >= dev::kWHugeWords ? 2 * dev::kWMaxSmemWords
@@ -1441,9 +1460,9 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 C.neg_h[ci] = (unsigned short)((p - H % p) % p);
             }
             device_intervals(c.intervals, C.nint, C.lo, C.hi);
-            // items of about 2^16 words, at least one denominator per warp
-            const long long chunk =
-                std::max<long long>(dev::kNWarps, std::min<long long>(1 << 14, (1LL << 16) / cw.words));
+            // items of about 2^16 swept words, at least one denominator per warp
+            const long long chunk = std::max<long long>(
+                dev::kNWarps, std::min<long long>(1 << 14, (1LL << 16) / std::max(1LL, cw.swept)));
             for (int range = 0; range < std::max(1, C.nint); ++range)
                 for (long long f = c.first; f <= c.last; f += chunk)
                     P.narrow_items.push_back({f, int(P.narrow.size()),

@@ -194,6 +194,11 @@ def test_interval_narrowing_matches_single_search(rpg, golden):
                                      ("-1e-400", "0")]})
         curves.append({"coefficients": dense, "bound": bound, "first": 1, "last": last,
                        "intervals": [(str(-i - 0.5), str(-i)) for i in range(10)]})
+    # narrowed rows still long enough for the class-layout kernel
+    for c in mixed_curves(rng, 4, (300000, 500000), (20, 60), bits=10):
+        lo = rng.uniform(-9000, -5000)
+        c["intervals"] = [(f"{lo:.2f}", f"{lo + 4000:.2f}"), ("15.5", f"{rng.uniform(6000, 9000):.3f}")]
+        curves.append(c)
     for _ in range(24):
         c = mixed_curves(rng, 1, (200, 120000), (1, 300), bits=10)[0]
         ivs = []
@@ -205,7 +210,7 @@ def test_interval_narrowing_matches_single_search(rpg, golden):
     curves = squarefree(rpg, curves)
     points, status, survivors, stats = rpg.batch_search(curves)
     assert all(s == 0 for s in status)
-    assert stats["wide_curves"] >= 4
+    assert stats["wide_curves"] >= 5 and stats["curves"] - stats["wide_curves"] >= 20
     for c, got in zip(curves, points):
         assert got == single(rpg, c), c
     full, _, full_survivors, _ = rpg.batch_search([dict(c, intervals=()) for c in curves[:2]])
