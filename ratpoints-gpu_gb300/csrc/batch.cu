@@ -403,28 +403,6 @@ __device__ __forceinline__ void wide_drain(const u64 *qmask, const u32 *qinfo, i
     emit(m, -C.bound + ofs + C.stride * off, C.class_mod, d, C.index, out);
 }
 
-// Position of the n-th set bit (n counted from 0) of a 64-bit mask that has
-// more than n set bits, by halving with population counts.
-__device__ __forceinline__ int nth_bit64(u64 mask, int n) {
-    int pos = 0;
-    int c = __popc(u32(mask));
-    if (n >= c) {
-        n -= c;
-        mask >>= 32;
-        pos = 32;
-    }
-    u32 m = u32(mask);
-    c = __popc(m & 0xFFFFu);
-    if (n >= c) { n -= c; m >>= 16; pos += 16; }
-    c = __popc(m & 0xFFu);
-    if (n >= c) { n -= c; m >>= 8; pos += 8; }
-    c = __popc(m & 0xFu);
-    if (n >= c) { n -= c; m >>= 4; pos += 4; }
-    c = __popc(m & 0x3u);
-    if (n >= c) { n -= c; m >>= 2; pos += 2; }
-    if (n >= int(m & 1u)) pos += 1;
-    return pos;
-}
 
 // Wide rows, one CTA per denominator, software-pipelined over the
 // denominators of an item: while every warp sweeps denominator d_i (rows in

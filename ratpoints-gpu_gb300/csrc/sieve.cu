@@ -250,6 +250,7 @@ struct Sieve::Impl {
     dev::FastTables F{};
     dev::u64 *fast_rows = nullptr;
     dev::u64 *fast_adm = nullptr;
+    dev::FastClassStart *fast_starts = nullptr;
     std::size_t fast_smem = 0;
     std::vector<dev::u64> fast_adm_host;
     FastPlan fast_plan;
@@ -300,6 +301,8 @@ struct Sieve::Impl {
         fast_rows = nullptr;
         cudaFree(fast_adm);
         fast_adm = nullptr;
+        cudaFree(fast_starts);
+        fast_starts = nullptr;
         if (h_count) cudaFreeHost(h_count);
         if (h_a) cudaFreeHost(h_a);
         if (h_d) cudaFreeHost(h_d);
@@ -422,7 +425,15 @@ struct Sieve::Impl {
     // admissible-class tables (2-adic by d mod 64, residues mod q by d mod q).
     void build_fast_tables(const std::vector<std::string> &coefficients) {
         auto t0 = Clock::now();
+        // the two staged row sets of a CTA must fit shared memory at 2 CTAs/SM
         fast_plan = choose_fast_plan(coefficients, bound);
+        for (int cap = kMaxModulus;;) {
+            int row_words = 0;
+            for (int m : fast_plan.moduli) row_words += (m + dev::kFExt + 1) & ~1;
+            if (row_words <= dev::kFRowBudget || cap <= 64) break;
+            cap = cap * 7 / 8;
+            fast_plan = choose_fast_plan(coefficients, bound, cap);
+        }
         const int n = int(coefficients.size()) - 1;
         const int q = fast_plan.class_prime;
         const long long M = 64LL * q;
@@ -547,10 +558,23 @@ struct Sieve::Impl {
             }
         }
         fast_adm_host = adm;
+        // class starts for every residue r mod M: ofs = (r + H) mod M and, per
+        // modulus, the row index ((-H + ofs) S^-1) mod m of class word 0
+        std::vector<dev::FastClassStart> starts(static_cast<std::size_t>(M));
+        for (long long r = 0; r < M; ++r) {
+            dev::FastClassStart &cs = starts[std::size_t(r)];
+            const long long ofs = (r + bound % M) % M;
+            cs.ofs = (unsigned short)ofs;
+            for (int sl = 0; sl < F.slots; ++sl) {
+                const dev::FastModulus &Md = F.mod[sl];
+                cs.start[sl] = (unsigned short)((Md.neg_h + ofs) % Md.m * Md.inv_stride % Md.m);
+            }
+        }
         timings.plan_ms += ms_since(t0);
         auto t1 = Clock::now();
         fast_rows = device_alloc<dev::u64>(std::size_t(total), "cudaMalloc(class tables)");
         fast_adm = device_alloc<dev::u64>(adm.size(), "cudaMalloc(admissible classes)");
+        fast_starts = device_alloc<dev::FastClassStart>(starts.size(), "cudaMalloc(class starts)");
         unsigned char *d_aff = device_alloc<unsigned char>(affine.size(), "cudaMalloc(affine)");
         unsigned short *d_inv = device_alloc<unsigned short>(inverse.size(), "cudaMalloc(inverse)");
         dev::TableSpec *d_specs = device_alloc<dev::TableSpec>(specs.size(), "cudaMalloc(specs)");
@@ -570,8 +594,12 @@ struct Sieve::Impl {
         check_cuda(cudaMemcpyAsync(fast_adm, adm.data(), adm.size() * sizeof(dev::u64),
                                    cudaMemcpyHostToDevice, stream),
                    "upload admissible classes");
+        check_cuda(cudaMemcpyAsync(fast_starts, starts.data(), starts.size() * sizeof(dev::FastClassStart),
+                                   cudaMemcpyHostToDevice, stream),
+                   "upload class starts");
         timings.h2d_bytes += affine.size() + inverse.size() * sizeof(unsigned short) +
-                             specs.size() * sizeof(dev::TableSpec) + adm.size() * sizeof(dev::u64);
+                             specs.size() * sizeof(dev::TableSpec) + adm.size() * sizeof(dev::u64) +
+                             starts.size() * sizeof(dev::FastClassStart);
         const int threads = 256;
         const long long blocks = (total + threads - 1) / threads;
         dev::class_table_kernel<<<unsigned(blocks), threads, 0, stream>>>(
@@ -590,8 +618,9 @@ struct Sieve::Impl {
         F.rows = fast_rows;
         F.prime_rows = fast_rows;
         F.admissible = fast_adm;
-        fast_smem = std::size_t(F.smem_words) * 8 + std::size_t(dev::kFWarps) * dev::kFQueue * 12 +
-                    std::size_t(dev::kFMaxClasses) * F.slots * 4;
+        F.class_starts = fast_starts;
+        fast_smem = std::size_t(dev::kFSlotCount) * std::size_t(F.smem_words) * 8 +
+                    std::size_t(dev::kFConsumers) * dev::kFQueue * 12;
         const void *kernel = fast_kernel_ptr(F.slots);
         check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(fast_smem)),
@@ -623,7 +652,7 @@ struct Sieve::Impl {
 
     void launch_fast(const dev::FastTables &Fl, const dev::SieveArgs &A, unsigned long long *work,
                      cudaStream_t st) const {
-        const int blocks = int(std::min<long long>(grid, (A.k_count + dev::kFFetch - 1) / dev::kFFetch));
+        const int blocks = int(std::min<long long>(grid, (A.k_count + dev::kFChunk - 1) / dev::kFChunk));
         switch (Fl.slots) {
         case 1: dev::fast_sieve_kernel<1><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
         case 2: dev::fast_sieve_kernel<2><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;

@@ -35,8 +35,9 @@ struct SieveArgs {
     unsigned long long *error;   // set nonzero if a bounded device wait ran out (may be null)
 };
 
-// Largest 32-bit quotient estimate used for n mod p with n < 2^31 and p < 2^9:
-// q = (n * ceil(2^40 / p)) >> 40 is exact in that range.
+// Quotient estimate for n mod p with n < 2^31 and 257 <= p < 2^9 (the
+// reference's candidate primes): q = (n * ceil(2^40 / p)) >> 40 is exact in
+// that range.  Below 257, ceil(2^40 / p) does not fit 32 bits: use mod_u32.
 __host__ __device__ inline u32 magic40(u32 p) {
     return u32(((u64(1) << 40) + p - 1) / p);
 }
@@ -87,6 +88,29 @@ __device__ __forceinline__ void bulk_copy_to_shared(u32 dst, const void *src, u3
 }
 __device__ __forceinline__ void fence_proxy_async_shared() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Position of the n-th set bit (n counted from 0) of a 64-bit mask that has
+// more than n set bits, by halving with population counts.
+__device__ __forceinline__ int nth_bit64(u64 mask, int n) {
+    int pos = 0;
+    int c = __popc(u32(mask));
+    if (n >= c) {
+        n -= c;
+        mask >>= 32;
+        pos = 32;
+    }
+    u32 m = u32(mask);
+    c = __popc(m & 0xFFFFu);
+    if (n >= c) { n -= c; m >>= 16; pos += 16; }
+    c = __popc(m & 0xFFu);
+    if (n >= c) { n -= c; m >>= 8; pos += 8; }
+    c = __popc(m & 0xFu);
+    if (n >= c) { n -= c; m >>= 4; pos += 4; }
+    c = __popc(m & 0x3u);
+    if (n >= c) { n -= c; m >>= 2; pos += 2; }
+    if (n >= int(m & 1u)) pos += 1;
+    return pos;
 }
 
 __device__ __forceinline__ u32 lanemask_lt() {

@@ -19,6 +19,12 @@
 // primes (same selection as the reference plan) from class-layout tables in
 // global memory, then emits (a, d).  Survivors are a subset of the reference
 // plan's.
+//
+// Warp-specialized pipeline: warp 0 produces denominators (prime selection,
+// class layout from the per-curve class-start table, TMA copies of the rows)
+// into one of two slots; the other warps consume a slot's sweep items once
+// its full barrier completes and release it through its empty barrier, so a
+// slot is refilled while the other is swept and no barrier spans the CTA.
 #pragma once
 
 #include "plan.hpp"
@@ -30,8 +36,12 @@ namespace dev {
 constexpr int kFastSlots = kMaxFastSlots;  // stage-1 moduli (at most)
 constexpr int kFastMaxFactors = 4;         // primes per stage-1 modulus
 constexpr int kFK = 4;                     // words per lane per step (lanes 32 apart)
-constexpr int kFWarps = 8;
+constexpr int kFWarps = 12;                // warp 0 produces, the others sweep
 constexpr int kFThreads = kFWarps * kWarpSize;
+constexpr int kFConsumers = kFWarps - 1;
+constexpr int kFSlotCount = 2;                             // denominators in flight per CTA
+constexpr int kFChunk = 32;                                // parameters per producer fetch
+constexpr int kFRowBudget = 5840;                          // staged row words per slot (2 CTAs/SM)
 constexpr int kFSteps = 4;                                 // steps per work item
 constexpr int kFItemWords = kWarpSize * kFK * kFSteps;     // 512 words per item
 constexpr int kFExt = kWarpSize * (kFK - 1);               // row extension
@@ -39,8 +49,8 @@ constexpr int kFQueue = 64;
 constexpr int kFClassBits = 8;                             // up to 256 classes
 constexpr int kFMaxClasses = kMaxFastClasses;
 constexpr long long kFMaxClassWords = 1LL << 23;           // word offset fits 24 bits
-constexpr int kFFetch = 4;                                 // denominators per fetch
 constexpr int kFAdmQ = 16;                                 // admissible-residue words for q <= 13
+constexpr int kFStage2Group = 8;                           // stage-2 primes loaded together
 
 static_assert(kFMaxClasses <= (1 << kFClassBits), "class index must fit the queue entry");
 
@@ -67,7 +77,17 @@ struct FastPrime {                 // one of the 36 reference candidates, class 
     u32 wlo_mod;                   // first word of the launch's tile, mod p
 };
 
+// Per class residue r mod M: the row index of class word 0 for each modulus,
+// (a0 S^-1) mod m with a0 = -H + ofs, and ofs = (r + H) mod M.
+struct FastClassStart {
+    unsigned short start[kFastSlots];
+    unsigned short ofs;
+    unsigned short pad;
+};
+static_assert(sizeof(FastClassStart) == 16, "one 16-byte load per class");
+
 struct FastTables {
+    const FastClassStart *class_starts;  // [M]
     const u64 *rows;               // stage-1 modulus tables
     const u64 *prime_rows;         // reference candidate tables (class layout)
     const u64 *admissible;         // [64] 2-adic classes by d mod 64, then [kFAdmQ] residues by d mod q
@@ -142,11 +162,35 @@ __global__ void class_table_kernel(u64 *rows, const TableSpec *specs, int nspecs
     rows[id] = word;
 }
 
+// One admissible class of the slot's denominator: its words inside the
+// launch's tile, where its last word is (or -1), and that word's valid bits.
+struct FastRun {
+    int words;
+    int last_word;
+    unsigned short ofs;            // (r + H) mod M
+    unsigned short r;              // class residue mod M
+    int last_bits;
+};
+
+// A denominator in flight: written by the producer warp, read by the others.
+struct FastSlot {
+    long long d;                   // denominator; -1: no more work
+    int nclass;
+    int next;                      // sweep-item counter
+    int sel[kSelectedPrimes];      // selected candidates, largest first
+    long long prow[kSelectedPrimes];  // class-layout row of each for d mod p
+    int prefix[kFMaxClasses + 1];  // first sweep item of each class
+    FastRun run[kFMaxClasses];
+};
+
+__device__ __forceinline__ void mbar_arrive(u32 bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 // Stage 2 for up to 32 queued class words (one per lane), then emission.
 __device__ __forceinline__ void fast_drain(const u64 *qmask, const u32 *qinfo, int start, int n,
                                            const FastTables &T, const SieveArgs &A,
-                                           int denominator, const int *s_sel,
-                                           const long long *s_prow, const u32 *s_ofs) {
+                                           const FastSlot &S) {
     const int lane = threadIdx.x & 31;
     u64 m = 0;
     u32 info = 0;
@@ -157,22 +201,30 @@ __device__ __forceinline__ void fast_drain(const u64 *qmask, const u32 *qinfo, i
     __syncwarp();
     const u32 off = info >> kFClassBits;
     const int c = int(info & ((1u << kFClassBits) - 1));
-    const u32 ofs = s_ofs[c];                          // (r + H) mod M
+    const u32 ofs = S.run[c].ofs;                      // (r + H) mod M
     const long long a0 = -A.bound + ofs;               // least a >= -H in the class
     const long long w = A.w_lo + off;
     if (m) {
-        for (int s = 0; s < kSelectedPrimes; ++s) {
-            const FastPrime &P = T.prime[s_sel[s]];
-            const u32 p = u32(P.p);
-            u32 a0m = P.neg_h + mod_small(ofs, p, P.magic);
-            if (a0m >= p) a0m -= p;
-            u32 u = mod_small(a0m * P.inv_stride, p, P.magic);
-            u += P.wlo_mod;
-            if (u >= p) u -= p;
-            u += mod_small(off, p, P.magic);
-            if (u >= p) u -= p;
-            m &= __ldg(T.prime_rows + s_prow[s] + u);
-            if (!m) break;
+        // the table words of kFStage2Group primes are loaded together, so a
+        // word pays one L2 round trip per group instead of one per prime
+        for (int s0 = 0; s0 < kSelectedPrimes && m; s0 += kFStage2Group) {
+            u64 rows[kFStage2Group];
+#pragma unroll
+            for (int t = 0; t < kFStage2Group; ++t) {
+                const int s = s0 + t;
+                const FastPrime &P = T.prime[S.sel[s]];
+                const u32 p = u32(P.p);
+                u32 a0m = P.neg_h + mod_small(ofs, p, P.magic);
+                if (a0m >= p) a0m -= p;
+                u32 u = mod_small(a0m * P.inv_stride, p, P.magic);
+                u += P.wlo_mod;
+                if (u >= p) u -= p;
+                u += mod_small(off, p, P.magic);
+                if (u >= p) u -= p;
+                rows[t] = __ldg(T.prime_rows + S.prow[s] + u);
+            }
+#pragma unroll
+            for (int t = 0; t < kFStage2Group; ++t) m &= rows[t];
         }
     }
     // emission: a = a0 + S w + M j
@@ -195,255 +247,296 @@ __device__ __forceinline__ void fast_drain(const u64 *qmask, const u32 *qinfo, i
         m &= m - 1;
         if (pos < A.capacity) {
             A.out_a[pos] = abase + (long long)T.class_mod * bit;
-            A.out_d[pos] = denominator;
+            A.out_d[pos] = int(S.d);
         }
         ++pos;
     }
 }
 
+// Producer work for denominator d into slot S (the whole warp): the 32
+// largest candidates not dividing d (two ballots), then the admissible
+// classes and their sweep items (a prefix scan, 32 classes per pass).
+__device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs &A, long long d,
+                                           FastSlot &S) {
+    const int lane = threadIdx.x & 31;
+    const u32 du = u32(d);
+    const int q = T.class_prime;
+    const int M = T.class_mod;
+    {
+        // lane l tests candidate 35 - l, lanes 0..3 also candidate 3 - l
+        const int ch = kCandidatePrimes - 1 - lane;
+        const u32 rh = mod_small(du, u32(T.prime[ch].p), T.prime[ch].magic);
+        const u32 hi_div = __ballot_sync(kFullMask, rh == 0);
+        const int cl = kCandidatePrimes - 1 - 32 - lane;
+        const u32 rl =
+            lane < kCandidatePrimes - 32 ? mod_small(du, u32(T.prime[cl].p), T.prime[cl].magic) : 1u;
+        const u32 lo_div = __ballot_sync(kFullMask, rl == 0);
+        const u32 below = lanemask_lt();
+        const int rank_h = lane - __popc(hi_div & below);
+        if (rh != 0 && rank_h < kSelectedPrimes) {
+            S.sel[rank_h] = ch;
+            S.prow[rank_h] = T.prime[ch].offset + (long long)rh * T.prime[ch].p;
+        }
+        const int rank_l = 32 - __popc(hi_div) + lane - __popc(lo_div & below);
+        if (lane < kCandidatePrimes - 32 && rl != 0 && rank_l < kSelectedPrimes) {
+            S.sel[rank_l] = cl;
+            S.prow[rank_l] = T.prime[cl].offset + (long long)rl * T.prime[cl].p;
+        }
+    }
+    const u64 classes2 = __ldg(T.admissible + (du & 63));
+    const u64 classesq =
+        q > 1 ? __ldg(T.admissible + 64 + int(mod_u32(du, u32(q), (~0ull) / u32(q) + 1))) : u64(1);
+    const int nq = __popcll(classesq);
+    const int nclass = __popcll(classes2) * nq;
+    int carry = 0;
+    for (int base = 0; base < nclass; base += 32) {
+        const int c = base + lane;
+        int items = 0;
+        if (c < nclass) {
+            const int i2 = nq == 1 ? c : c / nq;
+            const int r64 = nth_bit64(classes2, i2);
+            int r = r64;
+            if (q > 1) {
+                const int rq = nth_bit64(classesq, c - i2 * nq);
+                r = r64 + 64 * int(T.crt[T.mod_q[r64] * 13 + rq]);
+            }
+            const int ofs = T.class_starts[r].ofs;
+            // sites of class r: a = -H + ofs + M t, t in [0, count)
+            const long long count = T.count_q + (ofs <= T.count_r ? 1 : 0);
+            const long long words = (count + 63) >> 6;
+            const long long lo = A.w_lo < words ? A.w_lo : words;
+            const long long hi = A.w_hi < words ? A.w_hi : words;
+            FastRun run;
+            run.words = int(hi - lo);
+            const bool has_last = hi == words && words > 0 && hi > lo;
+            run.last_word = has_last ? int(words - 1 - lo) : -1;
+            run.last_bits = has_last ? int(count - 64 * (words - 1)) : 64;
+            run.ofs = (unsigned short)ofs;
+            run.r = (unsigned short)r;
+            S.run[c] = run;
+            items = (run.words + kFItemWords - 1) / kFItemWords;
+        }
+        int incl = items;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(kFullMask, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (c < nclass) S.prefix[c] = carry + incl - items;
+        carry += __shfl_sync(kFullMask, incl, 31);
+    }
+    if (lane == 0) {
+        S.prefix[nclass] = carry;
+        S.nclass = nclass;
+        S.next = 0;
+        S.d = d;
+    }
+    (void)M;
+}
+
 template <int NS>
-__global__ void __launch_bounds__(kFThreads, 3) fast_sieve_kernel(FastTables T, SieveArgs A,
+__global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, SieveArgs A,
                                                                unsigned long long *work) {
     extern __shared__ __align__(16) u64 smem[];
-    u64 *rows = smem;
-    u64 *qmask = rows + T.smem_words;
-    u32 *qinfo = reinterpret_cast<u32 *>(qmask + kFWarps * kFQueue);
-    u32 *s_start = qinfo + kFWarps * kFQueue;                 // [kFMaxClasses][NS]
+    const int row_stride = T.smem_words;  // even: buffers stay 16-byte aligned
+    u64 *qmask = smem + kFSlotCount * row_stride;
+    u32 *qinfo = reinterpret_cast<u32 *>(qmask + kFConsumers * kFQueue);
 
-    __shared__ long long s_items[kFFetch];
-    __shared__ int s_nitems;
-    __shared__ u32 s_ofs[kFMaxClasses];      // (r + H) mod M of class c
-    __shared__ int s_wtile[kFMaxClasses];    // words of the class inside this launch's tile
-    __shared__ int s_last_word[kFMaxClasses];
-    __shared__ int s_last_bits[kFMaxClasses];
-    __shared__ int s_prefix[kFMaxClasses + 1];
-    __shared__ int s_sel[kSelectedPrimes];
-    __shared__ long long s_prow[kSelectedPrimes];
-    __shared__ int s_next;
-    __shared__ int s_abort;
-    __shared__ __align__(8) unsigned long long s_bar;   // row-copy completion
+    __shared__ FastSlot slot[kFSlotCount];
+    __shared__ __align__(8) unsigned long long s_full[kFSlotCount];
+    __shared__ __align__(8) unsigned long long s_empty[kFSlotCount];
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    u64 *wq_mask = qmask + warp * kFQueue;
-    u32 *wq_info = qinfo + warp * kFQueue;
-    const long long sites_total = 2 * A.bound + 1;
-    const int q = T.class_prime;
-    const int M = T.class_mod;
-    const unsigned char *sbase = reinterpret_cast<const unsigned char *>(rows);
-    const u32 rows_addr = smem_addr(rows);
-    const u32 bar = smem_addr(&s_bar);
-    u32 phase = 0;
     if (threadIdx.x == 0) {
-        mbar_init(bar, 1);
-        s_abort = 0;
+        for (int b = 0; b < kFSlotCount; ++b) {
+            mbar_init(smem_addr(&s_full[b]), 1);
+            mbar_init(smem_addr(&s_empty[b]), kFConsumers);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 
-    for (;;) {
-        if (threadIdx.x == 0) {
-            const unsigned long long base = atomicAdd(work, (unsigned long long)kFFetch);
-            int n = 0;
-            for (int i = 0; i < kFFetch; ++i)
-                if (base + i < (unsigned long long)A.k_count) s_items[n++] = (long long)base + i;
-            s_nitems = n;
-        }
-        __syncthreads();
-        const int nitems = s_nitems;
-        if (nitems == 0) break;
-        for (int it = 0; it < nitems; ++it) {
-            const long long k = A.k_first + s_items[it];
-            const long long d = A.square ? k * k : k;
-            const u32 du = u32(d);  // d < 2^31 (k <= INT_MAX, or k <= 46340 when square)
-            const u64 classes2 = __ldg(T.admissible + (du & 63));
-            const u64 classesq = q > 1 ? __ldg(T.admissible + 64 + int(du % u32(q))) : u64(1);
-            if (!classes2 || !classesq) continue;
-            const int nq = __popcll(classesq);
-            const int nclass = __popcll(classes2) * nq;
-
-            // ---- per-denominator setup ----
-            // Thread 0 starts the bulk copies of this denominator's stage-1 rows
-            // (all rows are contiguous in shared memory: one transaction count).
-            if (threadIdx.x == 0) {
+    if (warp == 0) {
+        // ---- producer: next live denominator into the next free slot ----
+        const int q = T.class_prime;
+        const unsigned long long magic_q = (~0ull) / u32(q) + 1;  // q >= 1: mod_u32 constant
+        long long chunk = 0;
+        int j = kFChunk;                 // position inside the fetched chunk
+        int uses0 = 0, uses1 = 0;        // fills of each slot so far
+        int b = 0;
+        bool failed = false;
+        for (;;) {
+            long long d = -1;
+            for (;;) {
+                if (j == kFChunk) {
+                    unsigned long long base = 0;
+                    if (lane == 0) base = atomicAdd(work, (unsigned long long)kFChunk);
+                    chunk = (long long)__shfl_sync(kFullMask, base, 0);
+                    j = 0;
+                    if (chunk >= A.k_count) break;
+                }
+                const long long idx = chunk + j++;
+                if (idx >= A.k_count) {
+                    j = kFChunk;
+                    continue;
+                }
+                const long long k = A.k_first + idx;
+                const long long dd = A.square ? k * k : k;
+                const u32 du = u32(dd);
+                if (__ldg(T.admissible + (du & 63)) == 0) continue;
+                if (q > 1 && __ldg(T.admissible + 64 + int(mod_u32(du, u32(q), magic_q))) == 0)
+                    continue;
+                d = dd;
+                break;
+            }
+            // slot b must be released by every consumer before it is refilled
+            const int used = b ? uses1 : uses0;
+            if (used > 0 && !mbar_wait(smem_addr(&s_empty[b]), u32(used - 1) & 1u)) {
+                failed = true;
+                break;
+            }
+            FastSlot &S = slot[b];
+            const u32 full = smem_addr(&s_full[b]);
+            if (d < 0) {
+                if (lane == 0) S.d = -1;
+                __syncwarp();
+                if (lane == 0) {
+                    __threadfence_block();
+                    mbar_arrive(full);
+                }
+                break;
+            }
+            fast_setup(T, A, d, S);
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence_block();
                 fence_proxy_async_shared();
-                mbar_arrive_expect_tx(bar, u32(T.smem_words) * 8u);
+                mbar_arrive_expect_tx(full, u32(T.smem_words) * 8u);
+                const u32 du = u32(d);
+                const u32 dst = smem_addr(smem + b * row_stride);
 #pragma unroll
                 for (int sl = 0; sl < NS; ++sl) {
                     const FastModulus &Md = T.mod[sl];
                     const u32 rho = mod_u32(du, u32(Md.m), Md.magic);
-                    bulk_copy_to_shared(rows_addr + u32(Md.smem_offset) * 8u,
+                    bulk_copy_to_shared(dst + u32(Md.smem_offset) * 8u,
                                         T.rows + Md.offset + (long long)rho * Md.length,
-                                        u32(Md.length) * 8u, bar);
+                                        u32(Md.length) * 8u, full);
                 }
             }
-            if (warp == 0) {
-                // The 32 largest candidates not dividing d: lane l tests
-                // candidate 35 - l, lanes 0..3 also candidate 3 - l.
-                const int ch = kCandidatePrimes - 1 - lane;
-                const u32 rh = du % u32(T.prime[ch].p);
-                const u32 hi_div = __ballot_sync(kFullMask, rh == 0);
-                const int cl = kCandidatePrimes - 1 - 32 - lane;
-                const u32 rl = lane < kCandidatePrimes - 32 ? du % u32(T.prime[cl].p) : 1u;
-                const u32 lo_div = __ballot_sync(kFullMask, rl == 0);
-                const u32 below = lanemask_lt();
-                const int rank_h = lane - __popc(hi_div & below);
-                if (rh != 0 && rank_h < kSelectedPrimes) {
-                    s_sel[rank_h] = ch;
-                    s_prow[rank_h] = T.prime[ch].offset + (long long)rh * T.prime[ch].p;
-                }
-                const int rank_l = 32 - __popc(hi_div) + lane - __popc(lo_div & below);
-                if (lane < kCandidatePrimes - 32 && rl != 0 && rank_l < kSelectedPrimes) {
-                    s_sel[rank_l] = cl;
-                    s_prow[rank_l] = T.prime[cl].offset + (long long)rl * T.prime[cl].p;
-                }
-                if (lane == 0) s_next = 0;
-            } else if (warp == 1) {
-                // Classes, 32 per pass: class c = (c / nq)-th 2-adic class crossed
-                // with the (c % nq)-th admissible residue mod q; item prefix by scan.
-                int carry = 0;
-                for (int base = 0; base < nclass; base += 32) {
-                    const int c = base + lane;
-                    int items = 0;
-                    if (c < nclass) {
-                        const int r64 = nth_set_bit(classes2, c / nq);
-                        int r = r64;
-                        if (q > 1) {
-                            const int rq = nth_set_bit(classesq, c % nq);
-                            r = r64 + 64 * int(T.crt[T.mod_q[r64] * 13 + rq]);
-                        }
-                        int ofs = r + T.h_mod_m;
-                        if (ofs >= M) ofs -= M;
-                        // sites of class r: a = -H + ofs + M t, t in [0, count)
-                        const long long count = T.count_q + (ofs <= T.count_r ? 1 : 0);
-                        const long long words = (count + 63) >> 6;
-                        const long long lo = A.w_lo < words ? A.w_lo : words;
-                        const long long hi = A.w_hi < words ? A.w_hi : words;
-                        const int wt = int(hi - lo);
-                        s_ofs[c] = u32(ofs);
-                        s_wtile[c] = wt;
-                        const bool has_last = hi == words && words > 0 && hi > lo;
-                        s_last_word[c] = has_last ? int(words - 1 - lo) : -1;
-                        s_last_bits[c] = has_last ? int(count - 64 * (words - 1)) : 64;
-#pragma unroll
-                        for (int sl = 0; sl < NS; ++sl) {
-                            // row index of tile word 0: (a0 * S^-1 + w_lo) mod m, a0 = -H + ofs
-                            const FastModulus &Md = T.mod[sl];
-                            const u32 a0m = mod_u32(Md.neg_h + u32(ofs), u32(Md.m), Md.magic);
-                            s_start[c * NS + sl] =
-                                mod_u32(a0m * Md.inv_stride + Md.wlo_mod, u32(Md.m), Md.magic);
-                        }
-                        items = (wt + kFItemWords - 1) / kFItemWords;
-                    }
-                    int incl = items;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int v = __shfl_up_sync(kFullMask, incl, o);
-                        if (lane >= o) incl += v;
-                    }
-                    if (c < nclass) s_prefix[c] = carry + incl - items;
-                    carry += __shfl_sync(kFullMask, incl, 31);
-                }
-                if (lane == 0) s_prefix[nclass] = carry;
-            }
-            __syncthreads();
-            if (!mbar_wait(bar, phase)) {  // rows landed (bounded wait)
-                s_abort = 1;
-                if (A.error) atomicOr(A.error, 1ull);
-            }
-            phase ^= 1u;
+            if (b) ++uses1;
+            else ++uses0;
+            b ^= 1;
+        }
+        if (failed) {
+            if (A.error && lane == 0) atomicOr(A.error, 1ull);
+            // let the copies already issued land (bounded) before leaving
+            if (lane == 0 && uses0 > 0) mbar_wait(smem_addr(&s_full[0]), u32(uses0 - 1) & 1u);
+            if (lane == 0 && uses1 > 0) mbar_wait(smem_addr(&s_full[1]), u32(uses1 - 1) & 1u);
+        }
+        return;
+    }
 
-            // ---- sweep: warps take work items (class, 512-word chunk) ----
-            const int total_items = s_prefix[nclass];
-            int qn = 0;
-            u32 step8[NS], mod8[NS];
-            const unsigned char *slot_base[NS];
+    // ---- consumers: sweep the items of each filled slot in turn ----
+    const int cw = warp - 1;
+    u64 *wq_mask = qmask + cw * kFQueue;
+    u32 *wq_info = qinfo + cw * kFQueue;
+    u32 phase = 0;  // bit b: parity of slot b's next fill
+    int b = 0;
+    for (;;) {
+        if (!mbar_wait(smem_addr(&s_full[b]), (phase >> b) & 1u)) {  // bounded wait
+            if (A.error && lane == 0) atomicOr(A.error, 1ull);
+            return;
+        }
+        phase ^= 1u << b;
+        const FastSlot &S = slot[b];
+        if (S.d < 0) return;  // the producer has no more work
+        const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
+        const int nclass = S.nclass;
+        const int total_items = S.prefix[nclass];
+        int qn = 0;
+        u32 step8[NS], mod8[NS];
+        const unsigned char *slot_base[NS];
 #pragma unroll
-            for (int sl = 0; sl < NS; ++sl) {
-                step8[sl] = 8u * T.mod[sl].step;
-                mod8[sl] = 8u * u32(T.mod[sl].m);
-                slot_base[sl] = sbase + 8 * T.mod[sl].smem_offset;
+        for (int sl = 0; sl < NS; ++sl) {
+            step8[sl] = 8u * T.mod[sl].step;
+            mod8[sl] = 8u * u32(T.mod[sl].m);
+            slot_base[sl] = sbase + 8 * T.mod[sl].smem_offset;
+        }
+        for (;;) {
+            int item = 0;
+            if (lane == 0) item = atomicAdd(const_cast<int *>(&S.next), 1);
+            item = __shfl_sync(kFullMask, item, 0);
+            if (item >= total_items) break;
+            // class index: largest c with prefix[c] <= item (32 classes per probe)
+            int c = 0;
+            for (int base = 0; base < nclass; base += 32) {
+                const int cc = base + lane;
+                const u32 bb = __ballot_sync(kFullMask, cc < nclass && S.prefix[cc] <= item);
+                if (bb) c = base + 31 - __clz(bb);
+                if (bb != kFullMask) break;
             }
-            for (;;) {
-                int item = 0;
-                if (lane == 0) item = atomicAdd(&s_next, 1);
-                item = __shfl_sync(kFullMask, item, 0);
-                if (item >= total_items) break;
-                // class index: largest c with s_prefix[c] <= item (32 classes per probe)
-                int c = 0;
-                for (int base = 0; base < nclass; base += 32) {
-                    const int cc = base + lane;
-                    const u32 b = __ballot_sync(kFullMask, cc < nclass && s_prefix[cc] <= item);
-                    if (b) c = base + 31 - __clz(b);
-                    if (b != kFullMask) break;
-                }
-                const int w0 = (item - s_prefix[c]) * kFItemWords;
-                const int wt = s_wtile[c];
-                const int last_word = s_last_word[c];
-                const u64 last_mask =
-                    s_last_bits[c] >= 64 ? ~u64(0) : ((u64(1) << s_last_bits[c]) - 1);
-                u32 o[NS];  // byte offset of this lane's word inside each staged row
+            const int w0 = (item - S.prefix[c]) * kFItemWords;
+            const FastRun run = S.run[c];
+            const FastClassStart cs = T.class_starts[run.r];
+            const int wt = run.words;
+            const int last_word = run.last_word;
+            const u64 last_mask = run.last_bits >= 64 ? ~u64(0) : ((u64(1) << run.last_bits) - 1);
+            u32 o[NS];  // byte offset of this lane's word inside each staged row
 #pragma unroll
-                for (int sl = 0; sl < NS; ++sl)
-                    o[sl] = 8u * mod_u32(s_start[c * NS + sl] + u32(w0 + lane), u32(T.mod[sl].m),
-                                         T.mod[sl].magic);
+            for (int sl = 0; sl < NS; ++sl)
+                o[sl] = 8u * mod_u32(u32(cs.start[sl]) + T.mod[sl].wlo_mod + u32(w0 + lane),
+                                     u32(T.mod[sl].m), T.mod[sl].magic);
 #pragma unroll 1
-                for (int step = 0; step < kFSteps; ++step) {
-                    const int ws = w0 + step * kWarpSize * kFK;
-                    if (ws >= wt) break;
-                    u64 acc[kFK];
+            for (int step = 0; step < kFSteps; ++step) {
+                const int ws = w0 + step * kWarpSize * kFK;
+                if (ws >= wt) break;
+                u64 acc[kFK];
+#pragma unroll
+                for (int kk = 0; kk < kFK; ++kk)
+                    acc[kk] = *reinterpret_cast<const u64 *>(slot_base[0] + o[0] + 256 * kk);
+#pragma unroll
+                for (int sl = 1; sl < NS; ++sl) {
 #pragma unroll
                     for (int kk = 0; kk < kFK; ++kk)
-                        acc[kk] = *reinterpret_cast<const u64 *>(slot_base[0] + o[0] + 256 * kk);
+                        acc[kk] &= *reinterpret_cast<const u64 *>(slot_base[sl] + o[sl] + 256 * kk);
+                }
 #pragma unroll
-                    for (int sl = 1; sl < NS; ++sl) {
+                for (int sl = 0; sl < NS; ++sl) {
+                    // advance (32 kFK) mod m words; unsigned min wraps into [0, m)
+                    const u32 t = o[sl] + step8[sl];
+                    o[sl] = min(t, t - mod8[sl]);
+                }
+                const u64 any = acc[0] | acc[1] | acc[2] | acc[3];
+                if (!__ballot_sync(kFullMask, any != 0)) continue;
 #pragma unroll
-                        for (int kk = 0; kk < kFK; ++kk)
-                            acc[kk] &= *reinterpret_cast<const u64 *>(slot_base[sl] + o[sl] + 256 * kk);
-                    }
-#pragma unroll
-                    for (int sl = 0; sl < NS; ++sl) {
-                        // advance (32 kFK) mod m words; unsigned min wraps into [0, m)
-                        const u32 t = o[sl] + step8[sl];
-                        o[sl] = min(t, t - mod8[sl]);
-                    }
-                    const u64 any = acc[0] | acc[1] | acc[2] | acc[3];
-                    if (!__ballot_sync(kFullMask, any != 0)) continue;
-#pragma unroll
-                    for (int kk = 0; kk < kFK; ++kk) {
-                        const int w = ws + kWarpSize * kk + lane;
-                        u64 a = acc[kk];
-                        if (w == last_word) a &= last_mask;
-                        const bool live = a != 0 && w < wt;
-                        const u32 b = __ballot_sync(kFullMask, live);
-                        if (b) {
-                            const int pos = qn + __popc(b & lanemask_lt());
-                            if (live) {
-                                wq_mask[pos] = a;
-                                wq_info[pos] = (u32(w) << kFClassBits) | u32(c);
-                            }
-                            qn += __popc(b);
-                            if (qn >= 32) {
-                                __syncwarp();
-                                fast_drain(wq_mask, wq_info, qn - 32, 32, T, A, int(d), s_sel,
-                                           s_prow, s_ofs);
-                                qn -= 32;
-                            }
+                for (int kk = 0; kk < kFK; ++kk) {
+                    const int w = ws + kWarpSize * kk + lane;
+                    u64 a = acc[kk];
+                    if (w == last_word) a &= last_mask;
+                    const bool live = a != 0 && w < wt;
+                    const u32 bb = __ballot_sync(kFullMask, live);
+                    if (bb) {
+                        const int pos = qn + __popc(bb & lanemask_lt());
+                        if (live) {
+                            wq_mask[pos] = a;
+                            wq_info[pos] = (u32(w) << kFClassBits) | u32(c);
+                        }
+                        qn += __popc(bb);
+                        if (qn >= 32) {
+                            __syncwarp();
+                            fast_drain(wq_mask, wq_info, qn - 32, 32, T, A, S);
+                            qn -= 32;
                         }
                     }
                 }
             }
-            __syncwarp();
-            fast_drain(wq_mask, wq_info, 0, qn, T, A, int(d), s_sel, s_prow, s_ofs);
-            __syncthreads();
-            if (s_abort) {
-                // a bulk copy did not complete in time: give in-flight copies a
-                // last bounded chance to land, then leave (the host reports it)
-                if (threadIdx.x == 0) mbar_wait(bar, phase ^ 1u);
-                return;
-            }
         }
-        __syncthreads();
+        __syncwarp();
+        fast_drain(wq_mask, wq_info, 0, qn, T, A, S);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_addr(&s_empty[b]));  // this warp is done with slot b
+        b ^= 1;
     }
 }
 
