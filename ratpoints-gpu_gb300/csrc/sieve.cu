@@ -620,7 +620,7 @@ struct Sieve::Impl {
         F.admissible = fast_adm;
         F.class_starts = fast_starts;
         fast_smem = std::size_t(dev::kFSlotCount) * std::size_t(F.smem_words) * 8 +
-                    std::size_t(dev::kFConsumers) * dev::kFQueue * 12;
+                    std::size_t(dev::kFConsumers) * dev::kFQueue * 16;
         const void *kernel = fast_kernel_ptr(F.slots);
         check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(fast_smem)),
@@ -900,6 +900,9 @@ Sieve::Sieve(const std::vector<std::string> &coefficients, long long bound,
              const SieveOptions &options)
     : impl_(new Impl) {
     if (bound < 1) throw std::invalid_argument("numerator bound must be positive");
+    // the fast kernel's queued positions a + H must stay below 2^47
+    if (options.plan == PlanKind::fast && bound > (1LL << 45))
+        throw std::invalid_argument("numerator bound too large for the fast plan (at most 2^45)");
     impl_->opt = options;
     impl_->bound = bound;
     impl_->words = word_count64(bound);

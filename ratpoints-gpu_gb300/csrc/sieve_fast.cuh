@@ -165,11 +165,10 @@ __global__ void class_table_kernel(u64 *rows, const TableSpec *specs, int nspecs
 // One admissible class of the slot's denominator: its words inside the
 // launch's tile, where its last word is (or -1), and that word's valid bits.
 struct FastRun {
-    int words;
-    int last_word;
+    u32 words_last;                // words in the tile (bits 0..23), last word in the tile (bit 24),
+                                   // valid bits of the class's last word (bits 25..31, 1..64)
     unsigned short ofs;            // (r + H) mod M
     unsigned short r;              // class residue mod M
-    int last_bits;
 };
 
 // A denominator in flight: written by the producer warp, read by the others.
@@ -177,33 +176,42 @@ struct FastSlot {
     long long d;                   // denominator; -1: no more work
     int nclass;
     int next;                      // sweep-item counter
-    int sel[kSelectedPrimes];      // selected candidates, largest first
-    long long prow[kSelectedPrimes];  // class-layout row of each for d mod p
+    unsigned char sel[kSelectedPrimes];  // selected candidates, largest first
     int prefix[kFMaxClasses + 1];  // first sweep item of each class
     FastRun run[kFMaxClasses];
+};
+
+// A denominator a consumer warp still has queued words of: its copy of the
+// slot's denominator and prime selection, so the slot can be refilled before
+// those words go through stage 2.
+constexpr int kFCtx = 4;
+struct FastCtx {
+    int d;
+    unsigned char sel[kSelectedPrimes];
 };
 
 __device__ __forceinline__ void mbar_arrive(u32 bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// Stage 2 for up to 32 queued class words (one per lane), then emission.
-__device__ __forceinline__ void fast_drain(const u64 *qmask, const u32 *qinfo, int start, int n,
+// Stage 2 for up to 32 queued words (one per lane), then emission.  A queued
+// word carries its denominator context (bits 56..57) and the position
+// pos = a - (-H) of its bit 0 (bits 0..55): its sites are a = -H + pos + M j,
+// and the class-layout row index of prime p is (a mod p) S^-1 mod p.
+__device__ __forceinline__ void fast_drain(const u64 *qmask, const u64 *qpos, int start, int n,
                                            const FastTables &T, const SieveArgs &A,
-                                           const FastSlot &S) {
+                                           const FastCtx *ctx) {
     const int lane = threadIdx.x & 31;
-    u64 m = 0;
-    u32 info = 0;
+    u64 m = 0, pos = 0;
     if (lane < n) {
         m = qmask[start + lane];
-        info = qinfo[start + lane];
+        pos = qpos[start + lane];
     }
     __syncwarp();
-    const u32 off = info >> kFClassBits;
-    const int c = int(info & ((1u << kFClassBits) - 1));
-    const u32 ofs = S.run[c].ofs;                      // (r + H) mod M
-    const long long a0 = -A.bound + ofs;               // least a >= -H in the class
-    const long long w = A.w_lo + off;
+    const FastCtx &X = ctx[int(pos >> 56) & (kFCtx - 1)];
+    const u64 p56 = pos & ((u64(1) << 56) - 1);
+    const u32 hi = u32(p56 >> 16), lo = u32(p56 & 0xFFFF);
+    const u32 d = u32(X.d);
     if (m) {
         // the table words of kFStage2Group primes are loaded together, so a
         // word pays one L2 round trip per group instead of one per prime
@@ -211,23 +219,21 @@ __device__ __forceinline__ void fast_drain(const u64 *qmask, const u32 *qinfo, i
             u64 rows[kFStage2Group];
 #pragma unroll
             for (int t = 0; t < kFStage2Group; ++t) {
-                const int s = s0 + t;
-                const FastPrime &P = T.prime[S.sel[s]];
+                const FastPrime &P = T.prime[X.sel[s0 + t]];
                 const u32 p = u32(P.p);
-                u32 a0m = P.neg_h + mod_small(ofs, p, P.magic);
-                if (a0m >= p) a0m -= p;
-                u32 u = mod_small(a0m * P.inv_stride, p, P.magic);
-                u += P.wlo_mod;
-                if (u >= p) u -= p;
-                u += mod_small(off, p, P.magic);
-                if (u >= p) u -= p;
-                rows[t] = __ldg(T.prime_rows + S.prow[s] + u);
+                u32 r = mod_small(hi, p, P.magic);
+                r = mod_small((r << 16) | lo, p, P.magic);  // pos mod p
+                r += P.neg_h;                               // a mod p
+                if (r >= p) r -= p;
+                const u32 u = mod_small(r * P.inv_stride, p, P.magic);
+                const u32 rho = mod_small(d, p, P.magic);
+                rows[t] = __ldg(T.prime_rows + P.offset + (long long)rho * p + u);
             }
 #pragma unroll
             for (int t = 0; t < kFStage2Group; ++t) m &= rows[t];
         }
     }
-    // emission: a = a0 + S w + M j
+    // emission: a = -H + pos + M j
     u32 cnt = __popcll(m);
     if (!__any_sync(kFullMask, cnt != 0)) return;
     u32 incl = cnt;
@@ -240,16 +246,16 @@ __device__ __forceinline__ void fast_drain(const u64 *qmask, const u32 *qinfo, i
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(A.out_count, (unsigned long long)total);
     base = __shfl_sync(kFullMask, base, 0);
-    unsigned long long pos = base + incl - cnt;
-    const long long abase = a0 + T.stride * w;
+    unsigned long long at = base + incl - cnt;
+    const long long abase = -A.bound + (long long)p56;
     while (m) {
         const int bit = __ffsll((long long)m) - 1;
         m &= m - 1;
-        if (pos < A.capacity) {
-            A.out_a[pos] = abase + (long long)T.class_mod * bit;
-            A.out_d[pos] = int(S.d);
+        if (at < A.capacity) {
+            A.out_a[at] = abase + (long long)T.class_mod * bit;
+            A.out_d[at] = int(d);
         }
-        ++pos;
+        ++at;
     }
 }
 
@@ -273,15 +279,10 @@ __device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs 
         const u32 lo_div = __ballot_sync(kFullMask, rl == 0);
         const u32 below = lanemask_lt();
         const int rank_h = lane - __popc(hi_div & below);
-        if (rh != 0 && rank_h < kSelectedPrimes) {
-            S.sel[rank_h] = ch;
-            S.prow[rank_h] = T.prime[ch].offset + (long long)rh * T.prime[ch].p;
-        }
+        if (rh != 0 && rank_h < kSelectedPrimes) S.sel[rank_h] = (unsigned char)ch;
         const int rank_l = 32 - __popc(hi_div) + lane - __popc(lo_div & below);
-        if (lane < kCandidatePrimes - 32 && rl != 0 && rank_l < kSelectedPrimes) {
-            S.sel[rank_l] = cl;
-            S.prow[rank_l] = T.prime[cl].offset + (long long)rl * T.prime[cl].p;
-        }
+        if (lane < kCandidatePrimes - 32 && rl != 0 && rank_l < kSelectedPrimes)
+            S.sel[rank_l] = (unsigned char)cl;
     }
     const u64 classes2 = __ldg(T.admissible + (du & 63));
     const u64 classesq =
@@ -307,14 +308,14 @@ __device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs 
             const long long lo = A.w_lo < words ? A.w_lo : words;
             const long long hi = A.w_hi < words ? A.w_hi : words;
             FastRun run;
-            run.words = int(hi - lo);
+            const u32 tile_words = u32(hi - lo);
             const bool has_last = hi == words && words > 0 && hi > lo;
-            run.last_word = has_last ? int(words - 1 - lo) : -1;
-            run.last_bits = has_last ? int(count - 64 * (words - 1)) : 64;
+            const u32 last_bits = has_last ? u32(count - 64 * (words - 1)) : 64u;
+            run.words_last = tile_words | (has_last ? 1u << 24 : 0u) | ((last_bits - 1) << 25);
             run.ofs = (unsigned short)ofs;
             run.r = (unsigned short)r;
             S.run[c] = run;
-            items = (run.words + kFItemWords - 1) / kFItemWords;
+            items = int((tile_words + kFItemWords - 1) / kFItemWords);
         }
         int incl = items;
 #pragma unroll
@@ -340,9 +341,10 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
     extern __shared__ __align__(16) u64 smem[];
     const int row_stride = T.smem_words;  // even: buffers stay 16-byte aligned
     u64 *qmask = smem + kFSlotCount * row_stride;
-    u32 *qinfo = reinterpret_cast<u32 *>(qmask + kFConsumers * kFQueue);
+    u64 *qpos = qmask + kFConsumers * kFQueue;
 
     __shared__ FastSlot slot[kFSlotCount];
+    __shared__ FastCtx s_ctx[kFConsumers][kFCtx];
     __shared__ __align__(8) unsigned long long s_full[kFSlotCount];
     __shared__ __align__(8) unsigned long long s_empty[kFSlotCount];
 
@@ -440,9 +442,21 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
     // ---- consumers: sweep the items of each filled slot in turn ----
     const int cw = warp - 1;
     u64 *wq_mask = qmask + cw * kFQueue;
-    u32 *wq_info = qinfo + cw * kFQueue;
-    u32 phase = 0;  // bit b: parity of slot b's next fill
+    u64 *wq_pos = qpos + cw * kFQueue;
+    FastCtx *ctx = s_ctx[cw];
+    u32 phase = 0;   // bit b: parity of slot b's next fill
     int b = 0;
+    int qn = 0;      // queued words (kept across denominators)
+    int seq = 0;     // slot fills this warp has taken
+    int oldest = 0;  // oldest context that may still have queued words
+    auto drain_all = [&]() {
+        while (qn > 0) {
+            const int n = qn < 32 ? qn : 32;
+            __syncwarp();
+            fast_drain(wq_mask, wq_pos, qn - n, n, T, A, ctx);
+            qn -= n;
+        }
+    };
     for (;;) {
         if (!mbar_wait(smem_addr(&s_full[b]), (phase >> b) & 1u)) {  // bounded wait
             if (A.error && lane == 0) atomicOr(A.error, 1ull);
@@ -450,11 +464,23 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
         }
         phase ^= 1u << b;
         const FastSlot &S = slot[b];
-        if (S.d < 0) return;  // the producer has no more work
+        if (S.d < 0) {  // the producer has no more work
+            drain_all();
+            return;
+        }
+        // context k replaces the one taken kFCtx fills ago: its queued words go first
+        const int k = seq & (kFCtx - 1);
+        if (qn > 0 && seq - oldest >= kFCtx) drain_all();
+        if (qn == 0) oldest = seq;
+        __syncwarp();
+        ctx[k].sel[lane] = S.sel[lane];
+        if (lane == 0) ctx[k].d = int(S.d);
+        __syncwarp();
+        const u64 tag = u64(k) << 56;
+
         const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
         const int nclass = S.nclass;
         const int total_items = S.prefix[nclass];
-        int qn = 0;
         u32 step8[NS], mod8[NS];
         const unsigned char *slot_base[NS];
 #pragma unroll
@@ -479,9 +505,12 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
             const int w0 = (item - S.prefix[c]) * kFItemWords;
             const FastRun run = S.run[c];
             const FastClassStart cs = T.class_starts[run.r];
-            const int wt = run.words;
-            const int last_word = run.last_word;
-            const u64 last_mask = run.last_bits >= 64 ? ~u64(0) : ((u64(1) << run.last_bits) - 1);
+            const int wt = int(run.words_last & 0xFFFFFFu);
+            const int last_word = (run.words_last >> 24) & 1u ? wt - 1 : -1;
+            const u32 last_bits = (run.words_last >> 25) + 1;
+            const u64 last_mask = last_bits >= 64 ? ~u64(0) : ((u64(1) << last_bits) - 1);
+            // pos of word w of this class: ofs + S (w_lo + w)
+            const u64 pos0 = u64(run.ofs) + u64(T.stride) * u64(A.w_lo);
             u32 o[NS];  // byte offset of this lane's word inside each staged row
 #pragma unroll
             for (int sl = 0; sl < NS; ++sl)
@@ -517,25 +546,25 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
                     const bool live = a != 0 && w < wt;
                     const u32 bb = __ballot_sync(kFullMask, live);
                     if (bb) {
-                        const int pos = qn + __popc(bb & lanemask_lt());
+                        const int at = qn + __popc(bb & lanemask_lt());
                         if (live) {
-                            wq_mask[pos] = a;
-                            wq_info[pos] = (u32(w) << kFClassBits) | u32(c);
+                            wq_mask[at] = a;
+                            wq_pos[at] = tag | (pos0 + u64(T.stride) * u64(w));
                         }
                         qn += __popc(bb);
                         if (qn >= 32) {
                             __syncwarp();
-                            fast_drain(wq_mask, wq_info, qn - 32, 32, T, A, S);
+                            fast_drain(wq_mask, wq_pos, qn - 32, 32, T, A, ctx);
                             qn -= 32;
+                            if (qn == 0) oldest = seq;
                         }
                     }
                 }
             }
         }
         __syncwarp();
-        fast_drain(wq_mask, wq_info, 0, qn, T, A, S);
-        __syncwarp();
         if (lane == 0) mbar_arrive(smem_addr(&s_empty[b]));  // this warp is done with slot b
+        ++seq;
         b ^= 1;
     }
 }
