@@ -239,6 +239,57 @@ T *device_alloc(std::size_t count, const char *what) {
 
 constexpr long long kInitialSurvivors = 1 << 16;  // survivors per buffer before any growth
 
+// Most admissible numerator classes of any denominator under the fast plan:
+// 2-adic classes (by d mod 64) times residues mod the class prime q (by d mod q).
+int max_admissible_classes(const std::vector<std::string> &coefficients, int q) {
+    const int n = int(coefficients.size()) - 1;
+    std::vector<int> c64(coefficients.size());
+    for (std::size_t i = 0; i < coefficients.size(); ++i) c64[i] = decimal_mod(coefficients[i], 64);
+    bool square64[64] = {};
+    for (int v = 0; v < 64; ++v) square64[(v * v) & 63] = true;
+    int most2 = 0;
+    for (int dd = 0; dd < 64; ++dd) {
+        int count = 0;
+        for (int r = 0; r < 64; ++r) {
+            if (dd % 2 == 0 && r % 2 == 0) continue;
+            int value = c64[n], power = 1;
+            for (int i = n - 1; i >= 0; --i) {
+                value = (value * r) & 63;
+                power = (power * dd) & 63;
+                value = (value + c64[i] * power) & 63;
+            }
+            if (n % 2 == 1) value = (value * dd) & 63;
+            count += square64[value];
+        }
+        most2 = std::max(most2, count);
+    }
+    if (q <= 1) return std::max(1, most2);
+    const auto aff = affine_mask(q, coefficients);
+    int most_q = 0;
+    for (int dq = 0; dq < q; ++dq) {
+        int count = 0;
+        for (int r = 0; r < q; ++r) count += dq == 0 ? (r != 0) : aff[(r * mod_inverse(dq, q)) % q];
+        most_q = std::max(most_q, count);
+    }
+    return std::max(1, most2 * std::max(1, most_q));
+}
+
+// Dynamic shared memory of the fast kernel: two staged row sets, the
+// consumer queues, and the two slots' class runs and item prefixes.
+std::size_t fast_dynamic_smem(int row_words, int max_classes) {
+    const std::size_t runs = (std::size_t(dev::kFSlotCount) * max_classes * sizeof(dev::FastRun) + 7) & ~std::size_t(7);
+    return std::size_t(dev::kFSlotCount) * std::size_t(row_words) * 8 +
+           std::size_t(dev::kFConsumers) * dev::kFQueue * 16 + runs +
+           std::size_t(dev::kFSlotCount) * std::size_t(max_classes + 1) * 4;
+}
+
+// Staged row words per slot that keep a CTA within half an SM's shared
+// memory (2 CTAs/SM, 1 KiB reserved each, 2 KiB of static shared memory).
+long long fast_row_budget(int max_classes) {
+    const long long per_cta = 228 * 1024 / 2 - 1024 - 2048;
+    return (per_cta - (long long)fast_dynamic_smem(0, max_classes)) / (8 * dev::kFSlotCount);
+}
+
 struct Sieve::Impl {
     SieveOptions opt;
     long long bound = 0, words = 0;
@@ -251,6 +302,7 @@ struct Sieve::Impl {
     dev::u64 *fast_rows = nullptr;
     dev::u64 *fast_adm = nullptr;
     dev::FastClassStart *fast_starts = nullptr;
+    int fast_max_classes = 1;
     std::size_t fast_smem = 0;
     std::vector<dev::u64> fast_adm_host;
     FastPlan fast_plan;
@@ -425,12 +477,15 @@ struct Sieve::Impl {
     // admissible-class tables (2-adic by d mod 64, residues mod q by d mod q).
     void build_fast_tables(const std::vector<std::string> &coefficients) {
         auto t0 = Clock::now();
-        // the two staged row sets of a CTA must fit shared memory at 2 CTAs/SM
+        // the two staged row sets of a CTA, its queues and its two slots' class
+        // runs must fit shared memory at 2 CTAs/SM
         fast_plan = choose_fast_plan(coefficients, bound);
+        fast_max_classes = max_admissible_classes(coefficients, fast_plan.class_prime);
+        const long long row_budget = fast_row_budget(fast_max_classes);
         for (int cap = kMaxModulus;;) {
             int row_words = 0;
             for (int m : fast_plan.moduli) row_words += (m + dev::kFExt + 1) & ~1;
-            if (row_words <= dev::kFRowBudget || cap <= 64) break;
+            if (row_words <= row_budget || cap <= 64) break;
             cap = cap * 7 / 8;
             fast_plan = choose_fast_plan(coefficients, bound, cap);
         }
@@ -619,8 +674,8 @@ struct Sieve::Impl {
         F.prime_rows = fast_rows;
         F.admissible = fast_adm;
         F.class_starts = fast_starts;
-        fast_smem = std::size_t(dev::kFSlotCount) * std::size_t(F.smem_words) * 8 +
-                    std::size_t(dev::kFConsumers) * dev::kFQueue * 16;
+        F.max_classes = fast_max_classes;
+        fast_smem = fast_dynamic_smem(F.smem_words, fast_max_classes);
         const void *kernel = fast_kernel_ptr(F.slots);
         check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(fast_smem)),

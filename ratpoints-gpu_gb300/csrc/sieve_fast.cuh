@@ -41,7 +41,6 @@ constexpr int kFThreads = kFWarps * kWarpSize;
 constexpr int kFConsumers = kFWarps - 1;
 constexpr int kFSlotCount = 2;                             // denominators in flight per CTA
 constexpr int kFChunk = 32;                                // parameters per producer fetch
-constexpr int kFRowBudget = 5840;                          // staged row words per slot (2 CTAs/SM)
 constexpr int kFSteps = 4;                                 // steps per work item
 constexpr int kFItemWords = kWarpSize * kFK * kFSteps;     // 512 words per item
 constexpr int kFExt = kWarpSize * (kFK - 1);               // row extension
@@ -88,6 +87,7 @@ static_assert(sizeof(FastClassStart) == 16, "one 16-byte load per class");
 
 struct FastTables {
     const FastClassStart *class_starts;  // [M]
+    int max_classes;               // most admissible classes of any denominator
     const u64 *rows;               // stage-1 modulus tables
     const u64 *prime_rows;         // reference candidate tables (class layout)
     const u64 *admissible;         // [64] 2-adic classes by d mod 64, then [kFAdmQ] residues by d mod q
@@ -168,17 +168,18 @@ struct FastRun {
     u32 words_last;                // words in the tile (bits 0..23), last word in the tile (bit 24),
                                    // valid bits of the class's last word (bits 25..31, 1..64)
     unsigned short ofs;            // (r + H) mod M
-    unsigned short r;              // class residue mod M
+    unsigned short start[kFastSlots];  // row index of the tile's first class word, per modulus
 };
+static_assert(sizeof(FastRun) == 20, "packed class run");
 
 // A denominator in flight: written by the producer warp, read by the others.
+// Its class runs and item prefix live in dynamic shared memory, sized by the
+// plan's largest class count (FastTables::max_classes).
 struct FastSlot {
     long long d;                   // denominator; -1: no more work
     int nclass;
     int next;                      // sweep-item counter
     unsigned char sel[kSelectedPrimes];  // selected candidates, largest first
-    int prefix[kFMaxClasses + 1];  // first sweep item of each class
-    FastRun run[kFMaxClasses];
 };
 
 // A denominator a consumer warp still has queued words of: its copy of the
@@ -263,7 +264,7 @@ __device__ __forceinline__ void fast_drain(const u64 *qmask, const u64 *qpos, in
 // largest candidates not dividing d (two ballots), then the admissible
 // classes and their sweep items (a prefix scan, 32 classes per pass).
 __device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs &A, long long d,
-                                           FastSlot &S) {
+                                           FastSlot &S, FastRun *runs, int *prefix) {
     const int lane = threadIdx.x & 31;
     const u32 du = u32(d);
     const int q = T.class_prime;
@@ -301,7 +302,8 @@ __device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs 
                 const int rq = nth_bit64(classesq, c - i2 * nq);
                 r = r64 + 64 * int(T.crt[T.mod_q[r64] * 13 + rq]);
             }
-            const int ofs = T.class_starts[r].ofs;
+            const FastClassStart cs = T.class_starts[r];
+            const int ofs = cs.ofs;
             // sites of class r: a = -H + ofs + M t, t in [0, count)
             const long long count = T.count_q + (ofs <= T.count_r ? 1 : 0);
             const long long words = (count + 63) >> 6;
@@ -313,8 +315,15 @@ __device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs 
             const u32 last_bits = has_last ? u32(count - 64 * (words - 1)) : 64u;
             run.words_last = tile_words | (has_last ? 1u << 24 : 0u) | ((last_bits - 1) << 25);
             run.ofs = (unsigned short)ofs;
-            run.r = (unsigned short)r;
-            S.run[c] = run;
+#pragma unroll
+            for (int sl = 0; sl < kFastSlots; ++sl) {
+                // tile word 0 is class word w_lo: (a0 S^-1 + w_lo) mod m
+                const FastModulus &Md = T.mod[sl];
+                u32 st = u32(cs.start[sl]) + Md.wlo_mod;  // both below m
+                if (st >= u32(Md.m)) st -= u32(Md.m);
+                run.start[sl] = (unsigned short)st;
+            }
+            runs[c] = run;
             items = int((tile_words + kFItemWords - 1) / kFItemWords);
         }
         int incl = items;
@@ -323,11 +332,11 @@ __device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs 
             const int v = __shfl_up_sync(kFullMask, incl, o);
             if (lane >= o) incl += v;
         }
-        if (c < nclass) S.prefix[c] = carry + incl - items;
+        if (c < nclass) prefix[c] = carry + incl - items;
         carry += __shfl_sync(kFullMask, incl, 31);
     }
     if (lane == 0) {
-        S.prefix[nclass] = carry;
+        prefix[nclass] = carry;
         S.nclass = nclass;
         S.next = 0;
         S.d = d;
@@ -342,6 +351,8 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
     const int row_stride = T.smem_words;  // even: buffers stay 16-byte aligned
     u64 *qmask = smem + kFSlotCount * row_stride;
     u64 *qpos = qmask + kFConsumers * kFQueue;
+    FastRun *runs0 = reinterpret_cast<FastRun *>(qpos + kFConsumers * kFQueue);  // [slots][max_classes]
+    int *prefix0 = reinterpret_cast<int *>(runs0 + kFSlotCount * T.max_classes);  // [slots][max_classes + 1]
 
     __shared__ FastSlot slot[kFSlotCount];
     __shared__ FastCtx s_ctx[kFConsumers][kFCtx];
@@ -409,7 +420,7 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
                 }
                 break;
             }
-            fast_setup(T, A, d, S);
+            fast_setup(T, A, d, S, runs0 + b * T.max_classes, prefix0 + b * (T.max_classes + 1));
             __syncwarp();
             if (lane == 0) {
                 __threadfence_block();
@@ -479,8 +490,10 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
         const u64 tag = u64(k) << 56;
 
         const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
+        const FastRun *runs = runs0 + b * T.max_classes;
+        const int *prefix = prefix0 + b * (T.max_classes + 1);
         const int nclass = S.nclass;
-        const int total_items = S.prefix[nclass];
+        const int total_items = prefix[nclass];
         u32 step8[NS], mod8[NS];
         const unsigned char *slot_base[NS];
 #pragma unroll
@@ -498,13 +511,12 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
             int c = 0;
             for (int base = 0; base < nclass; base += 32) {
                 const int cc = base + lane;
-                const u32 bb = __ballot_sync(kFullMask, cc < nclass && S.prefix[cc] <= item);
+                const u32 bb = __ballot_sync(kFullMask, cc < nclass && prefix[cc] <= item);
                 if (bb) c = base + 31 - __clz(bb);
                 if (bb != kFullMask) break;
             }
-            const int w0 = (item - S.prefix[c]) * kFItemWords;
-            const FastRun run = S.run[c];
-            const FastClassStart cs = T.class_starts[run.r];
+            const int w0 = (item - prefix[c]) * kFItemWords;
+            const FastRun run = runs[c];
             const int wt = int(run.words_last & 0xFFFFFFu);
             const int last_word = (run.words_last >> 24) & 1u ? wt - 1 : -1;
             const u32 last_bits = (run.words_last >> 25) + 1;
@@ -514,8 +526,8 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
             u32 o[NS];  // byte offset of this lane's word inside each staged row
 #pragma unroll
             for (int sl = 0; sl < NS; ++sl)
-                o[sl] = 8u * mod_u32(u32(cs.start[sl]) + T.mod[sl].wlo_mod + u32(w0 + lane),
-                                     u32(T.mod[sl].m), T.mod[sl].magic);
+                o[sl] = 8u * mod_u32(u32(run.start[sl]) + u32(w0 + lane), u32(T.mod[sl].m),
+                                     T.mod[sl].magic);
 #pragma unroll 1
             for (int step = 0; step < kFSteps; ++step) {
                 const int ws = w0 + step * kWarpSize * kFK;
