@@ -45,6 +45,21 @@ DENOMINATORS = 5_000_000
 BATCH = 1 << 16
 SMS = 152
 SMEM_BYTES_PER_CLK = 128      # lane-contiguous LDS.64, measured per SM on GB300
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 65,536-denominator
+# fast-plan launch of this workload, from an ncu capture of the kernel:
+#   ncu --set full --clock-control none -k regex:fast_sieve -s 1 -c 1 python bench.py
+#       --steps 1 --warmup 1 --no-cpu-baseline --reference-plan-steps 0
+#       --reference-gpu-denominators 0 --restricted 0 --serving-requests 0 --batch-curves 0
+#       --denominators 131072
+FAST_LAUNCH_DRAM_BYTES = 46_370_560 + 36_864
+
+
+def measured_hbm_gbs():
+    """The machine's measured HBM copy bandwidth (GB/s), None if not recorded."""
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return None
 REF_FAST_PRIMES = 10          # reference-plan primes read from shared memory per site
 
 
@@ -531,7 +546,17 @@ def main():
                    "modular_survivors": fast["survivors"],
                    "words_swept_per_step": fast["words"]},
         "roofline": {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak,
+                     "traffic": FAST_LAUNCH_DRAM_BYTES if args.plan == "fast" else None,
+                     "traffic_note": "DRAM bytes per 65,536-denominator launch from ncu; the "
+                                     "algorithmic shared-memory bytes per launch are "
+                                     f"{total_bytes / launches_per_step:.3g}",
+                     "hbm": None if args.plan != "fast" or not measured_hbm_gbs() else {
+                         "achieved": FAST_LAUNCH_DRAM_BYTES / (step_ms / launches_per_step / 1e3) / 1e9,
+                         "peak": measured_hbm_gbs(), "unit": "GB/s",
+                         "frac": FAST_LAUNCH_DRAM_BYTES / (step_ms / launches_per_step / 1e3) / 1e9
+                                 / measured_hbm_gbs(),
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (STREAM-style copy)"},
                      "algorithmic": f"{fast['bytes_per_word']} B of stage-1 shared-memory rows per "
                                     f"swept 64-site word x {fast['words']} words per step "
                                     f"/ {launches_per_step} launches",
