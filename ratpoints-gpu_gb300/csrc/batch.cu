@@ -1148,8 +1148,9 @@ FastPlan narrow_plan(const std::vector<std::string> &coefficients) {
 FastPlan wide_plan(const std::vector<std::string> &coefficients, long long bound, long double work,
                    int smem_budget) {
     int cap = int(std::min<long double>(kMaxModulus, std::max<long double>(64, std::sqrt(work / 48.0L))));
+    const FastPlanner planner(coefficients, bound, true);
     for (;;) {
-        FastPlan plan = choose_fast_plan(coefficients, bound, cap, true);
+        FastPlan plan = planner.plan(cap);
         long long smem = 0;
         for (int sl = 0; sl < dev::kWideSlots; ++sl) {
             const int m = sl < int(plan.moduli.size()) ? plan.moduli[sl] : 1;

@@ -117,31 +117,40 @@ int max_classes(int q, const std::vector<std::string> &coefficients) {
 }
 }  // namespace
 
-FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long long bound,
-                          int max_modulus, bool class_layout) {
-    FastPlan plan;
-    std::vector<std::pair<double, int>> strength;  // (bits, prime)
+FastPlanner::FastPlanner(const std::vector<std::string> &coefficients, long long bound,
+                         bool class_layout) {
     for (int q = 3; q < kFastPrimeLimit; q += 2) {
         bool prime = true;
         for (int f = 3; f * f <= q; f += 2) prime = prime && q % f;
         if (!prime) continue;
         const double rate = pass_rate(q, coefficients);
-        strength.push_back({rate > 0 ? -std::log2(rate) : 8.0, q});
+        strength_.push_back({rate > 0 ? -std::log2(rate) : 8.0, q});
     }
     // Class prime: the strongest of 3..13 whose classes stay long enough
     // (at least 256 words of 64 sites per class) and few enough.
     const long double sites = 2.0L * bound + 1.0L;
     double best = 0.45;  // below ~0.45 bits a class prime does not pay for its classes
-    for (const auto &s : strength) {
+    for (const auto &s : strength_) {
         const int q = s.second;
         if (!class_layout || q > 13) continue;
         if (sites / (64.0L * 64.0L * q) < 256.0L) continue;
         if (max_classes(q, coefficients) > kMaxFastClasses) continue;
         if (s.first > best) {
             best = s.first;
-            plan.class_prime = q;
+            class_prime_ = q;
         }
     }
+}
+
+FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long long bound,
+                          int max_modulus, bool class_layout) {
+    return FastPlanner(coefficients, bound, class_layout).plan(max_modulus);
+}
+
+FastPlan FastPlanner::plan(int max_modulus) const {
+    FastPlan plan;
+    plan.class_prime = class_prime_;
+    const std::vector<std::pair<double, int>> &strength = strength_;
     // Stage-1 moduli: pack primes into at most kMaxFastSlots products below
     // kMaxModulus.  Each packing puts a prime into the open modulus with the
     // most headroom that it fits, else opens a new one; it is tried with the

@@ -19,6 +19,7 @@
 #include <array>
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace rpg {
@@ -70,5 +71,18 @@ struct FastPlan {
 // batched search, 64 consecutive numerators per word).
 FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long long bound,
                           int max_modulus = kMaxModulus, bool class_prime = true);
+
+// The autotuner's per-curve work done once (pass rates of every small prime,
+// the class prime), for callers that try several modulus caps.
+class FastPlanner {
+public:
+    FastPlanner(const std::vector<std::string> &coefficients, long long bound, bool class_prime = true);
+    FastPlan plan(int max_modulus = kMaxModulus) const;
+    int class_prime() const { return class_prime_; }
+
+private:
+    std::vector<std::pair<double, int>> strength_;  // (bits, prime) of the odd primes below 128
+    int class_prime_ = 1;
+};
 
 }  // namespace rpg

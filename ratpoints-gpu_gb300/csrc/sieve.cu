@@ -479,7 +479,8 @@ struct Sieve::Impl {
         auto t0 = Clock::now();
         // the two staged row sets of a CTA, its queues and its two slots' class
         // runs must fit shared memory at 2 CTAs/SM
-        fast_plan = choose_fast_plan(coefficients, bound);
+        const FastPlanner planner(coefficients, bound);
+        fast_plan = planner.plan();
         fast_max_classes = max_admissible_classes(coefficients, fast_plan.class_prime);
         const long long row_budget = fast_row_budget(fast_max_classes);
         for (int cap = kMaxModulus;;) {
@@ -487,7 +488,7 @@ struct Sieve::Impl {
             for (int m : fast_plan.moduli) row_words += (m + dev::kFExt + 1) & ~1;
             if (row_words <= row_budget || cap <= 64) break;
             cap = cap * 7 / 8;
-            fast_plan = choose_fast_plan(coefficients, bound, cap);
+            fast_plan = planner.plan(cap);
         }
         const int n = int(coefficients.size()) - 1;
         const int q = fast_plan.class_prime;
