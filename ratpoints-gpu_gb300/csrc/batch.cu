@@ -999,30 +999,6 @@ bool lead_is_square(const std::vector<std::string> &coefficients, int q) {
     return false;
 }
 
-// 2-adic admissible classes r mod 64 by d mod 64: F(r, d) a square mod 64, r
-// odd when d is even (the fast plan's 2-adic filter).
-void two_adic_classes(const std::vector<std::string> &coefficients, dev::u64 out[64]) {
-    const int n = int(coefficients.size()) - 1;
-    std::vector<int> c64(coefficients.size());
-    for (std::size_t i = 0; i < coefficients.size(); ++i) c64[i] = decimal_mod(coefficients[i], 64);
-    bool square64[64] = {};
-    for (int v = 0; v < 64; ++v) square64[(v * v) & 63] = true;
-    for (int dd = 0; dd < 64; ++dd) {
-        out[dd] = 0;
-        for (int r = 0; r < 64; ++r) {
-            if (dd % 2 == 0 && r % 2 == 0) continue;
-            int value = c64[n], power = 1;
-            for (int i = n - 1; i >= 0; --i) {
-                value = (value * r) & 63;
-                power = (power * dd) & 63;
-                value = (value + c64[i] * power) & 63;
-            }
-            if (n % 2 == 1) value = (value * dd) & 63;
-            if (square64[value]) out[dd] |= dev::u64(1) << r;
-        }
-    }
-}
-
 int round_even(long long v) { return int((v + 1) & ~1LL); }
 
 // A rational bound as a double (leading 18 digits of numerator and
@@ -1075,6 +1051,8 @@ struct CurveWork {
     long long words = 0;       // dense 64-site words per row
     long long swept = 0;       // words a denominator sweeps after interval narrowing (estimate)
     long long count = 0;       // parameters
+    dev::u64 adm2[64] = {};    // 2-adic admissible classes by d mod 64
+    std::vector<unsigned short> cand_residues;  // c_i mod p for the 36 candidates, candidate-major
 };
 
 // Words of one denominator's row that the sieve sweeps: the whole row, or with
@@ -1213,6 +1191,14 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                                     cw.words >= dev::kWHugeWords ? 2 * dev::kWMaxSmemWords
                                                                  : dev::kWMaxSmemWords);
             else cw.plan = narrow_plan(c.coefficients);
+            two_adic_classes(c.coefficients, cw.adm2);
+            {
+                const auto &cps = candidate_primes();
+                cw.cand_residues.reserve(kCandidatePrimes * c.coefficients.size());
+                for (int ci = 0; ci < kCandidatePrimes; ++ci)
+                    for (const auto &coef : c.coefficients)
+                        cw.cand_residues.push_back((unsigned short)decimal_mod(coef, cps[ci]));
+            }
             r.wide = cw.wide;
             r.class_prime = cw.plan.class_prime;
             r.moduli = cw.plan.moduli;
@@ -1249,7 +1235,21 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
         const FastPlan &plan = cw.plan;
         const long long H = c.bound;
         const long long aff_base = P.aff_words;
-        for (int ci = 0; ci < kCandidatePrimes; ++ci) add_affine(cands[ci], c.coefficients);
+        {
+            // the 36 candidate bitmasks, residues computed in the parallel phase
+            const std::size_t nc = c.coefficients.size();
+            for (int ci = 0; ci < kCandidatePrimes; ++ci) {
+                dev::AffineSpec A{};
+                A.out = P.aff_words;
+                A.residues = (long long)P.residues.size();
+                A.p = cands[ci];
+                A.n = int(nc) - 1;
+                P.residues.insert(P.residues.end(), cw.cand_residues.begin() + std::ptrdiff_t(ci * nc),
+                                  cw.cand_residues.begin() + std::ptrdiff_t((ci + 1) * nc));
+                P.aspecs.push_back(A);
+                P.aff_words += dev::kRefWords;
+            }
+        }
         // per-prime patterns of this curve's stage-1 factors
         const long long M = cw.wide ? 64LL * plan.class_prime : 1;
         const long long S = cw.wide ? 64LL * M : 64;
@@ -1326,7 +1326,7 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             // row buffers are row_stride words apart; a one-buffer curve spans both
             P.wide_smem_words =
                 std::max(P.wide_smem_words, round_even(C.nbuf == 2 ? smem : (smem + 1) / 2));
-            two_adic_classes(c.coefficients, C.admissible);
+            std::copy(cw.adm2, cw.adm2 + 64, C.admissible);
             if (q > 1) {
                 const auto aff = affine_mask(q, c.coefficients);
                 const bool lead = lead_is_square(c.coefficients, q);
@@ -1425,8 +1425,7 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             if (used > dev::kNarrowTableWords) throw std::logic_error("narrow tables exceed shared memory");
             C.table_words = used;
             // dense layout: bit j of a word holds a = -H + 64 w + j, so a = j - H (mod 64)
-            dev::u64 by_class[64];
-            two_adic_classes(c.coefficients, by_class);
+            const dev::u64 *by_class = cw.adm2;
             const int h64 = int(H % 64);
             for (int dd = 0; dd < 64; ++dd) {
                 dev::u64 mask = 0;

@@ -81,21 +81,14 @@ double pass_rate(int q, const std::vector<std::string> &coefficients) {
     return double(n) / q;
 }
 
-namespace {
-// Worst-case number of numerator classes for class prime q: admissible
-// 2-adic classes times admissible residues mod q, over all d.
-int max_classes(int q, const std::vector<std::string> &coefficients) {
+void two_adic_classes(const std::vector<std::string> &coefficients, std::uint64_t out[64]) {
     const int n = int(coefficients.size()) - 1;
-    std::vector<int> c64(coefficients.size()), cq(coefficients.size());
-    for (std::size_t i = 0; i < coefficients.size(); ++i) {
-        c64[i] = decimal_mod(coefficients[i], 64);
-        cq[i] = decimal_mod(coefficients[i], q);
-    }
-    bool sq64[64] = {};
-    for (int v = 0; v < 64; ++v) sq64[(v * v) & 63] = true;
-    int worst2 = 0;
+    std::vector<int> c64(coefficients.size());
+    for (std::size_t i = 0; i < coefficients.size(); ++i) c64[i] = decimal_mod(coefficients[i], 64);
+    bool square64[64] = {};
+    for (int v = 0; v < 64; ++v) square64[(v * v) & 63] = true;
     for (int dd = 0; dd < 64; ++dd) {
-        int count = 0;
+        out[dd] = 0;
         for (int r = 0; r < 64; ++r) {
             if (dd % 2 == 0 && r % 2 == 0) continue;
             int value = c64[n], power = 1;
@@ -105,17 +98,10 @@ int max_classes(int q, const std::vector<std::string> &coefficients) {
                 value = (value + c64[i] * power) & 63;
             }
             if (n % 2 == 1) value = (value * dd) & 63;
-            count += sq64[value];
+            if (square64[value]) out[dd] |= std::uint64_t(1) << r;
         }
-        worst2 = std::max(worst2, count);
     }
-    const auto aff = affine_mask(q, coefficients);
-    int admissible = 0;
-    for (auto v : aff) admissible += v;
-    // q | d admits every class r != 0 (mod q) at most
-    return worst2 * std::max(admissible, q - 1);
 }
-}  // namespace
 
 FastPlanner::FastPlanner(const std::vector<std::string> &coefficients, long long bound,
                          bool class_layout) {
@@ -127,14 +113,24 @@ FastPlanner::FastPlanner(const std::vector<std::string> &coefficients, long long
         strength_.push_back({rate > 0 ? -std::log2(rate) : 8.0, q});
     }
     // Class prime: the strongest of 3..13 whose classes stay long enough
-    // (at least 256 words of 64 sites per class) and few enough.
+    // (at least 256 words of 64 sites per class) and few enough: admissible
+    // 2-adic classes times admissible residues mod q (q | d admits every
+    // r != 0 at most), over all d.
     const long double sites = 2.0L * bound + 1.0L;
     double best = 0.45;  // below ~0.45 bits a class prime does not pay for its classes
+    int worst2 = -1;
     for (const auto &s : strength_) {
         const int q = s.second;
         if (!class_layout || q > 13) continue;
         if (sites / (64.0L * 64.0L * q) < 256.0L) continue;
-        if (max_classes(q, coefficients) > kMaxFastClasses) continue;
+        if (worst2 < 0) {
+            std::uint64_t adm2[64];
+            two_adic_classes(coefficients, adm2);
+            worst2 = 0;
+            for (auto m : adm2) worst2 = std::max(worst2, __builtin_popcountll(m));
+        }
+        const int admissible = int(std::lround(std::exp2(-s.first) * q));
+        if (worst2 * std::max(admissible, q - 1) > kMaxFastClasses) continue;
         if (s.first > best) {
             best = s.first;
             class_prime_ = q;

@@ -51,6 +51,10 @@ long long word_count32(long long bound);
 // sites (a, d), q !| d, that pass the test mod q.
 double pass_rate(int q, const std::vector<std::string> &coefficients);
 
+// 2-adic admissible classes by d mod 64: bit r of out[d mod 64] is set iff
+// F(r, d) is a square mod 64, with r odd when d is even (gcd).
+void two_adic_classes(const std::vector<std::string> &coefficients, std::uint64_t out[64]);
+
 // Per-curve choice of the fast plan's small-prime filters (this project's
 // autotuner).  Numerator classes are taken modulo 64 * class_prime (2-adic
 // classes crossed with the admissible residues mod class_prime; class_prime 1
