@@ -375,34 +375,54 @@ struct ClassStart {
 };
 static_assert(sizeof(ClassStart) == 16, "one 16-byte load per class");
 
-__device__ __forceinline__ void wide_drain(const u64 *qmask, const u32 *qinfo, int start, int n,
+// A denominator a warp still has queued words of (wide kernel): its prime
+// selection and 1/d mod p, copied from the CTA's set so that the words can
+// wait in the queue past later denominators of the same curve.
+constexpr int kWCtx = 4;
+struct WideCtx {
+    int d;
+    unsigned char sel[kSelectedPrimes];
+    unsigned short dinv[kSelectedPrimes];
+};
+
+// Stage 2 and emission for up to 32 queued words.  A queued word carries its
+// context (bits 56..57) and the position pos = a + H of its bit 0 (bits
+// 0..55); its sites are a = -H + pos + M j.
+__device__ __forceinline__ void wide_drain(const u64 *qmask, const u64 *qpos, int start, int n,
                                            const WideCurve &C, const Candidates &cand,
-                                           const u64 *s_aff, const int *s_ci, const u32 *s_dinv,
-                                           const ClassRun *s_run, long long d, const BatchOut &out) {
+                                           const u64 *s_aff, const WideCtx *ctx,
+                                           const BatchOut &out) {
     const int lane = threadIdx.x & 31;
-    u64 m = 0;
-    u32 info = 0;
+    u64 m = 0, pos = 0;
     if (lane < n) {
         m = qmask[start + lane];
-        info = qinfo[start + lane];
+        pos = qpos[start + lane];
     }
     __syncwarp();
-    const u32 off = info >> kClassBits;
-    const u32 ofs = s_run[info & ((1u << kClassBits) - 1)].ofs;
-    if (m) {
-        m = stage2(
-            m, s_ci, s_dinv, cand, s_aff,
-            [&](int ci, u32 p, u32 magic) {
-                u32 r = C.neg_h[ci] + mod_small(ofs, p, magic);
-                if (r >= p) r -= p;
-                r += mod_small(u32(C.s_mod[ci]) * mod_small(off, p, magic), p, magic);
-                return r >= p ? r - p : r;
-            },
-            [&](int ci) { return u32(C.m_mod[ci]); });
+    const WideCtx &X = ctx[int(pos >> 56) & (kWCtx - 1)];
+    const u64 p56 = pos & ((u64(1) << 56) - 1);
+    const u32 hi = u32(p56 >> 16), lo = u32(p56 & 0xFFFF);
+    for (int s = 0; s < kSelectedPrimes && m; ++s) {
+        const int ci = X.sel[s];
+        const u32 p = u32(cand.p[ci]), magic = cand.magic[ci];
+        const u32 dinv = X.dinv[s];
+        u32 r = mod_small(hi, p, magic);
+        r = mod_small((r << 16) | lo, p, magic);  // pos mod p
+        r += C.neg_h[ci];                          // a mod p
+        if (r >= p) r -= p;
+        const u32 x0 = mod_small(r * dinv, p, magic);
+        const u32 dx = mod_small(u32(C.m_mod[ci]) * dinv, p, magic);
+        const u64 *bits = s_aff + ci * kRefWords;
+        u64 rest = m;
+        while (rest) {
+            const int j = __ffsll((long long)rest) - 1;
+            rest &= rest - 1;
+            const u32 x = mod_small(x0 + u32(j) * dx, p, magic);
+            if (!((bits[x >> 6] >> (x & 63)) & 1)) m &= ~(u64(1) << j);
+        }
     }
-    emit(m, -C.bound + ofs + C.stride * off, C.class_mod, d, C.index, out);
+    emit(m, -C.bound + (long long)p56, C.class_mod, X.d, C.index, out);
 }
-
 
 // Wide rows, one CTA per denominator, software-pipelined over the
 // denominators of an item: while every warp sweeps denominator d_i (rows in
@@ -417,12 +437,11 @@ __global__ void __launch_bounds__(kWThreads, 3)
                 int nitems, const u64 *__restrict__ pool, const u64 *__restrict__ affine,
                 const ClassStart *__restrict__ class_starts,
                 const unsigned short *__restrict__ inv_table, Candidates cand, BatchOut out,
-                int row_stride, unsigned long long *work) {
+                int row_stride, int max_classes, unsigned long long *work) {
     extern __shared__ __align__(16) u64 smem[];
     __shared__ WideCurve C;
     __shared__ u64 s_aff[kAffWords];
-    __shared__ ClassRun s_run[2][kMaxClasses];
-    __shared__ int s_prefix[2][kMaxClasses + 1];
+    __shared__ WideCtx s_ctx[kWWarps][kWCtx];
     __shared__ int s_nclass[2];
     __shared__ int s_ci[2][kSelectedPrimes];
     __shared__ u32 s_dinv[2][kSelectedPrimes];
@@ -434,9 +453,23 @@ __global__ void __launch_bounds__(kWThreads, 3)
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     u64 *qmask = smem + 2 * row_stride;
-    u32 *qinfo = reinterpret_cast<u32 *>(qmask + kWWarps * kQueue);
+    u64 *qpos = qmask + kWWarps * kQueue;
+    ClassRun *runs0 = reinterpret_cast<ClassRun *>(qpos + kWWarps * kQueue);  // [2][max_classes]
+    int *prefix0 = reinterpret_cast<int *>(runs0 + 2 * max_classes);          // [2][max_classes + 1]
     u64 *wq_mask = qmask + warp * kQueue;
-    u32 *wq_info = qinfo + warp * kQueue;
+    u64 *wq_pos = qpos + warp * kQueue;
+    WideCtx *ctx = s_ctx[warp];
+    int qn = 0;       // queued words of this warp, kept across denominators of a curve
+    int seq = 0;      // denominators this CTA has swept
+    int oldest = 0;   // oldest context that may still have queued words
+    auto drain_all = [&]() {
+        while (qn > 0) {
+            const int nd = qn < 32 ? qn : 32;
+            __syncwarp();
+            wide_drain(wq_mask, wq_pos, qn - nd, nd, C, cand, s_aff, ctx, out);
+            qn -= nd;
+        }
+    };
     u32 phase = 0;     // bit b: parity of buffer b's next completion
     u32 pending = 0;   // bit b: a copy into buffer b is in flight and not yet waited for
     int cur = -1;
@@ -455,6 +488,9 @@ __global__ void __launch_bounds__(kWThreads, 3)
         if (it >= nitems) break;
         const BatchItem item = items[it];
         if (item.curve != cur) {
+            // queued words need their curve's descriptor and bitmasks: drain first
+            drain_all();
+            __syncthreads();
             const u32 *src = reinterpret_cast<const u32 *>(curves + item.curve);
             u32 *dst = reinterpret_cast<u32 *>(&C);
             for (int i = threadIdx.x; i < int(sizeof(WideCurve) / 4); i += kWThreads) dst[i] = src[i];
@@ -554,7 +590,7 @@ __global__ void __launch_bounds__(kWThreads, 3)
                             run.first = 0;
                             run.last = 64;
                         }
-                        s_run[st][c] = run;
+                        runs0[st * max_classes + c] = run;
                         nitems_c = (run.words + kWItemWords - 1) / kWItemWords;
                     }
                     int incl = nitems_c;
@@ -563,11 +599,11 @@ __global__ void __launch_bounds__(kWThreads, 3)
                         const int v = __shfl_up_sync(kFullMask, incl, o);
                         if (lane >= o) incl += v;
                     }
-                    if (c < nclass) s_prefix[st][c] = carry + incl - nitems_c;
+                    if (c < nclass) prefix0[st * (max_classes + 1) + c] = carry + incl - nitems_c;
                     carry += __shfl_sync(kFullMask, incl, 31);
                 }
                 if (lane == 0) {
-                    s_prefix[st][nclass] = carry;
+                    prefix0[st * (max_classes + 1) + nclass] = carry;
                     s_nclass[st] = nclass;
                 }
             }
@@ -600,10 +636,19 @@ __global__ void __launch_bounds__(kWThreads, 3)
 
             const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
             const int nclass = s_nclass[st];
-            const int *prefix = s_prefix[st];
-            const ClassRun *runs = s_run[st];
+            const int *prefix = prefix0 + st * (max_classes + 1);
+            const ClassRun *runs = runs0 + st * max_classes;
             const int total_items = prefix[nclass];
-            int qn = 0;
+            // this denominator's context; the one it replaces is drained first
+            const int kc = seq & (kWCtx - 1);
+            if (qn > 0 && seq - oldest >= kWCtx) drain_all();
+            if (qn == 0) oldest = seq;
+            __syncwarp();
+            ctx[kc].sel[lane] = (unsigned char)s_ci[st][lane];
+            ctx[kc].dinv[lane] = (unsigned short)s_dinv[st][lane];
+            if (lane == 0) ctx[kc].d = int(d);
+            __syncwarp();
+            const u64 tag = u64(kc) << 56;
             u32 step8[kWideSlots], mod8[kWideSlots];
             const unsigned char *slot_base[kWideSlots];
 #pragma unroll
@@ -666,24 +711,23 @@ __global__ void __launch_bounds__(kWThreads, 3)
                         const bool live_word = a != 0 && w < wt;
                         const u32 bb = __ballot_sync(kFullMask, live_word);
                         if (bb) {
-                            const int pos = qn + __popc(bb & lanemask_lt());
+                            const int at = qn + __popc(bb & lanemask_lt());
                             if (live_word) {
-                                wq_mask[pos] = a;
-                                wq_info[pos] = (u32(run.wbase + w) << kClassBits) | u32(c);
+                                wq_mask[at] = a;
+                                wq_pos[at] = tag | (u64(run.ofs) + u64(C.stride) * u64(run.wbase + w));
                             }
                             qn += __popc(bb);
                             if (qn >= 32) {
                                 __syncwarp();
-                                wide_drain(wq_mask, wq_info, qn - 32, 32, C, cand, s_aff, s_ci[st],
-                                           s_dinv[st], runs, d, out);
+                                wide_drain(wq_mask, wq_pos, qn - 32, 32, C, cand, s_aff, ctx, out);
                                 qn -= 32;
+                                if (qn == 0) oldest = seq;
                             }
                         }
                     }
                 }
             }
-            __syncwarp();
-            wide_drain(wq_mask, wq_info, 0, qn, C, cand, s_aff, s_ci[st], s_dinv[st], runs, d, out);
+            ++seq;
             __syncthreads();
             if (s_abort) {
                 // a bulk copy did not complete in time: give the copies in
@@ -707,6 +751,7 @@ __global__ void __launch_bounds__(kWThreads, 3)
         }
         __syncthreads();
     }
+    drain_all();  // the last curve's queued words
 }
 
 // ---------------------------------------------------------------------------
@@ -1157,6 +1202,7 @@ struct BatchPlan {
     std::vector<dev::ClassStart> class_starts;
     long long aff_words = 0, pattern_words = 0, row_words = 0;
     int wide_smem_words = 0;
+    int wide_max_classes = 1;   // most admissible classes of any wide curve's denominator
 };
 
 // Validation and per-curve plans (one curve per task), then descriptors,
@@ -1327,6 +1373,11 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             P.wide_smem_words =
                 std::max(P.wide_smem_words, round_even(C.nbuf == 2 ? smem : (smem + 1) / 2));
             std::copy(cw.adm2, cw.adm2 + 64, C.admissible);
+            {
+                int most2 = 0;
+                for (auto m : cw.adm2) most2 = std::max(most2, __builtin_popcountll(m));
+                P.wide_max_classes = std::max(P.wide_max_classes, most2);  // times mod-q residues below
+            }
             if (q > 1) {
                 const auto aff = affine_mask(q, c.coefficients);
                 const bool lead = lead_is_square(c.coefficients, q);
@@ -1339,6 +1390,11 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 for (int a = 0; a < q; ++a)
                     for (int rq = 0; rq < q; ++rq)
                         C.crt[a * 13 + rq] = (unsigned char)(((rq - a + q) % q) * C.inv64_q % q);
+                int most2 = 0, mostq = 0;
+                for (auto m : cw.adm2) most2 = std::max(most2, __builtin_popcountll(m));
+                for (int dq = 0; dq < q; ++dq)
+                    mostq = std::max(mostq, __builtin_popcountll(C.admissible[64 + dq]));
+                P.wide_max_classes = std::max(P.wide_max_classes, most2 * std::max(1, mostq));
             }
             for (int r64 = 0; r64 < 64; ++r64) C.mod_q[r64] = (unsigned char)(q > 1 ? r64 % q : 0);
             // class starts for every residue r mod M: ofs = (r + H) mod M, and per
@@ -1584,8 +1640,11 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
         d_rows.ensure(std::size_t(P.row_words), "cudaMalloc(batch tables)");
 
         const int wide_smem_words = P.wide_smem_words;
-        const std::size_t wide_smem =
-            2 * std::size_t(wide_smem_words) * 8 + std::size_t(dev::kWWarps) * dev::kQueue * 12;
+        const int wide_max_classes = P.wide_max_classes;
+        const std::size_t wide_smem = 2 * std::size_t(wide_smem_words) * 8 +
+                                      std::size_t(dev::kWWarps) * dev::kQueue * 16 +
+                                      2 * std::size_t(wide_max_classes) * sizeof(dev::ClassRun) +
+                                      2 * std::size_t(wide_max_classes + 1) * 4;
         const std::size_t narrow_smem = std::size_t(dev::kNarrowTableWords + dev::kAffWords) * 8 +
                                         std::size_t(dev::kNWarps) * dev::kQueue * 12;
         int wide_grid = 0, narrow_grid = 0;
@@ -1627,7 +1686,7 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
             if (wide_grid) {
                 dev::wide_kernel<<<wide_grid, dev::kWThreads, wide_smem, stream>>>(
                     d_wide.p, d_witems.p, int(P.wide_items.size()), d_rows.p, d_aff.p, d_cls.p,
-                    d_inv.p, cand, out, wide_smem_words, d_counters.p + 1);
+                    d_inv.p, cand, out, wide_smem_words, wide_max_classes, d_counters.p + 1);
                 check_cuda(cudaGetLastError(), "wide_kernel launch");
             }
             record(ev[3], stream);
