@@ -32,9 +32,7 @@ constexpr int kWMaxSmemWords = 3300;                    // staged row words per 
 constexpr long long kWHugeWords = 1LL << 17;            // rows this long use one buffer of
                                                         // twice the size (stronger moduli)
 constexpr int kQueue = 64;
-constexpr int kClassBits = 8;
-constexpr int kMaxClasses = kMaxFastClasses;
-constexpr long long kMaxClassWords = 1LL << 23;         // class word index fits 24 bits
+constexpr long long kMaxClassWords = 1LL << 23;         // class words of a row (sweep-item arithmetic)
 constexpr int kAdmQ = 16;                               // residue words for class primes <= 13
 constexpr int kNarrowSlots = 8;
 constexpr int kNK = 4;                                  // consecutive row words per lane
@@ -47,7 +45,6 @@ constexpr int kRefWords = 8;                            // u64 words of a bitmas
 constexpr int kMaxFactors = 4;
 constexpr int kMaxIntervals = 8;                        // more: sweep the whole row
 
-static_assert(kMaxClasses <= (1 << kClassBits), "class index must fit the queue entry");
 
 struct Modulus {                   // one stage-1 modulus of a wide curve (class layout)
     long long offset;              // word offset of row 0 in the table pool
@@ -855,91 +852,91 @@ __global__ void __launch_bounds__(kNThreads, 3)
             const int jn = min(kND, item.count - idx0);
             u32 rho[kNarrowSlots];
             for (int j = 0; j < jn; ++j) {
-            const long long k = item.first + idx0 + j;
-            const long long d = C.square ? k * k : k;
-            const u32 du = u32(d);
-            // d mod m for every modulus: reduced for the first parameter of the
-            // fetch (and for square denominators), else advanced by one
-#pragma unroll
-            for (int s = 0; s < kNarrowSlots; ++s) {
-                if (j == 0 || C.square) {
-                    rho[s] = mod_u32(du, u32(C.m[s]), C.magic[s]);
-                } else {
-                    rho[s] += 1;
-                    if (rho[s] == u32(C.m[s])) rho[s] = 0;
-                }
-            }
-            const u64 mask2 = C.dense2[du & 63];
-            if (!mask2) continue;
-            // words [w_lo, w_hi] hold the numerator range of this item: a in [L, U]
-            long long L = -C.bound, U = C.bound;
-            if (C.nint > 0 && !x_range(C.lo, C.hi, C.nint, C.bound, d, item.range, L, U)) continue;
-            const int w_lo = int((L + C.bound) >> 6), w_hi = int((U + C.bound) >> 6);
-            const u64 first_mask = ~u64(0) << ((L + C.bound) & 63);
-            const int last_bits = int((U + C.bound) & 63) + 1;
-            const u64 last_mask = last_bits >= 64 ? ~u64(0) : ((u64(1) << last_bits) - 1);
-            // lane l takes words w0 + kNK l .. w0 + kNK l + kNK - 1 of each
-            // 128-word step: rows repeat their first kNK - 1 words, so the kNK
-            // words of a lane never wrap and one index per modulus advances
-            u32 base[kNarrowSlots], at[kNarrowSlots], mods[kNarrowSlots], steps[kNarrowSlots];
-#pragma unroll
-            for (int s = 0; s < kNarrowSlots; ++s) {
-                const u32 m = u32(C.m[s]);
-                mods[s] = m;
-                steps[s] = C.step[s];
-                base[s] = u32(C.off[s]) + rho[s] * u32(C.len[s]);
-                at[s] = mod_u32(C.shift[s] + u32(w_lo + kNK * lane), m, C.magic[s]);
-            }
-            bool selected = false;
-            int qn = 0;
-            for (int w0 = w_lo; w0 <= w_hi; w0 += kWarpSize * kNK) {
-                u64 acc[kNK];
-#pragma unroll
-                for (int k = 0; k < kNK; ++k) acc[k] = mask2;
+                const long long k = item.first + idx0 + j;
+                const long long d = C.square ? k * k : k;
+                const u32 du = u32(d);
+                // d mod m for every modulus: reduced for the first parameter of the
+                // fetch (and for square denominators), else advanced by one
 #pragma unroll
                 for (int s = 0; s < kNarrowSlots; ++s) {
-                    const u64 *row = tab + base[s] + at[s];
-#pragma unroll
-                    for (int k = 0; k < kNK; ++k) acc[k] &= row[k];
-                    const u32 t = at[s] + steps[s];  // advance 32 kNK words mod m
-                    at[s] = min(t, t - mods[s]);
-                }
-                const int wl = w0 + kNK * lane;
-#pragma unroll
-                for (int k = 0; k < kNK; ++k) {
-                    const int w = wl + k;
-                    if (w > w_hi) acc[k] = 0;
-                    if (w == w_lo) acc[k] &= first_mask;
-                    if (w == w_hi) acc[k] &= last_mask;
-                }
-                if (!__ballot_sync(kFullMask, (acc[0] | acc[1] | acc[2] | acc[3]) != 0)) continue;
-#pragma unroll
-                for (int k = 0; k < kNK; ++k) {
-                    const u32 b = __ballot_sync(kFullMask, acc[k] != 0);
-                    if (!b) continue;
-                    const int pos = qn + __popc(b & lanemask_lt());
-                    if (acc[k]) {
-                        wq_mask[pos] = acc[k];
-                        wq_word[pos] = u32(wl + k);
+                    if (j == 0 || C.square) {
+                        rho[s] = mod_u32(du, u32(C.m[s]), C.magic[s]);
+                    } else {
+                        rho[s] += 1;
+                        if (rho[s] == u32(C.m[s])) rho[s] = 0;
                     }
-                    qn += __popc(b);
-                    if (qn >= 32) {
-                        if (!selected) {
-                            select_warp(du, cand, inv_table, w_ci, w_dinv);
-                            selected = true;
+                }
+                const u64 mask2 = C.dense2[du & 63];
+                if (!mask2) continue;
+                // words [w_lo, w_hi] hold the numerator range of this item: a in [L, U]
+                long long L = -C.bound, U = C.bound;
+                if (C.nint > 0 && !x_range(C.lo, C.hi, C.nint, C.bound, d, item.range, L, U)) continue;
+                const int w_lo = int((L + C.bound) >> 6), w_hi = int((U + C.bound) >> 6);
+                const u64 first_mask = ~u64(0) << ((L + C.bound) & 63);
+                const int last_bits = int((U + C.bound) & 63) + 1;
+                const u64 last_mask = last_bits >= 64 ? ~u64(0) : ((u64(1) << last_bits) - 1);
+                // lane l takes words w0 + kNK l .. w0 + kNK l + kNK - 1 of each
+                // 128-word step: rows repeat their first kNK - 1 words, so the kNK
+                // words of a lane never wrap and one index per modulus advances
+                u32 base[kNarrowSlots], at[kNarrowSlots], mods[kNarrowSlots], steps[kNarrowSlots];
+#pragma unroll
+                for (int s = 0; s < kNarrowSlots; ++s) {
+                    const u32 m = u32(C.m[s]);
+                    mods[s] = m;
+                    steps[s] = C.step[s];
+                    base[s] = u32(C.off[s]) + rho[s] * u32(C.len[s]);
+                    at[s] = mod_u32(C.shift[s] + u32(w_lo + kNK * lane), m, C.magic[s]);
+                }
+                bool selected = false;
+                int qn = 0;
+                for (int w0 = w_lo; w0 <= w_hi; w0 += kWarpSize * kNK) {
+                    u64 acc[kNK];
+#pragma unroll
+                    for (int k = 0; k < kNK; ++k) acc[k] = mask2;
+#pragma unroll
+                    for (int s = 0; s < kNarrowSlots; ++s) {
+                        const u64 *row = tab + base[s] + at[s];
+#pragma unroll
+                        for (int k = 0; k < kNK; ++k) acc[k] &= row[k];
+                        const u32 t = at[s] + steps[s];  // advance 32 kNK words mod m
+                        at[s] = min(t, t - mods[s]);
+                    }
+                    const int wl = w0 + kNK * lane;
+#pragma unroll
+                    for (int k = 0; k < kNK; ++k) {
+                        const int w = wl + k;
+                        if (w > w_hi) acc[k] = 0;
+                        if (w == w_lo) acc[k] &= first_mask;
+                        if (w == w_hi) acc[k] &= last_mask;
+                    }
+                    if (!__ballot_sync(kFullMask, (acc[0] | acc[1] | acc[2] | acc[3]) != 0)) continue;
+#pragma unroll
+                    for (int k = 0; k < kNK; ++k) {
+                        const u32 b = __ballot_sync(kFullMask, acc[k] != 0);
+                        if (!b) continue;
+                        const int pos = qn + __popc(b & lanemask_lt());
+                        if (acc[k]) {
+                            wq_mask[pos] = acc[k];
+                            wq_word[pos] = u32(wl + k);
                         }
-                        __syncwarp();
-                        narrow_drain(wq_mask, wq_word, qn - 32, 32, C, cand, s_aff, w_ci, w_dinv, d,
-                                     out);
-                        qn -= 32;
+                        qn += __popc(b);
+                        if (qn >= 32) {
+                            if (!selected) {
+                                select_warp(du, cand, inv_table, w_ci, w_dinv);
+                                selected = true;
+                            }
+                            __syncwarp();
+                            narrow_drain(wq_mask, wq_word, qn - 32, 32, C, cand, s_aff, w_ci, w_dinv, d,
+                                         out);
+                            qn -= 32;
+                        }
                     }
                 }
-            }
-            if (qn) {
-                if (!selected) select_warp(du, cand, inv_table, w_ci, w_dinv);
-                __syncwarp();
-                narrow_drain(wq_mask, wq_word, 0, qn, C, cand, s_aff, w_ci, w_dinv, d, out);
-            }
+                if (qn) {
+                    if (!selected) select_warp(du, cand, inv_table, w_ci, w_dinv);
+                    __syncwarp();
+                    narrow_drain(wq_mask, wq_word, 0, qn, C, cand, s_aff, w_ci, w_dinv, d, out);
+                }
             }
         }
         __syncthreads();

@@ -45,13 +45,10 @@ constexpr int kFSteps = 4;                                 // steps per work ite
 constexpr int kFItemWords = kWarpSize * kFK * kFSteps;     // 512 words per item
 constexpr int kFExt = kWarpSize * (kFK - 1);               // row extension
 constexpr int kFQueue = 64;
-constexpr int kFClassBits = 8;                             // up to 256 classes
-constexpr int kFMaxClasses = kMaxFastClasses;
-constexpr long long kFMaxClassWords = 1LL << 23;           // word offset fits 24 bits
+constexpr long long kFMaxClassWords = 1LL << 23;           // class words of a launch's tile (24-bit field)
 constexpr int kFAdmQ = 16;                                 // admissible-residue words for q <= 13
 constexpr int kFStage2Group = 8;                           // stage-2 primes loaded together
 
-static_assert(kFMaxClasses <= (1 << kFClassBits), "class index must fit the queue entry");
 
 struct FastModulus {
     int m;                         // modulus (odd, prime to the class modulus)
