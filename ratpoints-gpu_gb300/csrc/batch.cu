@@ -1094,6 +1094,8 @@ struct CurveWork {
     long long swept = 0;       // words a denominator sweeps after interval narrowing (estimate)
     long long count = 0;       // parameters
     dev::u64 adm2[64] = {};    // 2-adic admissible classes by d mod 64
+    int classes = 1;           // wide curves: most numerator classes of one denominator
+    std::unique_ptr<FastPlanner> planner;  // wide curves, until planned
     std::vector<unsigned short> cand_residues;  // c_i mod p for the 36 candidates, candidate-major
 };
 
@@ -1165,10 +1167,53 @@ FastPlan narrow_plan(const std::vector<std::string> &coefficients) {
 
 // Wide plan: moduli capped so that tables stay small against the curve's
 // work, and the staged rows fit the shared-memory budget.
-FastPlan wide_plan(const std::vector<std::string> &coefficients, long long bound, long double work,
-                   int smem_budget) {
+// Staged row words a wide curve may use (both buffers together) so that a
+// CTA stays within a third of an SM's shared memory: static arrays, queues,
+// and two sets of class runs and item prefixes for max_classes classes.
+long long wide_row_budget(int max_classes) {
+    const long long per_cta = 228 * 1024 / 3 - 1024;
+    const long long fixed = 8 * 1024 +  // static shared memory of the kernel (7.6 KB) and slack
+                            (long long)dev::kWWarps * dev::kQueue * 16 +
+                            2LL * max_classes * (long long)sizeof(dev::ClassRun) + 2LL * (max_classes + 1) * 4;
+    return std::max(2LL * 64, (per_cta - fixed) / 8);
+}
+
+// Admissible residues mod the class prime q by d mod q: bit r of out[dq] is
+// set iff f(r / dq) is a square mod q, or (q | d) r != 0 and c_n is a square.
+void class_prime_residues(const std::vector<std::string> &coefficients, int q, dev::u64 *out) {
+    const auto aff = affine_mask(q, coefficients);
+    const bool lead = lead_is_square(coefficients, q);
+    for (int dq = 0; dq < q; ++dq) {
+        out[dq] = 0;
+        for (int r = 0; r < q; ++r) {
+            const bool ok = dq == 0 ? (r != 0 && lead) : aff[(r * mod_inverse(dq, q)) % q] != 0;
+            if (ok) out[dq] |= dev::u64(1) << r;
+        }
+    }
+}
+
+// Most numerator classes of any one denominator of a wide curve: admissible
+// 2-adic classes times admissible residues of the class prime.
+int wide_classes(const std::vector<std::string> &coefficients, const dev::u64 adm2[64], int q) {
+    int most2 = 0, mostq = 1;
+    for (int dd = 0; dd < 64; ++dd) most2 = std::max(most2, __builtin_popcountll(adm2[dd]));
+    if (q > 1) {
+        dev::u64 admq[13];
+        class_prime_residues(coefficients, q, admq);
+        mostq = 0;
+        for (int dq = 0; dq < q; ++dq) mostq = std::max(mostq, __builtin_popcountll(admq[dq]));
+    }
+    return most2 * std::max(1, mostq);
+}
+
+// max_classes: the most classes of any wide curve in the launch, which sizes
+// the launch's class arrays and so this curve's share of shared memory.
+FastPlan wide_plan(const FastPlanner &planner, long double work, bool huge_rows, int max_classes) {
     int cap = int(std::min<long double>(kMaxModulus, std::max<long double>(64, std::sqrt(work / 48.0L))));
-    const FastPlanner planner(coefficients, bound, true);
+    const long long both = wide_row_budget(max_classes);
+    // two row buffers, or one twice as large for huge rows
+    const long long smem_budget = std::min<long long>(huge_rows ? 2 * dev::kWMaxSmemWords : dev::kWMaxSmemWords,
+                                                      huge_rows ? both : both / 2);
     for (;;) {
         FastPlan plan = planner.plan(cap);
         long long smem = 0;
@@ -1229,12 +1274,13 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             cw.count = c.last >= c.first ? c.last - c.first + 1 : 0;
             cw.swept = swept_row_words(c, cw.words);
             cw.wide = cw.swept >= kBatchWideWords;
-            if (cw.wide)
-                cw.plan = wide_plan(c.coefficients, c.bound, (long double)cw.words * cw.count,
-                                    cw.words >= dev::kWHugeWords ? 2 * dev::kWMaxSmemWords
-                                                                 : dev::kWMaxSmemWords);
-            else cw.plan = narrow_plan(c.coefficients);
             two_adic_classes(c.coefficients, cw.adm2);
+            if (cw.wide) {
+                cw.planner.reset(new FastPlanner(c.coefficients, c.bound, true));
+                cw.classes = wide_classes(c.coefficients, cw.adm2, cw.planner->class_prime());
+            } else {
+                cw.plan = narrow_plan(c.coefficients);
+            }
             {
                 const auto &cps = candidate_primes();
                 cw.cand_residues.reserve(kCandidatePrimes * c.coefficients.size());
@@ -1242,14 +1288,27 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                     for (const auto &coef : c.coefficients)
                         cw.cand_residues.push_back((unsigned short)decimal_mod(coef, cps[ci]));
             }
-            r.wide = cw.wide;
-            r.class_prime = cw.plan.class_prime;
-            r.moduli = cw.plan.moduli;
             cw.ok = true;
         } catch (const std::exception &e) {
             r.status = 1;
             r.error = e.what();
         }
+    });
+    // wide plans: one row budget for the launch, from its largest class count
+    int max_classes = 1;
+    for (const CurveWork &cw : P.work)
+        if (cw.ok && cw.wide) max_classes = std::max(max_classes, cw.classes);
+    parallel_for(curves.size(), [&](std::size_t i) {
+        CurveWork &cw = P.work[i];
+        if (!cw.ok) return;
+        if (cw.wide) {
+            cw.plan = wide_plan(*cw.planner, (long double)cw.words * cw.count, cw.words >= dev::kWHugeWords,
+                                max_classes);
+            cw.planner.reset();
+        }
+        results[i].wide = cw.wide;
+        results[i].class_prime = cw.plan.class_prime;
+        results[i].moduli = cw.plan.moduli;
     });
 
     const auto &cands = candidate_primes();
@@ -1370,28 +1429,12 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             P.wide_smem_words =
                 std::max(P.wide_smem_words, round_even(C.nbuf == 2 ? smem : (smem + 1) / 2));
             std::copy(cw.adm2, cw.adm2 + 64, C.admissible);
-            {
-                int most2 = 0;
-                for (auto m : cw.adm2) most2 = std::max(most2, __builtin_popcountll(m));
-                P.wide_max_classes = std::max(P.wide_max_classes, most2);  // times mod-q residues below
-            }
+            P.wide_max_classes = std::max(P.wide_max_classes, cw.classes);
             if (q > 1) {
-                const auto aff = affine_mask(q, c.coefficients);
-                const bool lead = lead_is_square(c.coefficients, q);
-                for (int dq = 0; dq < q; ++dq)
-                    for (int r = 0; r < q; ++r) {
-                        const bool ok = dq == 0 ? (r != 0 && lead)
-                                                : aff[(r * mod_inverse(dq, q)) % q] != 0;
-                        if (ok) C.admissible[64 + dq] |= dev::u64(1) << r;
-                    }
+                class_prime_residues(c.coefficients, q, C.admissible + 64);
                 for (int a = 0; a < q; ++a)
                     for (int rq = 0; rq < q; ++rq)
                         C.crt[a * 13 + rq] = (unsigned char)(((rq - a + q) % q) * C.inv64_q % q);
-                int most2 = 0, mostq = 0;
-                for (auto m : cw.adm2) most2 = std::max(most2, __builtin_popcountll(m));
-                for (int dq = 0; dq < q; ++dq)
-                    mostq = std::max(mostq, __builtin_popcountll(C.admissible[64 + dq]));
-                P.wide_max_classes = std::max(P.wide_max_classes, most2 * std::max(1, mostq));
             }
             for (int r64 = 0; r64 < 64; ++r64) C.mod_q[r64] = (unsigned char)(q > 1 ? r64 % q : 0);
             // class starts for every residue r mod M: ofs = (r + H) mod M, and per
