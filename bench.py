@@ -365,6 +365,40 @@ def restricted_benchmark(rpg, high_degree=256, cubics=32, plain_cubics=8):
     return out
 
 
+def dense_curve_benchmark(rpg, height=10 ** 7):
+    """The record curve (a dense curve: squares modulo most small primes, so
+    many modular survivors) over a in [-H, H], b in [1, H] through the command
+    line, with device pre-verification (default) and with every modular
+    survivor checked on the host (--host-verify-only), both plans.  Each run's
+    stdout SHA-256 is compared with the reference's published full-box output
+    at H = 10^7."""
+    import hashlib
+    import workloads
+
+    golden = json.loads((Path(__file__).resolve().parent / "tests" / "golden" / "golden.json").read_text())
+    expected = next((g["sha256"] for g in golden["record_full"]
+                     if g["height"] == height and g["last"] == height), None)
+    rect = (2 * height + 1) * height
+    reduced = workloads.reduced_sites(height, 1, height, workloads.mobius(height))
+    runs = {}
+    for plan in ("fast", "reference"):
+        for mode, extra in (("device_preverify", []), ("host_verify_only", ["--host-verify-only"])):
+            t0 = time.perf_counter()
+            result = rpg.cli([workloads.RECORD_CURVE, height, "-v", "--sieve-plan", plan, *extra])
+            wall = time.perf_counter() - t0
+            m = rpg.parse_metrics(result.stderr) or {}
+            runs[f"{plan}/{mode}"] = {
+                "exit": result.returncode, "wall_s": wall, "value": reduced / wall / 1e9, "unit": UNIT,
+                "internal_wall_ms": m.get("wall_ms"), "verification_ms": m.get("verification_ms"),
+                "sieve_ms": m.get("sieve_ms"), "modular_survivors": m.get("survivors"),
+                "exact_survivors": m.get("exact_survivors"),
+                "sha256_matches_reference": hashlib.sha256(result.stdout).hexdigest() == expected}
+    return {"workload": f"record curve, a in [-{height:g}, {height:g}], b in [1, {height:g}], "
+                        "default output, through the ratpoints_gpu command line (process start, "
+                        "table build, sieve, verification and output)",
+            "reduced_sites": reduced, "rectangle_sites": rect, "runs": runs}
+
+
 def serving_benchmark(rpg, count=1000, rate=200.0, lanes=2, check=40):
     """Poisson stream of requests into the serving loop: per-request latency
     (submit -> answer) percentiles and aggregate throughput over the stream."""
@@ -455,6 +489,8 @@ def main():
                         help="square-denominator cubics of the restricted searches (0: skip)")
     parser.add_argument("--serving-requests", type=int, default=1000,
                         help="requests of the serving stream (0: skip)")
+    parser.add_argument("--dense-height", type=int, default=10 ** 7,
+                        help="record-curve box height for the pre-verification runs (0: skip)")
     args = parser.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -584,6 +620,8 @@ def main():
         line["restricted"] = restricted_benchmark(rpg, args.restricted, args.square_cubics)
     if args.serving_requests > 0:
         line["serving"] = serving_benchmark(rpg, args.serving_requests)
+    if args.dense_height > 0:
+        line["dense_curve"] = dense_curve_benchmark(rpg, args.dense_height)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(coeffs, seconds=args.cpu_seconds)
     print(json.dumps(line))

@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define RPG_ABI_VERSION 1
+#define RPG_ABI_VERSION 2
 
 typedef enum rpg_status {
     RPG_OK = 0,
@@ -60,6 +60,8 @@ typedef struct rpg_sieve_stats {
     double initial_mask_bytes;
     uint64_t h2d_bytes;        /* host-to-device bytes copied */
     uint64_t d2h_bytes;        /* device-to-host bytes copied */
+    uint64_t host_candidates;  /* survivors handed to the host's exact check (after device
+                                  pre-verification; survivor_count without it) */
 } rpg_sieve_stats;
 
 /* Receives one batch of modular survivors (structure of arrays).  The arrays
@@ -105,7 +107,16 @@ typedef struct rpg_search_options {
     int32_t plan;                     /* RPG_PLAN_REFERENCE or RPG_PLAN_FAST */
     int32_t device;                   /* CUDA device ordinal, -1: current */
     int32_t verify_threads;           /* host verification threads, 0: all cores */
+    uint32_t flags;                   /* RPG_SEARCH_* bits */
 } rpg_search_options;
+
+/* rpg_search_options.flags.  By default a kernel drops, before the copy to the
+ * host, the survivors that fail gcd(a, d) = 1 or a residue test of F(a, d)
+ * (mod 2^64, the primes 3..97 and four primes below 2^31): no point fails
+ * them, so the reported points are the same; the survivor count stays the
+ * modular one.  This flag sends every modular survivor to the host instead,
+ * as the reference does (src/point_search.cpp:48-60). */
+#define RPG_SEARCH_HOST_VERIFY_ONLY 1u
 
 /* One verified point (numerator : ordinate : denominator); the ordinate is
  * the non-negative root in decimal, valid only during the call.  Return
@@ -132,6 +143,13 @@ rpg_status rpg_is_squarefree(const char *const *coefficients, int32_t coefficien
 rpg_status rpg_square_root(const char *const *coefficients, int32_t coefficient_count,
                            int64_t numerator, int64_t denominator, char *ordinate,
                            size_t ordinate_capacity, int32_t *is_point);
+
+/* The device pre-verification test of one site, evaluated on the host:
+ * *may_be_point = 0 iff gcd(a, d) != 1 or F(a, d) fails a residue test that
+ * every square passes (mod 2^64, the primes 3..97, four primes below 2^31).
+ * No counterpart in the reference. */
+rpg_status rpg_preverify(const char *const *coefficients, int32_t coefficient_count, int64_t numerator,
+                         int64_t denominator, int32_t *may_be_point);
 
 /* The ratpoints_gpu command line in-process (src/main.cpp:48-85): writes to
  * stdout/stderr and returns the exit status. */
@@ -201,6 +219,7 @@ rpg_status rpg_session_sieve_noalloc(rpg_session *session, int32_t first, int32_
  * argument, a negative count, or a device error.
  */
 #define RPG_BATCH_NO_GRAPH 1u /* launch the batch's kernels directly, not as a CUDA graph */
+#define RPG_BATCH_HOST_VERIFY_ONLY 2u /* no device pre-verification (see RPG_SEARCH_HOST_VERIFY_ONLY) */
 
 typedef struct rpg_batch_stats {
     uint64_t curves;           /* curves searched (valid, with denominators) */
@@ -224,6 +243,7 @@ typedef struct rpg_batch_stats {
     uint64_t h2d_bytes;
     uint64_t d2h_bytes;
     int32_t graph;             /* nonzero if the kernels ran as a CUDA graph */
+    uint64_t host_candidates;  /* survivors given to the host's exact check */
 } rpg_batch_stats;
 
 typedef int (*rpg_batch_point_cb)(int32_t curve, int64_t numerator, const char *ordinate,

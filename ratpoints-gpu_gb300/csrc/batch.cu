@@ -14,23 +14,23 @@
 
 #include "exact.hpp"
 #include "plan.hpp"
+#include "preverify.hpp"
 #include "sieve.hpp"
 #include "sieve_device.cuh"
 
 namespace rpg {
 namespace dev {
 
-constexpr int kWideSlots = kMaxFastSlots;          // stage-1 moduli of a wide curve (padded)
+constexpr int kWideSlots = 6;                      // stage-1 moduli of a wide curve (padded)
 constexpr int kWK = 4;                             // words per lane per step (lanes 32 apart)
-constexpr int kWWarps = 8;
+constexpr int kWWarps = 12;                        // warp 0 produces, the others sweep
 constexpr int kWThreads = kWWarps * kWarpSize;
+constexpr int kWConsumers = kWWarps - 1;
 constexpr int kWSteps = 4;
 constexpr int kWItemWords = kWarpSize * kWK * kWSteps;  // class words per sweep item
 constexpr int kWExt = kWarpSize * (kWK - 1);            // row extension
-constexpr int kWMaxSmemWords = 3300;                    // staged row words per buffer (two
-                                                        // buffers, 3 CTAs per SM)
-constexpr long long kWHugeWords = 1LL << 17;            // rows this long use one buffer of
-                                                        // twice the size (stronger moduli)
+constexpr int kWMaxSmemWords = 6000;                    // staged row words per slot (two
+                                                        // slots, 2 CTAs per SM)
 constexpr int kQueue = 64;
 constexpr long long kMaxClassWords = 1LL << 23;         // class words of a row (sweep-item arithmetic)
 constexpr int kAdmQ = 16;                               // residue words for class primes <= 13
@@ -63,6 +63,11 @@ struct WideCurve {
     long long count_q;             // 2H = count_q M + count_r
     long long aff;                 // u64 offset of the 36 candidate bitmasks
     long long cls;                 // index of the curve's ClassStart[M] block
+    // class lists by denominator class k = (d mod 64) q + (d mod q): counts at
+    // list_count + k, runs at list_runs + k list_max, item prefixes at
+    // list_prefix + k (list_max + 1); list_count = -1 for curves with x
+    // intervals (their classes are clipped per denominator)
+    long long list_count, list_runs, list_prefix;
     Modulus mod[kWideSlots];
     u64 admissible[64 + kAdmQ];    // 2-adic classes by d mod 64, residues mod q by d mod q
     int count_r;
@@ -71,7 +76,7 @@ struct WideCurve {
     int h_mod_m;                   // H mod M
     int inv64_q;                   // 64^-1 mod q (CRT)
     int smem_words;
-    int nbuf;                      // row buffers: 2 (the next row copied during a sweep) or 1
+    int list_max;                  // class-list stride: most classes of one denominator
     int square;
     int index;                     // position in the caller's curve list
     unsigned short neg_h[kCandidatePrimes];   // (-H) mod p
@@ -269,9 +274,10 @@ __global__ void composite_kernel(const CompositeSpec *specs, int nspecs, const u
 
 // The 32 largest candidates not dividing d with 1/d mod p, by one warp: lane l
 // tests candidate 35 - l, lanes 0..3 also candidate 3 - l.
+template <typename Index, typename Inverse>
 __device__ __forceinline__ void select_warp(u32 du, const Candidates &cand,
-                                            const unsigned short *inv_table, int *s_ci,
-                                            u32 *s_dinv) {
+                                            const unsigned short *inv_table, Index *s_ci,
+                                            Inverse *s_dinv) {
     const int lane = threadIdx.x & 31;
     const int ch = kCandidatePrimes - 1 - lane;
     const u32 rh = mod_small(du, u32(cand.p[ch]), cand.magic[ch]);
@@ -282,13 +288,13 @@ __device__ __forceinline__ void select_warp(u32 du, const Candidates &cand,
     const u32 below = lanemask_lt();
     const int rank_h = lane - __popc(hi_div & below);
     if (rh != 0 && rank_h < kSelectedPrimes) {
-        s_ci[rank_h] = ch;
-        s_dinv[rank_h] = __ldg(inv_table + cand.p[ch] * kMaximumPrime + rh);
+        s_ci[rank_h] = static_cast<Index>(ch);
+        s_dinv[rank_h] = static_cast<Inverse>(__ldg(inv_table + cand.p[ch] * kMaximumPrime + rh));
     }
     const int rank_l = 32 - __popc(hi_div) + lane - __popc(lo_div & below);
     if (lane < kCandidatePrimes - 32 && rl != 0 && rank_l < kSelectedPrimes) {
-        s_ci[rank_l] = cl;
-        s_dinv[rank_l] = __ldg(inv_table + cand.p[cl] * kMaximumPrime + rl);
+        s_ci[rank_l] = static_cast<Index>(cl);
+        s_dinv[rank_l] = static_cast<Inverse>(__ldg(inv_table + cand.p[cl] * kMaximumPrime + rl));
     }
     __syncwarp();
 }
@@ -348,20 +354,31 @@ __device__ __forceinline__ void emit(u64 m, long long base, long long step, long
 }
 
 // ---------------------------------------------------------------------------
-// Wide rows: class layout, one CTA per denominator.
+// Wide rows: class layout, warp-specialized like the single-curve fast
+// kernel.  Warp 0 produces denominators into two slots: it takes work items
+// (curve, parameter range, numerator range) from the device queue, skips
+// parameters without admissible classes, selects the 32 reference primes
+// with 1/d mod p, points the slot at the curve's class list for the
+// denominator's class k = (d mod 64) q + (d mod q) (or, for curves with x
+// intervals, lays out the classes clipped to the numerator range in shared
+// memory), and copies the curve's stage-1 rows into the slot by TMA.  The
+// other warps sweep each filled slot's items and release it; queued words
+// carry a private context (curve, d, primes), so they wait past later
+// denominators and curves.  No barrier spans the CTA.
 
-// One admissible class of one denominator: words [wbase, wbase + words) of
-// the class hold its sites in the numerator range being swept; the first
-// word drops its `first` low bits, the last keeps its `last` low bits.
-struct ClassRun {
+// One class of one denominator in the numerator range being swept: class
+// words [wbase, wbase + words); the first word drops its `first` low bits,
+// the last keeps its `last` low bits; start[sl] is the row index of class word
+// wbase for modulus sl.
+struct WideRun {
     int wbase;
     int words;
-    unsigned short r;              // class residue mod M
     unsigned short ofs;            // (r + H) mod M: the class's least a is -H + ofs
     unsigned char first;
-    unsigned char last;
-    unsigned short pad;
+    unsigned char last;            // 1..64
+    unsigned short start[kWideSlots];
 };
+static_assert(sizeof(WideRun) == 24, "packed class run");
 
 // Per curve and class residue r mod M (precomputed on the host): the row
 // index of class word 0 for each modulus, (a0 S^-1) mod m with a0 = -H + ofs.
@@ -372,22 +389,35 @@ struct ClassStart {
 };
 static_assert(sizeof(ClassStart) == 16, "one 16-byte load per class");
 
-// A denominator a warp still has queued words of (wide kernel): its prime
-// selection and 1/d mod p, copied from the CTA's set so that the words can
-// wait in the queue past later denominators of the same curve.
+// A denominator in flight: written by the producer warp, read by the others.
+struct WideSlot {
+    long long d;                   // -1: no more work
+    const WideRun *runs;           // class list (global) or laid-out runs (shared)
+    const int *prefix;             // sweep-item prefix of the runs
+    int curve;
+    int nclass;
+    int next;                      // sweep-item counter
+    int pad;
+    unsigned char sel[kSelectedPrimes];
+    unsigned short dinv[kSelectedPrimes];
+};
+
+// A denominator a consumer warp still has queued words of.
 constexpr int kWCtx = 4;
 struct WideCtx {
     int d;
+    int curve;
     unsigned char sel[kSelectedPrimes];
     unsigned short dinv[kSelectedPrimes];
 };
 
 // Stage 2 and emission for up to 32 queued words.  A queued word carries its
 // context (bits 56..57) and the position pos = a + H of its bit 0 (bits
-// 0..55); its sites are a = -H + pos + M j.
+// 0..55); its sites are a = -H + pos + M j.  The curve's descriptor and
+// bitmasks are read through the read-only cache.
 __device__ __forceinline__ void wide_drain(const u64 *qmask, const u64 *qpos, int start, int n,
-                                           const WideCurve &C, const Candidates &cand,
-                                           const u64 *s_aff, const WideCtx *ctx,
+                                           const WideCurve *curves, const u64 *affine,
+                                           const Candidates &cand, const WideCtx *ctx,
                                            const BatchOut &out) {
     const int lane = threadIdx.x & 31;
     u64 m = 0, pos = 0;
@@ -397,358 +427,386 @@ __device__ __forceinline__ void wide_drain(const u64 *qmask, const u64 *qpos, in
     }
     __syncwarp();
     const WideCtx &X = ctx[int(pos >> 56) & (kWCtx - 1)];
+    const WideCurve *Cg = curves + (lane < n ? X.curve : 0);
     const u64 p56 = pos & ((u64(1) << 56) - 1);
     const u32 hi = u32(p56 >> 16), lo = u32(p56 & 0xFFFF);
-    for (int s = 0; s < kSelectedPrimes && m; ++s) {
-        const int ci = X.sel[s];
-        const u32 p = u32(cand.p[ci]), magic = cand.magic[ci];
-        const u32 dinv = X.dinv[s];
-        u32 r = mod_small(hi, p, magic);
-        r = mod_small((r << 16) | lo, p, magic);  // pos mod p
-        r += C.neg_h[ci];                          // a mod p
-        if (r >= p) r -= p;
-        const u32 x0 = mod_small(r * dinv, p, magic);
-        const u32 dx = mod_small(u32(C.m_mod[ci]) * dinv, p, magic);
-        const u64 *bits = s_aff + ci * kRefWords;
-        u64 rest = m;
-        while (rest) {
-            const int j = __ffsll((long long)rest) - 1;
-            rest &= rest - 1;
-            const u32 x = mod_small(x0 + u32(j) * dx, p, magic);
-            if (!((bits[x >> 6] >> (x & 63)) & 1)) m &= ~(u64(1) << j);
+    if (m) {
+        const u64 *aff = affine + __ldg(&Cg->aff);
+        for (int s = 0; s < kSelectedPrimes && m; ++s) {
+            const int ci = X.sel[s];
+            const u32 p = u32(cand.p[ci]), magic = cand.magic[ci];
+            const u32 dinv = X.dinv[s];
+            u32 r = mod_small(hi, p, magic);
+            r = mod_small((r << 16) | lo, p, magic);  // pos mod p
+            r += __ldg(&Cg->neg_h[ci]);               // a mod p
+            if (r >= p) r -= p;
+            const u32 x0 = mod_small(r * dinv, p, magic);
+            const u32 dx = mod_small(u32(__ldg(&Cg->m_mod[ci])) * dinv, p, magic);
+            const u64 *bits = aff + ci * kRefWords;
+            u64 rest = m;
+            while (rest) {
+                const int j = __ffsll((long long)rest) - 1;
+                rest &= rest - 1;
+                const u32 x = mod_small(x0 + u32(j) * dx, p, magic);
+                if (!((__ldg(bits + (x >> 6)) >> (x & 63)) & 1)) m &= ~(u64(1) << j);
+            }
         }
     }
-    emit(m, -C.bound + (long long)p56, C.class_mod, X.d, C.index, out);
+    const bool any = __any_sync(kFullMask, m != 0);
+    if (!any) return;
+    emit(m, -__ldg(&Cg->bound) + (long long)p56, __ldg(&Cg->class_mod), X.d, __ldg(&Cg->index), out);
 }
 
-// Wide rows, one CTA per denominator, software-pipelined over the
-// denominators of an item: while every warp sweeps denominator d_i (rows in
-// buffer b, class runs and prime selection in set s), warp 0 selects the
-// reference primes of the next live denominator d_j and warp 1 lays out its
-// classes into set s ^ 1, and thread 0 copies its rows into buffer b ^ 1
-// (TMA bulk copies, one mbarrier per buffer); one barrier per denominator.
-// Curves with huge rows use one row buffer of twice the size: their next
-// rows are copied after the barrier.
-__global__ void __launch_bounds__(kWThreads, 3)
+// Producer layout for curves with x intervals: denominator d's admissible
+// classes clipped to the item's numerator range, into runs / prefix in
+// shared memory (the whole warp; 32 classes per pass).
+__device__ __forceinline__ int wide_layout(const WideCurve &C, const ClassStart *cstart, u32 du,
+                                           long long d, int range, WideRun *runs, int *prefix) {
+    const int lane = threadIdx.x & 31;
+    const int q = C.class_prime;
+    const int M = C.class_mod;
+    const u64 classes2 = C.admissible[du & 63];
+    const u64 classesq = q > 1 ? C.admissible[64 + int(du % u32(q))] : u64(1);
+    const int nq = __popcll(classesq);
+    const int nclass = __popcll(classes2) * nq;
+    long long lo_a = -C.bound, hi_a = C.bound;
+    if (C.nint > 0) x_range(C.lo, C.hi, C.nint, C.bound, d, range, lo_a, hi_a);
+    int carry = 0;
+    for (int base = 0; base < nclass; base += 32) {
+        const int c = base + lane;
+        int nitems_c = 0;
+        if (c < nclass) {
+            const int r64 = nth_bit64(classes2, c / nq);
+            int r = r64;
+            if (q > 1) {
+                const int rq = nth_bit64(classesq, c % nq);
+                r = r64 + 64 * int(C.crt[C.mod_q[r64] * 13 + rq]);
+            }
+            const ClassStart cs = cstart[r];
+            const int ofs = cs.ofs;
+            // sites of class r: a = -H + ofs + M t, t in [0, count); those in
+            // [lo_a, hi_a] are t in [t_lo, t_hi]
+            const long long count = C.count_q + (ofs <= C.count_r ? 1 : 0);
+            const long long a0 = -C.bound + ofs;
+            const long long below = lo_a - a0;
+            const long long t_lo = below <= 0 ? 0 : (below + M - 1) / M;
+            const long long above = hi_a - a0;
+            const long long t_hi = above < 0 ? -1 : min(count - 1, above / M);
+            WideRun run;
+            run.ofs = (unsigned short)ofs;
+            if (t_lo <= t_hi) {
+                run.wbase = int(t_lo >> 6);
+                run.words = int((t_hi >> 6) - (t_lo >> 6) + 1);
+                run.first = (unsigned char)(t_lo & 63);
+                run.last = (unsigned char)((t_hi & 63) + 1);
+            } else {
+                run.wbase = 0;
+                run.words = 0;
+                run.first = 0;
+                run.last = 64;
+            }
+#pragma unroll
+            for (int sl = 0; sl < kWideSlots; ++sl)
+                run.start[sl] = (unsigned short)mod_u32(u32(cs.start[sl]) + u32(run.wbase), u32(C.mod[sl].m),
+                                                        C.mod[sl].magic);
+            runs[c] = run;
+            nitems_c = (run.words + kWItemWords - 1) / kWItemWords;
+        }
+        int incl = nitems_c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(kFullMask, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (c < nclass) prefix[c] = carry + incl - nitems_c;
+        carry += __shfl_sync(kFullMask, incl, 31);
+    }
+    if (lane == 0) prefix[nclass] = carry;
+    return nclass;
+}
+
+__global__ void __launch_bounds__(kWThreads, 2)
     wide_kernel(const WideCurve *__restrict__ curves, const BatchItem *__restrict__ items,
                 int nitems, const u64 *__restrict__ pool, const u64 *__restrict__ affine,
-                const ClassStart *__restrict__ class_starts,
+                const ClassStart *__restrict__ class_starts, const WideRun *__restrict__ list_runs,
+                const int *__restrict__ list_prefix, const int *__restrict__ list_count,
                 const unsigned short *__restrict__ inv_table, Candidates cand, BatchOut out,
                 int row_stride, int max_classes, unsigned long long *work) {
     extern __shared__ __align__(16) u64 smem[];
-    __shared__ WideCurve C;
-    __shared__ u64 s_aff[kAffWords];
-    __shared__ WideCtx s_ctx[kWWarps][kWCtx];
-    __shared__ int s_nclass[2];
-    __shared__ int s_ci[2][kSelectedPrimes];
-    __shared__ u32 s_dinv[2][kSelectedPrimes];
-    __shared__ int s_next[2];
-    __shared__ int s_item;
-    __shared__ int s_abort;
-    __shared__ __align__(8) unsigned long long s_bar[2];
+    u64 *qmask = smem + 2 * row_stride;
+    u64 *qpos = qmask + kWConsumers * kQueue;
+    WideRun *runs0 = reinterpret_cast<WideRun *>(qpos + kWConsumers * kQueue);  // [2][max_classes]
+    int *prefix0 = reinterpret_cast<int *>(runs0 + 2 * max_classes);            // [2][max_classes + 1]
+    __shared__ WideSlot slot[2];
+    __shared__ WideCtx s_ctx[kWConsumers][kWCtx];
+    __shared__ __align__(8) unsigned long long s_full[2];
+    __shared__ __align__(8) unsigned long long s_empty[2];
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    u64 *qmask = smem + 2 * row_stride;
-    u64 *qpos = qmask + kWWarps * kQueue;
-    ClassRun *runs0 = reinterpret_cast<ClassRun *>(qpos + kWWarps * kQueue);  // [2][max_classes]
-    int *prefix0 = reinterpret_cast<int *>(runs0 + 2 * max_classes);          // [2][max_classes + 1]
-    u64 *wq_mask = qmask + warp * kQueue;
-    u64 *wq_pos = qpos + warp * kQueue;
-    WideCtx *ctx = s_ctx[warp];
-    int qn = 0;       // queued words of this warp, kept across denominators of a curve
-    int seq = 0;      // denominators this CTA has swept
-    int oldest = 0;   // oldest context that may still have queued words
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_addr(&s_full[b]), 1);
+            mbar_init(smem_addr(&s_empty[b]), kWConsumers);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int i = threadIdx.x; i < kWConsumers * kWCtx; i += kWThreads) {
+        s_ctx[i / kWCtx][i % kWCtx].d = 1;
+        s_ctx[i / kWCtx][i % kWCtx].curve = 0;
+    }
+    __syncthreads();
+
+    if (warp == 0) {
+        // ---- producer ----
+        int b = 0, uses0 = 0, uses1 = 0;
+        bool failed = false;
+        BatchItem item{};
+        int i = 0, count = 0;
+        int q = 1, square = 0, nint = 0;
+        long long lists = -1;  // the item's curve's class-list offset (-1: laid out here)
+        unsigned long long magic_q = 0;
+        for (;;) {
+            long long d = -1;
+            int combo = 0, nlist = 0;
+            for (;;) {
+                if (i >= count) {
+                    int nxt = 0;
+                    if (lane == 0) nxt = int(atomicAdd(work, 1ull));
+                    nxt = __shfl_sync(kFullMask, nxt, 0);
+                    if (nxt >= nitems) break;
+                    item = items[nxt];
+                    i = 0;
+                    count = item.count;
+                    const WideCurve &C = curves[item.curve];
+                    q = C.class_prime;
+                    square = C.square;
+                    nint = C.nint;
+                    lists = C.list_count;
+                    magic_q = (~0ull) / u32(q) + 1;
+                    continue;
+                }
+                const long long k = item.first + i++;
+                const long long dd = square ? k * k : k;
+                const u32 du = u32(dd);
+                const int dq = q > 1 ? int(mod_u32(du, u32(q), magic_q)) : 0;
+                if (lists >= 0) {
+                    combo = int(du & 63) * q + dq;
+                    nlist = __ldg(list_count + lists + combo);
+                    if (nlist == 0) continue;
+                } else {
+                    const WideCurve &C = curves[item.curve];
+                    if (C.admissible[du & 63] == 0 || (q > 1 && C.admissible[64 + dq] == 0)) continue;
+                    long long L, U;
+                    if (nint > 0 && !x_range(C.lo, C.hi, nint, C.bound, dd, item.range, L, U)) continue;
+                }
+                d = dd;
+                break;
+            }
+            // slot b must be released by every consumer before it is refilled
+            const int used = b ? uses1 : uses0;
+            if (used > 0 && !mbar_wait(smem_addr(&s_empty[b]), u32(used - 1) & 1u)) {
+                failed = true;
+                break;
+            }
+            WideSlot &S = slot[b];
+            const u32 full = smem_addr(&s_full[b]);
+            if (d < 0) {
+                if (lane == 0) S.d = -1;
+                __syncwarp();
+                if (lane == 0) {
+                    __threadfence_block();
+                    mbar_arrive(full);
+                }
+                break;
+            }
+            const u32 du = u32(d);
+            const WideCurve &C = curves[item.curve];
+            select_warp(du, cand, inv_table, S.sel, S.dinv);
+            if (lists >= 0) {
+                if (lane == 0) {
+                    const int lm = C.list_max;
+                    S.runs = list_runs + C.list_runs + (long long)combo * lm;
+                    S.prefix = list_prefix + C.list_prefix + (long long)combo * (lm + 1);
+                    S.nclass = nlist;
+                }
+            } else {
+                WideRun *runs = runs0 + b * max_classes;
+                int *prefix = prefix0 + b * (max_classes + 1);
+                const int nclass = wide_layout(C, class_starts + C.cls, du, d, item.range, runs, prefix);
+                if (lane == 0) {
+                    S.runs = runs;
+                    S.prefix = prefix;
+                    S.nclass = nclass;
+                }
+            }
+            __syncwarp();
+            if (lane == 0) {
+                S.d = d;
+                S.curve = item.curve;
+                S.next = 0;
+                __threadfence_block();
+                fence_proxy_async_shared();
+                mbar_arrive_expect_tx(full, u32(C.smem_words) * 8u);
+                const u32 dst = smem_addr(smem + b * row_stride);
+#pragma unroll
+                for (int sl = 0; sl < kWideSlots; ++sl) {
+                    const Modulus &Md = C.mod[sl];
+                    const u32 rho = mod_u32(du, u32(Md.m), Md.magic);
+                    bulk_copy_to_shared(dst + u32(Md.smem_offset) * 8u,
+                                        pool + Md.offset + (long long)rho * Md.length,
+                                        u32(Md.length) * 8u, full);
+                }
+            }
+            __syncwarp();
+            if (b) ++uses1;
+            else ++uses0;
+            b ^= 1;
+        }
+        if (failed) {
+            if (out.error && lane == 0) atomicOr(out.error, 1ull);
+            // let the copies already issued land (bounded) before leaving
+            if (lane == 0 && uses0 > 0) mbar_wait(smem_addr(&s_full[0]), u32(uses0 - 1) & 1u);
+            if (lane == 0 && uses1 > 0) mbar_wait(smem_addr(&s_full[1]), u32(uses1 - 1) & 1u);
+        }
+        return;
+    }
+
+    // ---- consumers ----
+    const int cw = warp - 1;
+    u64 *wq_mask = qmask + cw * kQueue;
+    u64 *wq_pos = qpos + cw * kQueue;
+    WideCtx *ctx = s_ctx[cw];
+    u32 phase = 0;
+    int b = 0;
+    int qn = 0;      // queued words (kept across denominators and curves)
+    int seq = 0;     // slot fills this warp has taken
+    int oldest = 0;  // oldest context that may still have queued words
     auto drain_all = [&]() {
         while (qn > 0) {
             const int nd = qn < 32 ? qn : 32;
             __syncwarp();
-            wide_drain(wq_mask, wq_pos, qn - nd, nd, C, cand, s_aff, ctx, out);
+            wide_drain(wq_mask, wq_pos, qn - nd, nd, curves, affine, cand, ctx, out);
             qn -= nd;
         }
     };
-    u32 phase = 0;     // bit b: parity of buffer b's next completion
-    u32 pending = 0;   // bit b: a copy into buffer b is in flight and not yet waited for
-    int cur = -1;
-    if (threadIdx.x == 0) {
-        mbar_init(smem_addr(&s_bar[0]), 1);
-        mbar_init(smem_addr(&s_bar[1]), 1);
-        s_abort = 0;
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-
     for (;;) {
-        if (threadIdx.x == 0) s_item = int(atomicAdd(work, 1ull));
-        __syncthreads();
-        const int it = s_item;
-        if (it >= nitems) break;
-        const BatchItem item = items[it];
-        if (item.curve != cur) {
-            // queued words need their curve's descriptor and bitmasks: drain first
+        if (!mbar_wait(smem_addr(&s_full[b]), (phase >> b) & 1u)) {  // bounded wait
+            if (out.error && lane == 0) atomicOr(out.error, 1ull);
+            return;
+        }
+        phase ^= 1u << b;
+        const WideSlot &S = slot[b];
+        if (S.d < 0) {
             drain_all();
-            __syncthreads();
-            const u32 *src = reinterpret_cast<const u32 *>(curves + item.curve);
-            u32 *dst = reinterpret_cast<u32 *>(&C);
-            for (int i = threadIdx.x; i < int(sizeof(WideCurve) / 4); i += kWThreads) dst[i] = src[i];
-            const u64 *aff_src = affine + curves[item.curve].aff;
-            for (int i = threadIdx.x; i < kAffWords; i += kWThreads) s_aff[i] = __ldg(aff_src + i);
-            cur = item.curve;
-            __syncthreads();
+            return;
         }
-        const int q = C.class_prime;
-        const int M = C.class_mod;
-        const ClassStart *cstart = class_starts + C.cls;
-        auto param = [&](int i) {
-            const long long k = item.first + i;
-            return C.square ? k * k : k;
-        };
-        // parameters whose denominator has no admissible class, or no
-        // numerator range of this item's index, are skipped
-        auto live = [&](int i) {
-            const long long d = param(i);
-            const u32 du = u32(d);
-            if (C.admissible[du & 63] == 0 || (q > 1 && C.admissible[64 + int(du % u32(q))] == 0))
-                return false;
-            if (C.nint == 0) return true;
-            long long L, U;
-            return x_range(C.lo, C.hi, C.nint, C.bound, d, item.range, L, U);
-        };
-        auto next_live = [&](int i) {
-            while (i < item.count && !live(i)) ++i;
-            return i;
-        };
-        auto stage_rows = [&](int i, int b) {  // thread 0: copy parameter i's rows into buffer b
-            const u32 du = u32(param(i));
-            const u32 bar = smem_addr(&s_bar[b]);
-            const u32 dst = smem_addr(smem + b * row_stride);
-            fence_proxy_async_shared();
-            mbar_arrive_expect_tx(bar, u32(C.smem_words) * 8u);
-#pragma unroll
-            for (int sl = 0; sl < kWideSlots; ++sl) {
-                const Modulus &Md = C.mod[sl];
-                const u32 rho = mod_u32(du, u32(Md.m), Md.magic);
-                bulk_copy_to_shared(dst + u32(Md.smem_offset) * 8u,
-                                    pool + Md.offset + (long long)rho * Md.length,
-                                    u32(Md.length) * 8u, bar);
-            }
-        };
-        // warps 0 and 1: prime selection and class runs of parameter i into set st
-        auto setup = [&](int i, int st) {
-            const long long d = param(i);
-            const u32 du = u32(d);
-            if (warp == 0) {
-                select_warp(du, cand, inv_table, s_ci[st], s_dinv[st]);
-                if (lane == 0) s_next[st] = 0;
-            } else if (warp == 1) {
-                const u64 classes2 = C.admissible[du & 63];
-                const u64 classesq = q > 1 ? C.admissible[64 + int(du % u32(q))] : u64(1);
-                const int nq = __popcll(classesq);
-                const int nclass = __popcll(classes2) * nq;
-                long long lo_a = -C.bound, hi_a = C.bound;
-                if (C.nint > 0) x_range(C.lo, C.hi, C.nint, C.bound, d, item.range, lo_a, hi_a);
-                // classes, 32 per pass: class c = (c / nq)-th 2-adic class crossed
-                // with the (c % nq)-th admissible residue mod q; item prefix by scan
-                int carry = 0;
-                for (int base = 0; base < nclass; base += 32) {
-                    const int c = base + lane;
-                    int nitems_c = 0;
-                    if (c < nclass) {
-                        const int r64 = nth_bit64(classes2, c / nq);
-                        int r = r64;
-                        if (q > 1) {
-                            const int rq = nth_bit64(classesq, c % nq);
-                            r = r64 + 64 * int(C.crt[C.mod_q[r64] * 13 + rq]);
-                        }
-                        const int ofs = cstart[r].ofs;
-                        // sites of class r: a = -H + ofs + M t, t in [0, count); those
-                        // in [lo_a, hi_a] are t in [t_lo, t_hi]
-                        const long long count = C.count_q + (ofs <= C.count_r ? 1 : 0);
-                        long long t_lo = 0, t_hi = count - 1;
-                        if (C.nint > 0) {
-                            const long long a0 = -C.bound + ofs;
-                            const long long below = lo_a - a0;
-                            t_lo = below <= 0 ? 0 : (below + M - 1) / M;
-                            const long long above = hi_a - a0;
-                            t_hi = above < 0 ? -1 : min(count - 1, above / M);
-                        }
-                        ClassRun run;
-                        run.r = (unsigned short)r;
-                        run.ofs = (unsigned short)ofs;
-                        run.pad = 0;
-                        if (t_lo <= t_hi) {
-                            run.wbase = int(t_lo >> 6);
-                            run.words = int((t_hi >> 6) - (t_lo >> 6) + 1);
-                            run.first = (unsigned char)(t_lo & 63);
-                            run.last = (unsigned char)((t_hi & 63) + 1);
-                        } else {
-                            run.wbase = 0;
-                            run.words = 0;
-                            run.first = 0;
-                            run.last = 64;
-                        }
-                        runs0[st * max_classes + c] = run;
-                        nitems_c = (run.words + kWItemWords - 1) / kWItemWords;
-                    }
-                    int incl = nitems_c;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int v = __shfl_up_sync(kFullMask, incl, o);
-                        if (lane >= o) incl += v;
-                    }
-                    if (c < nclass) prefix0[st * (max_classes + 1) + c] = carry + incl - nitems_c;
-                    carry += __shfl_sync(kFullMask, incl, 31);
-                }
-                if (lane == 0) {
-                    prefix0[st * (max_classes + 1) + nclass] = carry;
-                    s_nclass[st] = nclass;
-                }
-            }
-        };
-
-        int i = next_live(0);
-        int b = 0, st = 0;
-        if (i < item.count) {
-            if (threadIdx.x == 0) stage_rows(i, b);
-            pending |= 1u << b;
-            setup(i, st);
+        // context kc replaces the one taken kWCtx fills ago: its queued words go first
+        const int kc = seq & (kWCtx - 1);
+        if (qn > 0 && seq - oldest >= kWCtx) drain_all();
+        if (qn == 0) oldest = seq;
+        __syncwarp();
+        ctx[kc].sel[lane] = S.sel[lane];
+        ctx[kc].dinv[lane] = S.dinv[lane];
+        if (lane == 0) {
+            ctx[kc].d = int(S.d);
+            ctx[kc].curve = S.curve;
         }
-        __syncthreads();
-        while (i < item.count) {
-            const long long d = param(i);
-            const int next = next_live(i + 1);
-            if (next < item.count) {
-                setup(next, st ^ 1);
-                if (C.nbuf == 2) {
-                    if (threadIdx.x == 0) stage_rows(next, b ^ 1);
-                    pending |= 1u << (b ^ 1);
-                }
-            }
-            if (!mbar_wait(smem_addr(&s_bar[b]), (phase >> b) & 1u)) {  // bounded wait
-                s_abort = 1;
-                if (out.error) atomicOr(out.error, 1ull);
-            }
-            phase ^= 1u << b;
-            pending &= ~(1u << b);
-
-            const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
-            const int nclass = s_nclass[st];
-            const int *prefix = prefix0 + st * (max_classes + 1);
-            const ClassRun *runs = runs0 + st * max_classes;
-            const int total_items = prefix[nclass];
-            // this denominator's context; the one it replaces is drained first
-            const int kc = seq & (kWCtx - 1);
-            if (qn > 0 && seq - oldest >= kWCtx) drain_all();
-            if (qn == 0) oldest = seq;
-            __syncwarp();
-            ctx[kc].sel[lane] = (unsigned char)s_ci[st][lane];
-            ctx[kc].dinv[lane] = (unsigned short)s_dinv[st][lane];
-            if (lane == 0) ctx[kc].d = int(d);
-            __syncwarp();
-            const u64 tag = u64(kc) << 56;
-            u32 step8[kWideSlots], mod8[kWideSlots];
-            const unsigned char *slot_base[kWideSlots];
+        __syncwarp();
+        const u64 tag = u64(kc) << 56;
+        const WideCurve &C = curves[S.curve];
+        const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
+        u32 step8[kWideSlots], mod8[kWideSlots];
+        const unsigned char *slot_base[kWideSlots];
 #pragma unroll
-            for (int sl = 0; sl < kWideSlots; ++sl) {
-                step8[sl] = 8u * C.mod[sl].step;
-                mod8[sl] = 8u * u32(C.mod[sl].m);
-                slot_base[sl] = sbase + 8 * C.mod[sl].smem_offset;
+        for (int sl = 0; sl < kWideSlots; ++sl) {
+            step8[sl] = 8u * C.mod[sl].step;
+            mod8[sl] = 8u * u32(C.mod[sl].m);
+            slot_base[sl] = sbase + 8 * C.mod[sl].smem_offset;
+        }
+        const u64 stride = u64(C.stride);
+        const WideRun *runs = S.runs;
+        const int *prefix = S.prefix;
+        const int nclass = S.nclass;
+        const int total_items = prefix[nclass];
+        for (;;) {
+            int sweep = 0;
+            if (lane == 0) sweep = atomicAdd(const_cast<int *>(&S.next), 1);
+            sweep = __shfl_sync(kFullMask, sweep, 0);
+            if (sweep >= total_items) break;
+            int c = 0;
+            for (int base = 0; base < nclass; base += 32) {
+                const int cc = base + lane;
+                const u32 bb = __ballot_sync(kFullMask, cc < nclass && prefix[cc] <= sweep);
+                if (bb) c = base + 31 - __clz(bb);
+                if (bb != kFullMask) break;
             }
-            for (;;) {
-                int sweep = 0;
-                if (lane == 0) sweep = atomicAdd(&s_next[st], 1);
-                sweep = __shfl_sync(kFullMask, sweep, 0);
-                if (sweep >= total_items) break;
-                int c = 0;
-                for (int base = 0; base < nclass; base += 32) {
-                    const int cc = base + lane;
-                    const u32 bb = __ballot_sync(kFullMask, cc < nclass && prefix[cc] <= sweep);
-                    if (bb) c = base + 31 - __clz(bb);
-                    if (bb != kFullMask) break;
-                }
-                const int w0 = (sweep - prefix[c]) * kWItemWords;
-                const ClassRun run = runs[c];
-                const ClassStart cs = cstart[run.r];
-                const int wt = run.words;
-                const u64 first_mask = ~u64(0) << run.first;
-                const u64 last_mask = run.last >= 64 ? ~u64(0) : ((u64(1) << run.last) - 1);
-                u32 o[kWideSlots];
+            const int w0 = (sweep - prefix[c]) * kWItemWords;
+            const WideRun run = runs[c];
+            const int wt = run.words;
+            const u64 first_mask = ~u64(0) << run.first;
+            const u64 last_mask = run.last >= 64 ? ~u64(0) : ((u64(1) << run.last) - 1);
+            const u64 pos0 = u64(run.ofs) + stride * u64(run.wbase);
+            u32 o[kWideSlots];
 #pragma unroll
-                for (int sl = 0; sl < kWideSlots; ++sl)
-                    o[sl] = 8u * mod_u32(u32(cs.start[sl]) + u32(run.wbase + w0 + lane),
-                                         u32(C.mod[sl].m), C.mod[sl].magic);
+            for (int sl = 0; sl < kWideSlots; ++sl)
+                o[sl] = 8u * mod_u32(u32(run.start[sl]) + u32(w0 + lane), u32(C.mod[sl].m), C.mod[sl].magic);
 #pragma unroll 1
-                for (int step = 0; step < kWSteps; ++step) {
-                    const int ws = w0 + step * kWarpSize * kWK;
-                    if (ws >= wt) break;
-                    u64 acc[kWK];
+            for (int step = 0; step < kWSteps; ++step) {
+                const int ws = w0 + step * kWarpSize * kWK;
+                if (ws >= wt) break;
+                // a class's last step often covers fewer than kWK groups of
+                // 32 words (short rows): the groups past its end are skipped
+                const int nk = min(kWK, (wt - ws + kWarpSize - 1) / kWarpSize);
+                u64 acc[kWK];
+#pragma unroll
+                for (int kk = 0; kk < kWK; ++kk)
+                    acc[kk] = kk < nk ? *reinterpret_cast<const u64 *>(slot_base[0] + o[0] + 256 * kk) : 0;
+#pragma unroll
+                for (int sl = 1; sl < kWideSlots; ++sl) {
 #pragma unroll
                     for (int kk = 0; kk < kWK; ++kk)
-                        acc[kk] = *reinterpret_cast<const u64 *>(slot_base[0] + o[0] + 256 * kk);
+                        if (kk < nk) acc[kk] &= *reinterpret_cast<const u64 *>(slot_base[sl] + o[sl] + 256 * kk);
+                }
 #pragma unroll
-                    for (int sl = 1; sl < kWideSlots; ++sl) {
+                for (int sl = 0; sl < kWideSlots; ++sl) {
+                    // advance (32 kWK) mod m words; unsigned min wraps into [0, m)
+                    const u32 t = o[sl] + step8[sl];
+                    o[sl] = min(t, t - mod8[sl]);
+                }
+                const u64 any = acc[0] | acc[1] | acc[2] | acc[3];
+                if (!__ballot_sync(kFullMask, any != 0)) continue;
 #pragma unroll
-                        for (int kk = 0; kk < kWK; ++kk)
-                            acc[kk] &= *reinterpret_cast<const u64 *>(slot_base[sl] + o[sl] + 256 * kk);
-                    }
-#pragma unroll
-                    for (int sl = 0; sl < kWideSlots; ++sl) {
-                        // advance (32 kWK) mod m words; unsigned min wraps into [0, m)
-                        const u32 t = o[sl] + step8[sl];
-                        o[sl] = min(t, t - mod8[sl]);
-                    }
-                    const u64 any = acc[0] | acc[1] | acc[2] | acc[3];
-                    if (!__ballot_sync(kFullMask, any != 0)) continue;
-#pragma unroll
-                    for (int kk = 0; kk < kWK; ++kk) {
-                        const int w = ws + kWarpSize * kk + lane;
-                        u64 a = acc[kk];
-                        if (w == 0) a &= first_mask;
-                        if (w == wt - 1) a &= last_mask;
-                        const bool live_word = a != 0 && w < wt;
-                        const u32 bb = __ballot_sync(kFullMask, live_word);
-                        if (bb) {
-                            const int at = qn + __popc(bb & lanemask_lt());
-                            if (live_word) {
-                                wq_mask[at] = a;
-                                wq_pos[at] = tag | (u64(run.ofs) + u64(C.stride) * u64(run.wbase + w));
-                            }
-                            qn += __popc(bb);
-                            if (qn >= 32) {
-                                __syncwarp();
-                                wide_drain(wq_mask, wq_pos, qn - 32, 32, C, cand, s_aff, ctx, out);
-                                qn -= 32;
-                                if (qn == 0) oldest = seq;
-                            }
+                for (int kk = 0; kk < kWK; ++kk) {
+                    if (kk >= nk) break;
+                    const int w = ws + kWarpSize * kk + lane;
+                    u64 a = acc[kk];
+                    if (w == 0) a &= first_mask;
+                    if (w == wt - 1) a &= last_mask;
+                    const bool live_word = a != 0 && w < wt;
+                    const u32 bb = __ballot_sync(kFullMask, live_word);
+                    if (bb) {
+                        const int at = qn + __popc(bb & lanemask_lt());
+                        if (live_word) {
+                            wq_mask[at] = a;
+                            wq_pos[at] = tag | (pos0 + stride * u64(w));
+                        }
+                        qn += __popc(bb);
+                        if (qn >= 32) {
+                            __syncwarp();
+                            wide_drain(wq_mask, wq_pos, qn - 32, 32, curves, affine, cand, ctx, out);
+                            qn -= 32;
+                            if (qn == 0) oldest = seq;
                         }
                     }
                 }
             }
-            ++seq;
-            __syncthreads();
-            if (s_abort) {
-                // a bulk copy did not complete in time: give the copies in
-                // flight a last bounded chance to land, then leave (the host
-                // reports the error word)
-                if (threadIdx.x == 0) {
-                    mbar_wait(smem_addr(&s_bar[b]), ((phase >> b) & 1u) ^ 1u);
-                    if (pending & (1u << (b ^ 1)))
-                        mbar_wait(smem_addr(&s_bar[b ^ 1]), (phase >> (b ^ 1)) & 1u);
-                }
-                return;
-            }
-            i = next;
-            st ^= 1;
-            if (C.nbuf == 2) {
-                b ^= 1;
-            } else if (i < item.count) {  // one buffer: copy the next row now that it is free
-                if (threadIdx.x == 0) stage_rows(i, b);
-                pending |= 1u << b;
-            }
         }
-        __syncthreads();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_addr(&s_empty[b]));  // this warp is done with slot b
+        ++seq;
+        b ^= 1;
     }
-    drain_all();  // the last curve's queued words
 }
 
 // ---------------------------------------------------------------------------
@@ -1032,6 +1090,12 @@ unsigned long long host_magic(int m) {
     return m == 1 ? ~0ull : (~0ull) / (unsigned long long)m + 1;
 }
 
+// Position of the k-th set bit (k counted from 0) of a 64-bit mask.
+int nth_bit_host(dev::u64 mask, int k) {
+    for (int i = 0; i < k; ++i) mask &= mask - 1;
+    return __builtin_ctzll(mask);
+}
+
 bool lead_is_square(const std::vector<std::string> &coefficients, int q) {
     const int n = int(coefficients.size()) - 1;
     if (n % 2) return true;  // odd degree: F(a, d) = d (...) vanishes mod q | d
@@ -1171,10 +1235,10 @@ FastPlan narrow_plan(const std::vector<std::string> &coefficients) {
 // CTA stays within a third of an SM's shared memory: static arrays, queues,
 // and two sets of class runs and item prefixes for max_classes classes.
 long long wide_row_budget(int max_classes) {
-    const long long per_cta = 228 * 1024 / 3 - 1024;
-    const long long fixed = 8 * 1024 +  // static shared memory of the kernel (7.6 KB) and slack
-                            (long long)dev::kWWarps * dev::kQueue * 16 +
-                            2LL * max_classes * (long long)sizeof(dev::ClassRun) + 2LL * (max_classes + 1) * 4;
+    const long long per_cta = 228 * 1024 / 2 - 1024;
+    const long long fixed = 6 * 1024 +  // static shared memory of the kernel (5 KB) and slack
+                            (long long)dev::kWConsumers * dev::kQueue * 16 +
+                            2LL * max_classes * (long long)sizeof(dev::WideRun) + 2LL * (max_classes + 1) * 4;
     return std::max(2LL * 64, (per_cta - fixed) / 8);
 }
 
@@ -1206,16 +1270,15 @@ int wide_classes(const std::vector<std::string> &coefficients, const dev::u64 ad
     return most2 * std::max(1, mostq);
 }
 
-// max_classes: the most classes of any wide curve in the launch, which sizes
-// the launch's class arrays and so this curve's share of shared memory.
-FastPlan wide_plan(const FastPlanner &planner, long double work, bool huge_rows, int max_classes) {
+// max_classes: the most classes of any wide curve with x intervals in the
+// launch (their classes are laid out in shared memory), which sizes the
+// launch's class arrays and so the share of shared memory left for rows.
+FastPlan wide_plan(const FastPlanner &planner, long double work, int max_classes) {
     int cap = int(std::min<long double>(kMaxModulus, std::max<long double>(64, std::sqrt(work / 48.0L))));
-    const long long both = wide_row_budget(max_classes);
-    // two row buffers, or one twice as large for huge rows
-    const long long smem_budget = std::min<long long>(huge_rows ? 2 * dev::kWMaxSmemWords : dev::kWMaxSmemWords,
-                                                      huge_rows ? both : both / 2);
+    // two slots of staged rows
+    const long long smem_budget = std::min<long long>(dev::kWMaxSmemWords, wide_row_budget(max_classes) / 2);
     for (;;) {
-        FastPlan plan = planner.plan(cap);
+        FastPlan plan = planner.plan(cap, dev::kWideSlots, 1LL << 40, false);
         long long smem = 0;
         for (int sl = 0; sl < dev::kWideSlots; ++sl) {
             const int m = sl < int(plan.moduli.size()) ? plan.moduli[sl] : 1;
@@ -1242,9 +1305,11 @@ struct BatchPlan {
     std::vector<dev::CompositeSpec> cspecs;
     std::vector<dev::BatchItem> wide_items, narrow_items;
     std::vector<dev::ClassStart> class_starts;
+    std::vector<dev::WideRun> list_runs;       // class lists of wide curves without x intervals
+    std::vector<int> list_prefix, list_count;
     long long aff_words = 0, pattern_words = 0, row_words = 0;
     int wide_smem_words = 0;
-    int wide_max_classes = 1;   // most admissible classes of any wide curve's denominator
+    int wide_max_classes = 1;   // most classes of a denominator of a wide curve with x intervals
 };
 
 // Validation and per-curve plans (one curve per task), then descriptors,
@@ -1276,7 +1341,7 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             cw.wide = cw.swept >= kBatchWideWords;
             two_adic_classes(c.coefficients, cw.adm2);
             if (cw.wide) {
-                cw.planner.reset(new FastPlanner(c.coefficients, c.bound, true));
+                cw.planner.reset(new FastPlanner(c.coefficients, c.bound, true, kFastPrimeLimit));
                 cw.classes = wide_classes(c.coefficients, cw.adm2, cw.planner->class_prime());
             } else {
                 cw.plan = narrow_plan(c.coefficients);
@@ -1294,16 +1359,17 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             r.error = e.what();
         }
     });
-    // wide plans: one row budget for the launch, from its largest class count
-    int max_classes = 1;
-    for (const CurveWork &cw : P.work)
-        if (cw.ok && cw.wide) max_classes = std::max(max_classes, cw.classes);
+    // wide plans: one row budget for the launch, from the largest class count
+    // of the curves whose classes are laid out in shared memory (x intervals)
+    int max_classes = 0;
+    for (std::size_t i = 0; i < curves.size(); ++i)
+        if (P.work[i].ok && P.work[i].wide && !curves[i].intervals.empty())
+            max_classes = std::max(max_classes, P.work[i].classes);
     parallel_for(curves.size(), [&](std::size_t i) {
         CurveWork &cw = P.work[i];
         if (!cw.ok) return;
         if (cw.wide) {
-            cw.plan = wide_plan(*cw.planner, (long double)cw.words * cw.count, cw.words >= dev::kWHugeWords,
-                                max_classes);
+            cw.plan = wide_plan(*cw.planner, (long double)cw.words * cw.count, max_classes);
             cw.planner.reset();
         }
         results[i].wide = cw.wide;
@@ -1424,12 +1490,8 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 Md.step = dev::u32((dev::kWarpSize * dev::kWK) % m);
             }
             C.smem_words = smem;
-            C.nbuf = cw.words >= dev::kWHugeWords ? 1 : 2;
-            // row buffers are row_stride words apart; a one-buffer curve spans both
-            P.wide_smem_words =
-                std::max(P.wide_smem_words, round_even(C.nbuf == 2 ? smem : (smem + 1) / 2));
+            P.wide_smem_words = std::max(P.wide_smem_words, round_even(smem));
             std::copy(cw.adm2, cw.adm2 + 64, C.admissible);
-            P.wide_max_classes = std::max(P.wide_max_classes, cw.classes);
             if (q > 1) {
                 class_prime_residues(c.coefficients, q, C.admissible + 64);
                 for (int a = 0; a < q; ++a)
@@ -1458,6 +1520,54 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 C.m_mod[ci] = (unsigned short)(M % p);
             }
             device_intervals(c.intervals, C.nint, C.lo, C.hi);
+            C.list_max = std::max(1, cw.classes);
+            if (C.nint == 0) {
+                // class lists by denominator class k = (d mod 64) q + (d mod q),
+                // in the order the producer lays out classes for interval curves
+                const int lm = C.list_max;
+                const std::size_t ncombo = std::size_t(64) * std::size_t(q);
+                C.list_count = (long long)P.list_count.size();
+                C.list_runs = (long long)P.list_runs.size();
+                C.list_prefix = (long long)P.list_prefix.size();
+                P.list_count.resize(P.list_count.size() + ncombo, 0);
+                P.list_runs.resize(P.list_runs.size() + ncombo * std::size_t(lm));
+                P.list_prefix.resize(P.list_prefix.size() + ncombo * std::size_t(lm + 1), 0);
+                for (int dd = 0; dd < 64; ++dd)
+                    for (int dq = 0; dq < q; ++dq) {
+                        const std::size_t k = std::size_t(dd) * std::size_t(q) + std::size_t(dq);
+                        const dev::u64 classes2 = cw.adm2[dd];
+                        const dev::u64 classesq = q > 1 ? C.admissible[64 + dq] : dev::u64(1);
+                        const int nq = __builtin_popcountll(classesq);
+                        const int nclass = __builtin_popcountll(classes2) * nq;
+                        if (nclass > lm) throw std::logic_error("class list longer than its stride");
+                        dev::WideRun *runs = P.list_runs.data() + C.list_runs + k * std::size_t(lm);
+                        int *prefix = P.list_prefix.data() + C.list_prefix + k * std::size_t(lm + 1);
+                        int items = 0;
+                        for (int cidx = 0; cidx < nclass; ++cidx) {
+                            const int r64 = nth_bit_host(classes2, cidx / nq);
+                            int r = r64;
+                            if (q > 1)
+                                r = r64 + 64 * int(C.crt[C.mod_q[r64] * 13 + nth_bit_host(classesq, cidx % nq)]);
+                            const dev::ClassStart &cs = P.class_starts[std::size_t(C.cls + r)];
+                            const long long count = C.count_q + (cs.ofs <= C.count_r ? 1 : 0);
+                            const long long words = (count + 63) >> 6;
+                            dev::WideRun &run = runs[cidx];
+                            run.wbase = 0;
+                            run.words = int(words);
+                            run.ofs = cs.ofs;
+                            run.first = 0;
+                            run.last = (unsigned char)(words > 0 ? count - 64 * (words - 1) : 64);
+                            for (int sl = 0; sl < dev::kWideSlots; ++sl) run.start[sl] = cs.start[sl];
+                            prefix[cidx] = items;
+                            items += int((words + dev::kWItemWords - 1) / dev::kWItemWords);
+                        }
+                        prefix[nclass] = items;
+                        P.list_count[C.list_count + k] = nclass;
+                    }
+            } else {
+                C.list_count = -1;
+                P.wide_max_classes = std::max(P.wide_max_classes, cw.classes);
+            }
             // items of about 2^20 row words, one set per numerator range
             const long long chunk = std::max(1LL, std::min<long long>(1 << 16, (1LL << 20) / cw.words));
             for (int range = 0; range < std::max(1, C.nint); ++range)
@@ -1585,11 +1695,16 @@ struct BatchEngine::Impl {
     DeviceArray<dev::PatternSpec> d_pspecs;
     DeviceArray<dev::CompositeSpec> d_cspecs;
     DeviceArray<dev::ClassStart> d_cls;
+    DeviceArray<dev::WideRun> d_lruns;
+    DeviceArray<int> d_lprefix, d_lcount;
     DeviceArray<unsigned short> d_res, d_inv;
     DeviceArray<dev::u64> d_sq, d_aff, d_patterns, d_rows;
-    DeviceArray<unsigned long long> d_counters;  // [0] survivors [1] wide work [2] narrow work [3] error
-    DeviceArray<long long> d_a;
-    DeviceArray<int> d_d, d_c;
+    // [0] survivors [1] wide work [2] narrow work [3] error [4] pre-verified survivors
+    DeviceArray<unsigned long long> d_counters;
+    DeviceArray<long long> d_a, d_pa;        // survivors, and those kept by pre-verification
+    DeviceArray<int> d_d, d_c, d_pd, d_pc;
+    DeviceArray<unsigned long long> d_curve_modular;  // per-curve modular survivors
+    Preverifier pre;
 
     explicit Impl(int dev_ordinal) {
         if (dev_ordinal >= 0) check_cuda(cudaSetDevice(dev_ordinal), "cudaSetDevice");
@@ -1626,7 +1741,7 @@ struct BatchEngine::Impl {
         unsigned long long bytes = 0;
         d_inv.upload(inv_table, stream, bytes, "upload inverses");
         d_sq.upload(square_masks, stream, bytes, "upload squares");
-        d_counters.ensure(4, "cudaMalloc(batch counters)");
+        d_counters.ensure(5, "cudaMalloc(batch counters)");
         ensure_output(capacity);
         check_cuda(cudaStreamSynchronize(stream), "batch engine setup");
     }
@@ -1647,14 +1762,17 @@ struct BatchEngine::Impl {
         d_a.ensure(cap, "cudaMalloc(batch survivors)");
         d_d.ensure(cap, "cudaMalloc(batch survivors)");
         d_c.ensure(cap, "cudaMalloc(batch survivors)");
+        d_pa.ensure(cap, "cudaMalloc(batch survivors)");
+        d_pd.ensure(cap, "cudaMalloc(batch survivors)");
+        d_pc.ensure(cap, "cudaMalloc(batch survivors)");
     }
 
     std::vector<BatchCurveResult> run(const std::vector<BatchCurveSpec> &curves, BatchStats *stats_out,
-                                      bool use_graph);
+                                      bool use_graph, bool preverify);
 };
 
 std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurveSpec> &curves,
-                                                     BatchStats *stats_out, bool use_graph) {
+                                                     BatchStats *stats_out, bool use_graph, bool preverify) {
     const auto started = Clock::now();
     BatchStats stats;
     std::vector<BatchCurveResult> results(curves.size());
@@ -1675,15 +1793,26 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
         d_cspecs.upload(P.cspecs, stream, stats.h2d_bytes, "upload table specs");
         d_res.upload(P.residues, stream, stats.h2d_bytes, "upload residues");
         d_cls.upload(P.class_starts, stream, stats.h2d_bytes, "upload class starts");
+        d_lruns.upload(P.list_runs, stream, stats.h2d_bytes, "upload class lists");
+        d_lprefix.upload(P.list_prefix, stream, stats.h2d_bytes, "upload class lists");
+        d_lcount.upload(P.list_count, stream, stats.h2d_bytes, "upload class lists");
         d_aff.ensure(std::size_t(P.aff_words), "cudaMalloc(batch bitmasks)");
         d_patterns.ensure(std::size_t(P.pattern_words), "cudaMalloc(batch patterns)");
         d_rows.ensure(std::size_t(P.row_words), "cudaMalloc(batch tables)");
+        if (preverify) {
+            std::vector<const std::vector<std::string> *> coefs(curves.size(), nullptr);
+            for (std::size_t i = 0; i < curves.size(); ++i)
+                if (work[i].ok) coefs[i] = &curves[i].coefficients;
+            pre.prepare(coefs, stream);
+            stats.h2d_bytes += pre.upload_bytes();
+            d_curve_modular.ensure(std::max<std::size_t>(1, curves.size()), "cudaMalloc(batch counters)");
+        }
 
         const int wide_smem_words = P.wide_smem_words;
         const int wide_max_classes = P.wide_max_classes;
         const std::size_t wide_smem = 2 * std::size_t(wide_smem_words) * 8 +
-                                      std::size_t(dev::kWWarps) * dev::kQueue * 16 +
-                                      2 * std::size_t(wide_max_classes) * sizeof(dev::ClassRun) +
+                                      std::size_t(dev::kWConsumers) * dev::kQueue * 16 +
+                                      2 * std::size_t(wide_max_classes) * sizeof(dev::WideRun) +
                                       2 * std::size_t(wide_max_classes + 1) * 4;
         const std::size_t narrow_smem = std::size_t(dev::kNarrowTableWords + dev::kAffWords) * 8 +
                                         std::size_t(dev::kNWarps) * dev::kQueue * 12;
@@ -1718,15 +1847,19 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
         };
         auto enqueue_sieve = [&]() {
             const dev::BatchOut out{d_a.p, d_d.p, d_c.p, d_counters.p, capacity, d_counters.p + 3};
-            check_cuda(cudaMemsetAsync(d_counters.p, 0, 4 * sizeof(unsigned long long), stream),
+            check_cuda(cudaMemsetAsync(d_counters.p, 0, 5 * sizeof(unsigned long long), stream),
                        "cudaMemsetAsync");
+            if (preverify)
+                check_cuda(cudaMemsetAsync(d_curve_modular.p, 0, curves.size() * sizeof(unsigned long long), stream),
+                           "cudaMemsetAsync");
             check_cuda(cudaEventRecord(fork, stream), "cudaEventRecord");
             check_cuda(cudaStreamWaitEvent(side, fork, 0), "cudaStreamWaitEvent");
             record(ev[2], stream);
             if (wide_grid) {
                 dev::wide_kernel<<<wide_grid, dev::kWThreads, wide_smem, stream>>>(
-                    d_wide.p, d_witems.p, int(P.wide_items.size()), d_rows.p, d_aff.p, d_cls.p,
-                    d_inv.p, cand, out, wide_smem_words, wide_max_classes, d_counters.p + 1);
+                    d_wide.p, d_witems.p, int(P.wide_items.size()), d_rows.p, d_aff.p, d_cls.p, d_lruns.p,
+                    d_lprefix.p, d_lcount.p, d_inv.p, cand, out, wide_smem_words, wide_max_classes,
+                    d_counters.p + 1);
                 check_cuda(cudaGetLastError(), "wide_kernel launch");
             }
             record(ev[3], stream);
@@ -1740,7 +1873,10 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
             record(ev[5], side);
             check_cuda(cudaEventRecord(join, side), "cudaEventRecord");
             check_cuda(cudaStreamWaitEvent(stream, join, 0), "cudaStreamWaitEvent");
-            check_cuda(cudaMemcpyAsync(h_counters, d_counters.p, 4 * sizeof(unsigned long long),
+            if (preverify)
+                pre.launch(d_a.p, d_d.p, d_c.p, d_counters.p, capacity, d_pa.p, d_pd.p, d_pc.p, d_counters.p + 4,
+                           d_curve_modular.p, stream);
+            check_cuda(cudaMemcpyAsync(h_counters, d_counters.p, 5 * sizeof(unsigned long long),
                                        cudaMemcpyDeviceToHost, stream),
                        "download batch counters");
         };
@@ -1795,7 +1931,7 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
             check_cuda(cudaStreamSynchronize(stream), "batch sieve");
         }
         stats.launches += (P.aspecs.empty() ? 0 : 1) + (P.pattern_words ? 1 : 0) + (P.row_words ? 1 : 0) +
-                          (wide_grid ? 1 : 0) + (narrow_grid ? 1 : 0);
+                          (wide_grid ? 1 : 0) + (narrow_grid ? 1 : 0) + (preverify ? 1 : 0);
         auto elapsed = [&](int a, int b) {
             float ms = 0;
             cudaEventElapsedTime(&ms, ev[a], ev[b]);
@@ -1812,24 +1948,35 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
             enqueue_sieve();
             check_cuda(cudaStreamSynchronize(stream), "batch sieve");
             stats.sieve_ms += std::max(elapsed(2, 3), elapsed(2, 5));
-            stats.launches += (wide_grid ? 1 : 0) + (narrow_grid ? 1 : 0);
+            stats.launches += (wide_grid ? 1 : 0) + (narrow_grid ? 1 : 0) + (preverify ? 1 : 0);
             if (h_counters[3]) throw DeviceTimeout("batched sieve: a bounded wait timed out");
         }
-        const std::size_t n = std::size_t(h_counters[0]);
-        stats.survivors = n;
+        stats.survivors = h_counters[0];
+        // survivors for the host: those kept by pre-verification, or all
+        const std::size_t n = std::size_t(preverify ? h_counters[4] : h_counters[0]);
+        stats.host_candidates = n;
         std::vector<long long> ha(n);
         std::vector<int> hd(n), hc(n);
+        std::vector<unsigned long long> curve_modular(preverify ? curves.size() : 0);
         if (n) {
-            check_cuda(cudaMemcpyAsync(ha.data(), d_a.p, n * sizeof(long long), cudaMemcpyDeviceToHost,
-                                       stream),
+            check_cuda(cudaMemcpyAsync(ha.data(), preverify ? d_pa.p : d_a.p, n * sizeof(long long),
+                                       cudaMemcpyDeviceToHost, stream),
                        "download batch survivors");
-            check_cuda(cudaMemcpyAsync(hd.data(), d_d.p, n * sizeof(int), cudaMemcpyDeviceToHost, stream),
+            check_cuda(cudaMemcpyAsync(hd.data(), preverify ? d_pd.p : d_d.p, n * sizeof(int),
+                                       cudaMemcpyDeviceToHost, stream),
                        "download batch survivors");
-            check_cuda(cudaMemcpyAsync(hc.data(), d_c.p, n * sizeof(int), cudaMemcpyDeviceToHost, stream),
+            check_cuda(cudaMemcpyAsync(hc.data(), preverify ? d_pc.p : d_c.p, n * sizeof(int),
+                                       cudaMemcpyDeviceToHost, stream),
                        "download batch survivors");
-            check_cuda(cudaStreamSynchronize(stream), "download batch survivors");
         }
-        stats.d2h_bytes += n * (sizeof(long long) + 2 * sizeof(int)) + 4 * sizeof(unsigned long long);
+        if (!curve_modular.empty())
+            check_cuda(cudaMemcpyAsync(curve_modular.data(), d_curve_modular.p,
+                                       curve_modular.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                       stream),
+                       "download batch survivor counts");
+        check_cuda(cudaStreamSynchronize(stream), "download batch survivors");
+        stats.d2h_bytes += n * (sizeof(long long) + 2 * sizeof(int)) + 5 * sizeof(unsigned long long) +
+                           curve_modular.size() * sizeof(unsigned long long);
 
         // ---- exact verification per curve, in single-search order ----
         const auto t_verify = Clock::now();
@@ -1853,7 +2000,7 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
             filter.intervals = curves[i].intervals;
             for (auto &p : found)
                 if (filter.accepts(p.numerator, p.denominator)) r.points.push_back(std::move(p));
-            r.survivors = by_curve[i].size();
+            r.survivors = preverify ? curve_modular[i] : by_curve[i].size();
         });
         stats.verify_ms = ms_since(t_verify);
     }
@@ -1874,8 +2021,8 @@ BatchEngine::BatchEngine(int device) : impl_(new Impl(device)) {}
 BatchEngine::~BatchEngine() = default;
 
 std::vector<BatchCurveResult> BatchEngine::run(const std::vector<BatchCurveSpec> &curves,
-                                               BatchStats *stats, bool use_graph) {
-    return impl_->run(curves, stats, use_graph);
+                                               BatchStats *stats, bool use_graph, bool preverify) {
+    return impl_->run(curves, stats, use_graph, preverify);
 }
 
 int BatchEngine::device() const { return impl_->device; }
@@ -1897,9 +2044,9 @@ unsigned long long BatchEngine::estimate_bytes(const BatchCurveSpec &c) {
 }
 
 std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &curves, int device,
-                                           BatchStats *stats, bool use_graph) {
+                                           BatchStats *stats, bool use_graph, bool preverify) {
     BatchEngine engine(device);
-    return engine.run(curves, stats, use_graph);
+    return engine.run(curves, stats, use_graph, preverify);
 }
 
 }  // namespace rpg

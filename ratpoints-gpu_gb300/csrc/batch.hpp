@@ -52,6 +52,7 @@ struct BatchCurveResult {
 
 struct BatchStats {
     unsigned long long curves = 0, wide_curves = 0, denominators = 0, survivors = 0, points = 0;
+    unsigned long long host_candidates = 0;   // survivors given to the host's exact check
     unsigned long long wide_items = 0, narrow_items = 0, launches = 0, words = 0;
     unsigned long long table_words = 0;
     unsigned long long swept_words = 0;       // 64-site words the sieve kernels sweep (no intervals)
@@ -77,9 +78,11 @@ public:
     // Runs every valid curve in one batched pass.  Curves that fail
     // validation get a nonzero status and no points; the others are searched
     // together.  The table build and sieve launches are captured in one CUDA
-    // graph when use_graph is set.
+    // graph when use_graph is set.  With preverify a kernel drops the
+    // survivors that cannot be points before the copy to the host
+    // (preverify.hpp); the points are the same either way.
     std::vector<BatchCurveResult> run(const std::vector<BatchCurveSpec> &curves, BatchStats *stats,
-                                      bool use_graph = true);
+                                      bool use_graph = true, bool preverify = true);
     int device() const;
 
     // Upper estimate of the device bytes a curve adds to a run (admission).
@@ -92,6 +95,6 @@ private:
 
 // One batched pass on a fresh engine on `device` (-1: current).
 std::vector<BatchCurveResult> batch_search(const std::vector<BatchCurveSpec> &curves, int device,
-                                           BatchStats *stats, bool use_graph = true);
+                                           BatchStats *stats, bool use_graph = true, bool preverify = true);
 
 }  // namespace rpg

@@ -12,6 +12,7 @@
 #include "cli.hpp"
 #include "exact.hpp"
 #include "plan.hpp"
+#include "preverify.hpp"
 #include "search.hpp"
 #include "serve.hpp"
 #include "session.hpp"
@@ -114,6 +115,7 @@ bool options_from(const rpg_search_options &o, rpg::SearchOptions &s, std::strin
     s.plan = o.plan == RPG_PLAN_REFERENCE ? rpg::PlanKind::reference : rpg::PlanKind::fast;
     if (o.device >= 0) s.devices = {o.device};
     s.verify_threads = o.verify_threads;
+    s.device_preverify = (o.flags & RPG_SEARCH_HOST_VERIFY_ONLY) == 0;
     return true;
 }
 
@@ -121,6 +123,7 @@ void fill_stats(rpg_sieve_stats *stats, const rpg::SearchMetrics &m) {
     if (!stats) return;
     std::memset(stats, 0, sizeof *stats);
     stats->survivor_count = m.modular_survivors;
+    stats->host_candidates = m.host_candidates;
     stats->word_count = m.word_count;
     stats->denominator_count = m.denominator_count;
     stats->launches = m.launches;
@@ -184,6 +187,7 @@ rpg_status rpg_sieve_run(const char *const *coefficients, int32_t coefficient_co
             std::memset(stats, 0, sizeof *stats);
             const auto &t = sieve.timings();
             stats->survivor_count = total;
+            stats->host_candidates = total;
             stats->word_count = (uint64_t)rpg::word_count32(numerator_bound);
             stats->denominator_count = denominators;
             stats->launches = t.launches;
@@ -211,6 +215,19 @@ rpg_status rpg_point_search(const rpg_search_options *o, rpg_point_cb callback, 
             return callback(p.numerator, p.ordinate.c_str(), p.denominator, user) != 0;
         });
         fill_stats(stats, m);
+        return RPG_OK;
+    });
+}
+
+rpg_status rpg_preverify(const char *const *coefficients, int32_t coefficient_count, int64_t numerator,
+                         int64_t denominator, int32_t *may_be_point) {
+    return guarded([&]() -> rpg_status {
+        std::vector<std::string> coeffs;
+        std::string error;
+        if (!coefficients_from(coefficients, coefficient_count, coeffs, error)) return fail(RPG_E_ARG, error);
+        if (!may_be_point) return fail(RPG_E_ARG, "output must not be NULL");
+        if (denominator < 1 || denominator > 2147483647LL) return fail(RPG_E_ARG, "denominator out of range");
+        *may_be_point = rpg::preverify_host(coeffs, numerator, denominator) ? 1 : 0;
         return RPG_OK;
     });
 }
@@ -357,7 +374,8 @@ rpg_status rpg_batch_search(const rpg_search_options *curves, int32_t curve_coun
             }
         rpg::BatchStats st;
         std::vector<rpg::BatchCurveResult> results =
-            rpg::batch_search(run, device, &st, (flags & RPG_BATCH_NO_GRAPH) == 0);
+            rpg::batch_search(run, device, &st, (flags & RPG_BATCH_NO_GRAPH) == 0,
+                              (flags & RPG_BATCH_HOST_VERIFY_ONLY) == 0);
         std::vector<const rpg::BatchCurveResult *> by_index(count, nullptr);
         for (std::size_t j = 0; j < valid.size(); ++j) {
             by_index[valid[j]] = &results[j];
@@ -378,6 +396,7 @@ rpg_status rpg_batch_search(const rpg_search_options *curves, int32_t curve_coun
             stats->wide_curves = st.wide_curves;
             stats->denominators = st.denominators;
             stats->survivors = st.survivors;
+            stats->host_candidates = st.host_candidates;
             stats->points = st.points;
             stats->launches = st.launches;
             stats->words = st.words;

@@ -5,8 +5,10 @@
 //   - parse_command_line / OptionParser (src/command_line.cpp:113-366);
 //   - OutputFormatter (src/output_formatter.cpp:7-105);
 //   - main, --help, --list-devices and the -v metrics line (src/main.cpp:14-85).
-// One extension: --sieve-plan reference|fast selects the sieve plan (default
-// fast; reference reproduces the reference's modular survivor set and counts).
+// Two extensions: --sieve-plan reference|fast selects the sieve plan (default
+// fast; reference reproduces the reference's modular survivor set and counts),
+// and --host-verify-only sends every modular survivor to the host's exact check
+// (by default a device kernel first drops those that cannot be points).
 #include "cli.hpp"
 
 #include <cerrno>
@@ -183,6 +185,8 @@ private:
             if (v == "reference") s.plan = PlanKind::reference;
             else if (v == "fast") s.plan = PlanKind::fast;
             else throw std::invalid_argument("--sieve-plan must be reference or fast");
+        } else if (o == "--host-verify-only") {
+            s.device_preverify = false;
         } else if (o == "-q") {
             result_.quiet = true;
         } else if (o == "-v") {
@@ -314,6 +318,7 @@ void print_help(std::FILE *stream) {
         "  --batch-size N         denominators per batch, 1..65536 (default 65536)\n"
         "  --square-denominators  treat -dl/-du as bounds on k and search d = k^2\n"
         "  --sieve-plan P         reference or fast (default fast); same points either way\n"
+        "  --host-verify-only     check every modular survivor on the host (no device pre-verification)\n"
         "  --list-devices         print the visible GPUs and exit\n"
         "\n"
         "Search and output options:\n"

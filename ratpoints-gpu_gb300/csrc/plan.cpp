@@ -104,8 +104,9 @@ void two_adic_classes(const std::vector<std::string> &coefficients, std::uint64_
 }
 
 FastPlanner::FastPlanner(const std::vector<std::string> &coefficients, long long bound,
-                         bool class_layout) {
-    for (int q = 3; q < kFastPrimeLimit; q += 2) {
+                         bool class_layout, int prime_limit)
+    : prime_limit_(prime_limit) {
+    for (int q = 3; q < prime_limit; q += 2) {
         bool prime = true;
         for (int f = 3; f * f <= q; f += 2) prime = prime && q % f;
         if (!prime) continue;
@@ -143,16 +144,16 @@ FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long lon
     return FastPlanner(coefficients, bound, class_layout).plan(max_modulus);
 }
 
-FastPlan FastPlanner::plan(int max_modulus) const {
+FastPlan FastPlanner::plan(int max_modulus, int max_slots, long long row_budget, bool by_cost) const {
     FastPlan plan;
     plan.class_prime = class_prime_;
     const std::vector<std::pair<double, int>> &strength = strength_;
-    // Stage-1 moduli: pack primes into at most kMaxFastSlots products below
-    // kMaxModulus.  Each packing puts a prime into the open modulus with the
+    // Stage-1 moduli: pack primes into at most `slots` products below
+    // max_modulus.  Each packing puts a prime into the open modulus with the
     // most headroom that it fits, else opens a new one; it is tried with the
-    // primes ordered by bits and by bits per bit of size, over primes below 72
-    // and below kFastPrimeLimit, and the packing with the most bits is kept.
-    auto pack = [&](std::vector<std::pair<double, int>> order, int limit, bool by_density) {
+    // primes ordered by bits and by bits per bit of size, over primes below 72,
+    // 128 and the planner's limit, and the packing with the most bits is kept.
+    auto pack = [&](std::vector<std::pair<double, int>> order, int limit, bool by_density, int slots) {
         if (by_density)
             std::sort(order.begin(), order.end(),
                       [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
@@ -180,7 +181,7 @@ FastPlan FastPlanner::plan(int max_modulus) const {
                 }
             }
             if (target < 0) {
-                if ((int)out.moduli.size() == kMaxFastSlots) continue;
+                if ((int)out.moduli.size() == slots) continue;
                 out.moduli.push_back(1);
                 out.slots.push_back({});
                 target = int(out.moduli.size()) - 1;
@@ -191,13 +192,31 @@ FastPlan FastPlanner::plan(int max_modulus) const {
         }
         return out;
     };
+    // one packing per row count; the cheapest by the cost model that fits
     FastPlan best_plan = plan;
-    best_plan.bits = -1;
-    for (int limit : {72, kFastPrimeLimit})
-        for (bool density : {false, true}) {
-            FastPlan candidate = pack(strength, limit, density);
-            if (candidate.bits > best_plan.bits) best_plan = candidate;
+    double best_cost = 0;
+    bool found = false;
+    for (int slots = by_cost ? 1 : std::min(max_slots, kMaxFastSlots); slots <= std::min(max_slots, kMaxFastSlots);
+         ++slots) {
+        FastPlan candidate = plan;
+        candidate.bits = -1;
+        for (int limit : {72, kFastPrimeLimit, prime_limit_})
+            for (bool density : {false, true}) {
+                FastPlan packed = pack(strength, std::min(limit, prime_limit_), density, slots);
+                if (packed.bits > candidate.bits) candidate = packed;
+            }
+        if (candidate.moduli.empty()) continue;
+        long long rows = 0;
+        for (int m : candidate.moduli) rows += (m + kFastRowExtension + 1) & ~1;
+        if (rows > row_budget) continue;
+        const double word_survives = 1.0 - std::pow(1.0 - std::exp2(-candidate.bits), 64.0);
+        const double cost = kStageRowCost * double(candidate.moduli.size()) + kSurvivorWordCost * word_survives;
+        if (!found || cost < best_cost - 1e-9) {
+            best_plan = candidate;
+            best_cost = cost;
+            found = true;
         }
+    }
     plan = best_plan;
     if (plan.moduli.empty()) {  // every small prime is weak: keep one modulus anyway
         // (prime to the class prime, so that the class layout can use it)

@@ -55,15 +55,24 @@ double pass_rate(int q, const std::vector<std::string> &coefficients);
 // F(r, d) is a square mod 64, with r odd when d is even (gcd).
 void two_adic_classes(const std::vector<std::string> &coefficients, std::uint64_t out[64]);
 
-// Per-curve choice of the fast plan's small-prime filters (this project's
-// autotuner).  Numerator classes are taken modulo 64 * class_prime (2-adic
-// classes crossed with the admissible residues mod class_prime; class_prime 1
-// means 2-adic classes only); the first-stage rows are products of the other
-// strong small primes, at most kMaxFastSlots of them, each below kMaxModulus.
-constexpr int kMaxFastSlots = 6;
+// Per-curve choice of the fast plan's filters (this project's autotuner).
+// Numerator classes are taken modulo 64 * class_prime (2-adic classes crossed
+// with the admissible residues mod class_prime; class_prime 1 means 2-adic
+// classes only); the first-stage rows are products of the other primes (odd,
+// below the planner's prime limit), at most max_slots of them, each below
+// kMaxModulus.  The number of rows is chosen by a cost model of the fast
+// kernel: stage 1 costs kStageRowCost per row and swept word, stage 2
+// kSurvivorWordCost per word that survives stage 1 (SM cycles, measured on
+// GB300).  Curves that are squares modulo most small primes (dense curves)
+// get more rows, of primes up to 509.
+constexpr int kMaxFastSlots = 12;
 constexpr int kMaxModulus = 1500;
 constexpr int kMaxFastClasses = 256;
-constexpr int kFastPrimeLimit = 128;  // small primes considered: 3 .. 127
+constexpr int kFastPrimeLimit = 128;   // primes of the class prime and the batch's rows: 3 .. 127
+constexpr int kStagePrimeLimit = 512;  // primes of the single-curve rows: 3 .. 509
+constexpr int kFastRowExtension = 96;  // words a staged row extends past its period
+constexpr double kStageRowCost = 0.16;
+constexpr double kSurvivorWordCost = 15.0;
 struct FastPlan {
     int class_prime = 1;
     std::vector<std::vector<int>> slots;   // prime factors of each stage-1 modulus
@@ -80,13 +89,20 @@ FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long lon
 // the class prime), for callers that try several modulus caps.
 class FastPlanner {
 public:
-    FastPlanner(const std::vector<std::string> &coefficients, long long bound, bool class_prime = true);
-    FastPlan plan(int max_modulus = kMaxModulus) const;
+    FastPlanner(const std::vector<std::string> &coefficients, long long bound, bool class_prime = true,
+                int prime_limit = kStagePrimeLimit);
+    // The cheapest plan (cost model above) with at most max_slots rows whose
+    // staged row words, sum of (m + kFastRowExtension) rounded up to even,
+    // stay within row_budget.  by_cost false: the plan with the most filtering
+    // bits in max_slots rows (kernels that sweep a fixed number of rows).
+    FastPlan plan(int max_modulus = kMaxModulus, int max_slots = kMaxFastSlots,
+                  long long row_budget = 1LL << 40, bool by_cost = true) const;
     int class_prime() const { return class_prime_; }
 
 private:
-    std::vector<std::pair<double, int>> strength_;  // (bits, prime) of the odd primes below 128
+    std::vector<std::pair<double, int>> strength_;  // (bits, prime) of the odd primes below the limit
     int class_prime_ = 1;
+    int prime_limit_ = kStagePrimeLimit;
 };
 
 }  // namespace rpg

@@ -195,6 +195,7 @@ SearchMetrics PointSearch::run(const PointCallback &callback) {
     so.square = options.square;
     so.capacity = options.capacity;
     so.device = devices.front().id;
+    so.preverify = options.device_preverify;
     Sieve sieve(options.coefficients, options.numerator_bound, so);
     const int threads = options.verify_threads > 0
                             ? options.verify_threads
@@ -204,13 +205,14 @@ SearchMetrics PointSearch::run(const PointCallback &callback) {
     double verification_ms = 0;
     sieve.start(options.first, options.last, options.batch_size);
     std::vector<Found> batch_points;
-    unsigned long long batch_survivors = 0;
+    unsigned long long batch_survivors = 0, batch_candidates = 0;
     BatchView view;
     bool stopped = false;
     while (!stopped && sieve.next(view)) {
         const auto v0 = Clock::now();
         verify(poly, view.a, view.d, view.count, threads, batch_points);
-        batch_survivors += view.count;
+        batch_survivors += view.modular;
+        batch_candidates += view.count;
         verification_ms += ms_since(v0);
         if (!view.complete) continue;
         std::sort(batch_points.begin(), batch_points.end(), [](const Found &l, const Found &r) {
@@ -221,6 +223,7 @@ SearchMetrics PointSearch::run(const PointCallback &callback) {
         metrics.devices[0].denominator_count += count;
         metrics.devices[0].batches += 1;
         metrics.modular_survivors += batch_survivors;
+        metrics.host_candidates += batch_candidates;
         metrics.exact_survivors += batch_points.size();
         metrics.initial_mask_bytes += (long double)count * (long double)metrics.word_count * 14.0L * 4.0L;
         for (const auto &p : batch_points) {
@@ -230,7 +233,7 @@ SearchMetrics PointSearch::run(const PointCallback &callback) {
             }
         }
         batch_points.clear();
-        batch_survivors = 0;
+        batch_survivors = batch_candidates = 0;
     }
     if (stopped) sieve.cancel();
     const SieveTimings &t = sieve.timings();

@@ -38,6 +38,7 @@ struct SearchOptions {
     PlanKind plan = PlanKind::fast;
     int verify_threads = 0;          // 0: hardware concurrency
     long long capacity = 1 << 22;    // survivors per device buffer
+    bool device_preverify = true;    // drop non-points on the device first (preverify.hpp)
 
     bool accepts(long long numerator, long long denominator) const;
 };
@@ -72,6 +73,7 @@ struct SearchMetrics {
     unsigned long long modular_survivors = 0;
     long double initial_mask_bytes = 0;
     unsigned long long exact_survivors = 0;
+    unsigned long long host_candidates = 0;     // survivors given to the host's exact check
     unsigned long long launches = 0;
     unsigned long long h2d_bytes = 0, d2h_bytes = 0;
     double initial_mask_gbs() const;

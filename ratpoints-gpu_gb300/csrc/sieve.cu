@@ -24,6 +24,7 @@
 #include <deque>
 
 #include "plan.hpp"
+#include "preverify.hpp"
 #include "sieve_device.cuh"
 #include "sieve_fast.cuh"
 
@@ -302,6 +303,10 @@ struct Sieve::Impl {
     dev::u64 *fast_rows = nullptr;
     dev::u64 *fast_adm = nullptr;
     dev::FastClassStart *fast_starts = nullptr;
+    dev::FastRun *list_runs = nullptr;     // class lists by denominator class (see FastTables)
+    int *list_prefix = nullptr;
+    int *list_count = nullptr;
+    long long list_words = 0;              // class words the lists cover (launches from word 0 to at least this)
     int fast_max_classes = 1;
     std::size_t fast_smem = 0;
     std::vector<dev::u64> fast_adm_host;
@@ -314,14 +319,18 @@ struct Sieve::Impl {
     struct Buffer {
         long long *a = nullptr;
         int *d = nullptr;
+        long long *pa = nullptr;  // survivors kept by device pre-verification (same capacity)
+        int *pd = nullptr;
         long long cap = 0;        // entries of a and d
-        unsigned long long *count = nullptr;  // [0] survivors, [1] work counter, [2] error word
+        // [0] survivors, [1] work counter, [2] error word, [3] pre-verified survivors
+        unsigned long long *count = nullptr;
         cudaEvent_t begin = nullptr, end = nullptr;
         long long first = 0, last = 0;
         bool busy = false;
     };
     Buffer buf[2];
-    unsigned long long *h_count = nullptr;  // pinned, one per buffer
+    Preverifier preverifier;
+    unsigned long long *h_count = nullptr;  // pinned, 4 words per buffer
     long long *h_a = nullptr;
     int *h_d = nullptr;
 
@@ -342,6 +351,8 @@ struct Sieve::Impl {
         for (auto &b : buf) {
             cudaFree(b.a);
             cudaFree(b.d);
+            cudaFree(b.pa);
+            cudaFree(b.pd);
             cudaFree(b.count);
             if (b.begin) cudaEventDestroy(b.begin);
             if (b.end) cudaEventDestroy(b.end);
@@ -355,6 +366,12 @@ struct Sieve::Impl {
         fast_adm = nullptr;
         cudaFree(fast_starts);
         fast_starts = nullptr;
+        cudaFree(list_runs);
+        cudaFree(list_prefix);
+        cudaFree(list_count);
+        list_runs = nullptr;
+        list_prefix = nullptr;
+        list_count = nullptr;
         if (h_count) cudaFreeHost(h_count);
         if (h_a) cudaFreeHost(h_a);
         if (h_d) cudaFreeHost(h_d);
@@ -458,18 +475,26 @@ struct Sieve::Impl {
         for (auto &b : buf) {
             b.a = device_alloc<long long>(std::size_t(initial), "cudaMalloc(survivors)");
             b.d = device_alloc<int>(std::size_t(initial), "cudaMalloc(survivors)");
+            if (opt.preverify) {
+                b.pa = device_alloc<long long>(std::size_t(initial), "cudaMalloc(survivors)");
+                b.pd = device_alloc<int>(std::size_t(initial), "cudaMalloc(survivors)");
+            }
             b.cap = initial;
-            b.count = device_alloc<unsigned long long>(3, "cudaMalloc(count)");
+            b.count = device_alloc<unsigned long long>(4, "cudaMalloc(count)");
             check_cuda(cudaEventCreate(&b.begin), "cudaEventCreate");
             check_cuda(cudaEventCreate(&b.end), "cudaEventCreate");
         }
-        check_cuda(cudaMallocHost(&h_count, 2 * sizeof(unsigned long long)), "cudaMallocHost");
+        check_cuda(cudaMallocHost(&h_count, 8 * sizeof(unsigned long long)), "cudaMallocHost");
         check_cuda(cudaMallocHost(&h_a, std::size_t(initial) * sizeof(long long)), "cudaMallocHost");
         check_cuda(cudaMallocHost(&h_d, std::size_t(initial) * sizeof(int)), "cudaMallocHost");
         host_capacity = initial;
         timings.workspace_ms += ms_since(t0);
         if (opt.plan == PlanKind::fast) build_fast_tables(coefficients);
         else build_tables(coefficients);
+        if (opt.preverify) {
+            preverifier.prepare({&coefficients}, stream);
+            timings.h2d_bytes += preverifier.upload_bytes();
+        }
     }
 
     // Fast plan: the per-curve plan (class prime, stage-1 moduli), class-layout
@@ -480,15 +505,14 @@ struct Sieve::Impl {
         // the two staged row sets of a CTA, its queues and its two slots' class
         // runs must fit shared memory at 2 CTAs/SM
         const FastPlanner planner(coefficients, bound);
-        fast_plan = planner.plan();
-        fast_max_classes = max_admissible_classes(coefficients, fast_plan.class_prime);
+        fast_max_classes = max_admissible_classes(coefficients, planner.class_prime());
         const long long row_budget = fast_row_budget(fast_max_classes);
         for (int cap = kMaxModulus;;) {
+            fast_plan = planner.plan(cap, kMaxFastSlots, row_budget);
             int row_words = 0;
             for (int m : fast_plan.moduli) row_words += (m + dev::kFExt + 1) & ~1;
             if (row_words <= row_budget || cap <= 64) break;
             cap = cap * 7 / 8;
-            fast_plan = planner.plan(cap);
         }
         const int n = int(coefficients.size()) - 1;
         const int q = fast_plan.class_prime;
@@ -626,8 +650,67 @@ struct Sieve::Impl {
                 cs.start[sl] = (unsigned short)((Md.neg_h + ofs) % Md.m * Md.inv_stride % Md.m);
             }
         }
+        // class lists by denominator class k = (d mod 64) q + (d mod q), in the
+        // order the producer would lay them out, for launches over whole rows
+        const int maxc = fast_max_classes;
+        const int ncombo = 64 * q;
+        list_words = (F.count_q + 1 + 63) >> 6;
+        std::vector<dev::FastRun> lruns;
+        std::vector<int> lprefix, lcount;
+        if (list_words < (1LL << 23)) {
+            lruns.assign(std::size_t(ncombo) * maxc, dev::FastRun{});
+            lprefix.assign(std::size_t(ncombo) * (maxc + 1), 0);
+            lcount.assign(std::size_t(ncombo), 0);
+            auto nth_bit = [](dev::u64 mask, int k) {
+                for (int i = 0; i < k; ++i) mask &= mask - 1;
+                return __builtin_ctzll(mask);
+            };
+            for (int dd = 0; dd < 64; ++dd)
+                for (int dq = 0; dq < q; ++dq) {
+                    const int k = dd * q + dq;
+                    const dev::u64 classes2 = adm[std::size_t(dd)];
+                    const dev::u64 classesq = q > 1 ? adm[std::size_t(64 + dq)] : dev::u64(1);
+                    const int nq = __builtin_popcountll(classesq);
+                    const int nclass = __builtin_popcountll(classes2) * nq;
+                    if (nclass > maxc) throw std::logic_error("class list longer than the class bound");
+                    int items = 0;
+                    for (int c = 0; c < nclass; ++c) {
+                        const int i2 = c / nq;
+                        const int r64 = nth_bit(classes2, i2);
+                        int r = r64;
+                        if (q > 1) r = r64 + 64 * int(F.crt[F.mod_q[r64] * 13 + nth_bit(classesq, c - i2 * nq)]);
+                        const dev::FastClassStart &cs = starts[std::size_t(r)];
+                        const long long count = F.count_q + (cs.ofs <= F.count_r ? 1 : 0);
+                        const long long cw = (count + 63) >> 6;
+                        const dev::u32 last_bits = cw > 0 ? dev::u32(count - 64 * (cw - 1)) : 64u;
+                        dev::FastRun &run = lruns[std::size_t(k) * maxc + c];
+                        run.words_last = dev::u32(cw) | (cw > 0 ? 1u << 24 : 0u) | ((last_bits - 1) << 25);
+                        run.ofs = cs.ofs;
+                        for (int sl = 0; sl < dev::kFastSlots; ++sl) run.start[sl] = cs.start[sl];
+                        lprefix[std::size_t(k) * (maxc + 1) + c] = items;
+                        items += int((cw + dev::kFItemWords - 1) / dev::kFItemWords);
+                    }
+                    lprefix[std::size_t(k) * (maxc + 1) + nclass] = items;
+                    lcount[std::size_t(k)] = nclass;
+                }
+        }
         timings.plan_ms += ms_since(t0);
         auto t1 = Clock::now();
+        if (!lruns.empty()) {
+            list_runs = device_alloc<dev::FastRun>(lruns.size(), "cudaMalloc(class lists)");
+            list_prefix = device_alloc<int>(lprefix.size(), "cudaMalloc(class lists)");
+            list_count = device_alloc<int>(lcount.size(), "cudaMalloc(class lists)");
+            check_cuda(cudaMemcpyAsync(list_runs, lruns.data(), lruns.size() * sizeof(dev::FastRun),
+                                       cudaMemcpyHostToDevice, stream),
+                       "upload class lists");
+            check_cuda(cudaMemcpyAsync(list_prefix, lprefix.data(), lprefix.size() * sizeof(int),
+                                       cudaMemcpyHostToDevice, stream),
+                       "upload class lists");
+            check_cuda(cudaMemcpyAsync(list_count, lcount.data(), lcount.size() * sizeof(int),
+                                       cudaMemcpyHostToDevice, stream),
+                       "upload class lists");
+            timings.h2d_bytes += lruns.size() * sizeof(dev::FastRun) + (lprefix.size() + lcount.size()) * sizeof(int);
+        }
         fast_rows = device_alloc<dev::u64>(std::size_t(total), "cudaMalloc(class tables)");
         fast_adm = device_alloc<dev::u64>(adm.size(), "cudaMalloc(admissible classes)");
         fast_starts = device_alloc<dev::FastClassStart>(starts.size(), "cudaMalloc(class starts)");
@@ -676,6 +759,9 @@ struct Sieve::Impl {
         F.admissible = fast_adm;
         F.class_starts = fast_starts;
         F.max_classes = fast_max_classes;
+        F.list_runs = list_runs;
+        F.list_prefix = list_prefix;
+        F.list_count = list_count;
         fast_smem = fast_dynamic_smem(F.smem_words, fast_max_classes);
         const void *kernel = fast_kernel_ptr(F.slots);
         check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -702,7 +788,13 @@ struct Sieve::Impl {
         case 3: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<3>);
         case 4: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<4>);
         case 5: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<5>);
-        default: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<6>);
+        case 6: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<6>);
+        case 7: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<7>);
+        case 8: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<8>);
+        case 9: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<9>);
+        case 10: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<10>);
+        case 11: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<11>);
+        default: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<12>);
         }
     }
 
@@ -710,12 +802,12 @@ struct Sieve::Impl {
                      cudaStream_t st) const {
         const int blocks = int(std::min<long long>(grid, (A.k_count + dev::kFChunk - 1) / dev::kFChunk));
         switch (Fl.slots) {
-        case 1: dev::fast_sieve_kernel<1><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
-        case 2: dev::fast_sieve_kernel<2><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
-        case 3: dev::fast_sieve_kernel<3><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
-        case 4: dev::fast_sieve_kernel<4><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
-        case 5: dev::fast_sieve_kernel<5><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
-        default: dev::fast_sieve_kernel<6><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
+#define RPG_FAST_CASE(n)                                                                 \
+    case n: dev::fast_sieve_kernel<n><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
+        RPG_FAST_CASE(1) RPG_FAST_CASE(2) RPG_FAST_CASE(3) RPG_FAST_CASE(4) RPG_FAST_CASE(5) RPG_FAST_CASE(6)
+        RPG_FAST_CASE(7) RPG_FAST_CASE(8) RPG_FAST_CASE(9) RPG_FAST_CASE(10) RPG_FAST_CASE(11)
+        default: dev::fast_sieve_kernel<12><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
+#undef RPG_FAST_CASE
         }
     }
 
@@ -751,6 +843,11 @@ struct Sieve::Impl {
             for (int i = 0; i < kCandidatePrimes; ++i)
                 Fl.prime[i].wlo_mod = dev::u32(A.w_lo % Fl.prime[i].p);
             for (int i = 0; i < Fl.slots; ++i) Fl.mod[i].wlo_mod = dev::u32(A.w_lo % Fl.mod[i].m);
+            if (A.w_lo != 0 || A.w_hi < list_words) {  // part of the class rows: the producer lays them out
+                Fl.list_runs = nullptr;
+                Fl.list_prefix = nullptr;
+                Fl.list_count = nullptr;
+            }
             launch_fast(Fl, A, work, stream);
         } else {
             const int blocks = int(std::min<long long>(grid, A.k_count));
@@ -765,15 +862,20 @@ struct Sieve::Impl {
         b.last = last;
         b.busy = true;
         const dev::SieveArgs A = args(which, first, last, w_lo, w_hi);
-        check_cuda(cudaMemsetAsync(b.count, 0, 3 * sizeof(unsigned long long), stream),
+        check_cuda(cudaMemsetAsync(b.count, 0, 4 * sizeof(unsigned long long), stream),
                    "cudaMemsetAsync");
         check_cuda(cudaEventRecord(b.begin, stream), "cudaEventRecord");
         launch_kernel(A, b.count + 1);
+        if (opt.preverify) {
+            preverifier.launch(b.a, b.d, nullptr, b.count, (unsigned long long)b.cap, b.pa, b.pd, nullptr,
+                               b.count + 3, nullptr, stream);
+            ++timings.launches;
+        }
         check_cuda(cudaEventRecord(b.end, stream), "cudaEventRecord");
-        check_cuda(cudaMemcpyAsync(h_count + which, b.count, sizeof(unsigned long long),
+        check_cuda(cudaMemcpyAsync(h_count + 4 * which, b.count, 4 * sizeof(unsigned long long),
                                    cudaMemcpyDeviceToHost, stream),
                    "download survivor count");
-        timings.d2h_bytes += sizeof(unsigned long long);
+        timings.d2h_bytes += 4 * sizeof(unsigned long long);
         ++timings.launches;
     }
 
@@ -810,23 +912,27 @@ struct Sieve::Impl {
         Buffer &b = buf[which];
         if (!n) return;
         check_cuda(cudaStreamWaitEvent(copy_stream, b.end, 0), "cudaStreamWaitEvent");
-        check_cuda(cudaMemcpyAsync(h_a, b.a, n * sizeof(long long), cudaMemcpyDeviceToHost,
-                                   copy_stream),
+        check_cuda(cudaMemcpyAsync(h_a, opt.preverify ? b.pa : b.a, n * sizeof(long long),
+                                   cudaMemcpyDeviceToHost, copy_stream),
                    "download survivors");
-        check_cuda(cudaMemcpyAsync(h_d, b.d, n * sizeof(int), cudaMemcpyDeviceToHost, copy_stream),
+        check_cuda(cudaMemcpyAsync(h_d, opt.preverify ? b.pd : b.d, n * sizeof(int), cudaMemcpyDeviceToHost,
+                                   copy_stream),
                    "download survivors");
         check_cuda(cudaStreamSynchronize(copy_stream), "download survivors");
         timings.d2h_bytes += n * (sizeof(long long) + sizeof(int));
     }
 
-    void deliver(BatchView &out, int which, std::size_t n, float ms, long long first,
+    // n modular survivors, of which kept (all, without pre-verification) are copied.
+    void deliver(BatchView &out, int which, std::size_t n, std::size_t kept, float ms, long long first,
                  long long last, bool complete) {
-        copy_out(which, n);
+        if (!opt.preverify) kept = n;
+        copy_out(which, kept);
         out.first = first;
         out.last = last;
         out.a = h_a;
         out.d = h_d;
-        out.count = n;
+        out.count = kept;
+        out.modular = n;
         out.kernel_ms = ms;
         out.complete = complete;
     }
@@ -841,11 +947,17 @@ struct Sieve::Impl {
         check_cuda(cudaStreamSynchronize(stream), "sieve stream");
         cudaFree(b.a);
         cudaFree(b.d);
-        b.a = nullptr;
-        b.d = nullptr;
+        cudaFree(b.pa);
+        cudaFree(b.pd);
+        b.a = b.pa = nullptr;
+        b.d = b.pd = nullptr;
         b.cap = 0;
         b.a = device_alloc<long long>(std::size_t(cap), "cudaMalloc(survivors)");
         b.d = device_alloc<int>(std::size_t(cap), "cudaMalloc(survivors)");
+        if (opt.preverify) {
+            b.pa = device_alloc<long long>(std::size_t(cap), "cudaMalloc(survivors)");
+            b.pd = device_alloc<int>(std::size_t(cap), "cudaMalloc(survivors)");
+        }
         b.cap = cap;
         if (host_capacity < cap) {
             cudaFreeHost(h_a);
@@ -895,7 +1007,7 @@ struct Sieve::Impl {
             check_cuda(cudaStreamSynchronize(stream), "sieve kernel");
             buf[which].busy = false;
             check_error_word(which);
-            const unsigned long long n = h_count[which];
+            const unsigned long long n = h_count[4 * which], kept = h_count[4 * which + 3];
             const float ms = elapsed(buf[which]);
             timings.sieve_ms += ms;
             if (n > (unsigned long long)buf[which].cap) {
@@ -904,7 +1016,7 @@ struct Sieve::Impl {
                 else pieces.push_front(p);
                 continue;
             }
-            deliver(out, which, std::size_t(n), ms, piece_batch_first, piece_batch_last,
+            deliver(out, which, std::size_t(n), std::size_t(kept), ms, piece_batch_first, piece_batch_last,
                     pieces.empty());
             return true;
         }
@@ -928,11 +1040,12 @@ struct Sieve::Impl {
         // The count download is queued right after the kernel on the compute stream.
         check_cuda(cudaEventSynchronize(b.end), "sieve kernel");
         check_cuda(cudaStreamWaitEvent(copy_stream, b.end, 0), "cudaStreamWaitEvent");
-        unsigned long long n = 0;
-        check_cuda(cudaMemcpyAsync(&n, b.count, sizeof n, cudaMemcpyDeviceToHost, copy_stream),
+        unsigned long long counts[4] = {};
+        check_cuda(cudaMemcpyAsync(counts, b.count, sizeof counts, cudaMemcpyDeviceToHost, copy_stream),
                    "download survivor count");
         check_cuda(cudaStreamSynchronize(copy_stream), "download survivor count");
-        timings.d2h_bytes += sizeof n;
+        timings.d2h_bytes += sizeof counts;
+        const unsigned long long n = counts[0];
         check_error_word(which);
         const float ms = elapsed(b);
         timings.sieve_ms += ms;
@@ -945,7 +1058,7 @@ struct Sieve::Impl {
             else split_front(Piece{b.first, b.last, 0, words});
             return next_piece(out);
         }
-        deliver(out, which, std::size_t(n), ms, b.first, b.last, true);
+        deliver(out, which, std::size_t(n), std::size_t(counts[3]), ms, b.first, b.last, true);
         b.busy = false;
         refill();
         return true;

@@ -38,6 +38,10 @@ struct SieveOptions {
     bool square = false;            // parameters k give denominators k*k
     long long capacity = 1 << 22;   // survivors per device buffer
     int device = -1;                // -1: current device
+    // Drop survivors that cannot be points on the device before the copy
+    // (gcd and residue tests; see preverify.hpp).  Deliveries then hold a
+    // subset of the modular survivors that still contains every point.
+    bool preverify = false;
 };
 
 // One delivery of survivors.  Pointers stay valid until the next call to
@@ -48,6 +52,7 @@ struct BatchView {
     const long long *a = nullptr;
     const int *d = nullptr;
     std::size_t count = 0;
+    std::size_t modular = 0;         // modular survivors behind this piece (count, unless pre-verified)
     bool complete = true;
     float kernel_ms = 0.0f;          // event time of the launches behind this piece
 };

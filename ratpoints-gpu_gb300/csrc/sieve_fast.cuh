@@ -78,13 +78,24 @@ struct FastPrime {                 // one of the 36 reference candidates, class 
 struct FastClassStart {
     unsigned short start[kFastSlots];
     unsigned short ofs;
-    unsigned short pad;
+    unsigned short pad[3];
 };
-static_assert(sizeof(FastClassStart) == 16, "one 16-byte load per class");
+static_assert(sizeof(FastClassStart) == 32, "two 16-byte loads per class");
+static_assert(kFExt == kFastRowExtension, "the planner sizes rows with the kernel's extension");
+
+struct FastRun;
 
 struct FastTables {
     const FastClassStart *class_starts;  // [M]
     int max_classes;               // most admissible classes of any denominator
+    // Class lists by denominator class k = (d mod 64) q + (d mod q), for
+    // launches over whole class rows (null otherwise): list_count[k] classes,
+    // their runs list_runs[k max_classes ..] and sweep-item prefix
+    // list_prefix[k (max_classes + 1) ..].  A denominator's classes depend on
+    // k alone, so the producer looks them up instead of laying them out.
+    const FastRun *list_runs;
+    const int *list_prefix;
+    const int *list_count;
     const u64 *rows;               // stage-1 modulus tables
     const u64 *prime_rows;         // reference candidate tables (class layout)
     const u64 *admissible;         // [64] 2-adic classes by d mod 64, then [kFAdmQ] residues by d mod q
@@ -166,14 +177,18 @@ struct FastRun {
                                    // valid bits of the class's last word (bits 25..31, 1..64)
     unsigned short ofs;            // (r + H) mod M
     unsigned short start[kFastSlots];  // row index of the tile's first class word, per modulus
+    unsigned short pad;
 };
-static_assert(sizeof(FastRun) == 20, "packed class run");
+static_assert(sizeof(FastRun) == 32, "packed class run");
 
 // A denominator in flight: written by the producer warp, read by the others.
-// Its class runs and item prefix live in dynamic shared memory, sized by the
-// plan's largest class count (FastTables::max_classes).
+// Its class runs and item prefix are its class list in global memory, or laid
+// out by the producer in dynamic shared memory (launches over part of the
+// class rows), sized by the plan's largest class count.
 struct FastSlot {
     long long d;                   // denominator; -1: no more work
+    const FastRun *runs;
+    const int *prefix;
     int nclass;
     int next;                      // sweep-item counter
     unsigned char sel[kSelectedPrimes];  // selected candidates, largest first
@@ -187,10 +202,6 @@ struct FastCtx {
     int d;
     unsigned char sel[kSelectedPrimes];
 };
-
-__device__ __forceinline__ void mbar_arrive(u32 bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
 
 // Stage 2 for up to 32 queued words (one per lane), then emission.  A queued
 // word carries its denominator context (bits 56..57) and the position
@@ -257,15 +268,9 @@ __device__ __forceinline__ void fast_drain(const u64 *qmask, const u64 *qpos, in
     }
 }
 
-// Producer work for denominator d into slot S (the whole warp): the 32
-// largest candidates not dividing d (two ballots), then the admissible
-// classes and their sweep items (a prefix scan, 32 classes per pass).
-__device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs &A, long long d,
-                                           FastSlot &S, FastRun *runs, int *prefix) {
+// The 32 largest candidates not dividing d (two ballots), into S.sel.
+__device__ __forceinline__ void fast_select(const FastTables &T, u32 du, FastSlot &S) {
     const int lane = threadIdx.x & 31;
-    const u32 du = u32(d);
-    const int q = T.class_prime;
-    const int M = T.class_mod;
     {
         // lane l tests candidate 35 - l, lanes 0..3 also candidate 3 - l
         const int ch = kCandidatePrimes - 1 - lane;
@@ -282,6 +287,18 @@ __device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs 
         if (lane < kCandidatePrimes - 32 && rl != 0 && rank_l < kSelectedPrimes)
             S.sel[rank_l] = (unsigned char)cl;
     }
+}
+
+// Producer work for denominator d into slot S (the whole warp): the prime
+// selection, then the admissible classes and their sweep items (a prefix
+// scan, 32 classes per pass) in shared memory.
+__device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs &A, long long d,
+                                           FastSlot &S, FastRun *runs, int *prefix) {
+    const int lane = threadIdx.x & 31;
+    const u32 du = u32(d);
+    const int q = T.class_prime;
+    const int M = T.class_mod;
+    fast_select(T, du, S);
     const u64 classes2 = __ldg(T.admissible + (du & 63));
     const u64 classesq =
         q > 1 ? __ldg(T.admissible + 64 + int(mod_u32(du, u32(q), (~0ull) / u32(q) + 1))) : u64(1);
@@ -334,6 +351,8 @@ __device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs 
     }
     if (lane == 0) {
         prefix[nclass] = carry;
+        S.runs = runs;
+        S.prefix = prefix;
         S.nclass = nclass;
         S.next = 0;
         S.d = d;
@@ -371,6 +390,7 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
         // ---- producer: next live denominator into the next free slot ----
         const int q = T.class_prime;
         const unsigned long long magic_q = (~0ull) / u32(q) + 1;  // q >= 1: mod_u32 constant
+        const bool lists = T.list_count != nullptr;
         long long chunk = 0;
         int j = kFChunk;                 // position inside the fetched chunk
         int uses0 = 0, uses1 = 0;        // fills of each slot so far
@@ -378,6 +398,7 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
         bool failed = false;
         for (;;) {
             long long d = -1;
+            int combo = 0, list_n = 0;
             for (;;) {
                 if (j == kFChunk) {
                     unsigned long long base = 0;
@@ -394,9 +415,15 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
                 const long long k = A.k_first + idx;
                 const long long dd = A.square ? k * k : k;
                 const u32 du = u32(dd);
-                if (__ldg(T.admissible + (du & 63)) == 0) continue;
-                if (q > 1 && __ldg(T.admissible + 64 + int(mod_u32(du, u32(q), magic_q))) == 0)
-                    continue;
+                if (lists) {
+                    combo = int(du & 63) * q + (q > 1 ? int(mod_u32(du, u32(q), magic_q)) : 0);
+                    list_n = __ldg(T.list_count + combo);
+                    if (list_n == 0) continue;
+                } else {
+                    if (__ldg(T.admissible + (du & 63)) == 0) continue;
+                    if (q > 1 && __ldg(T.admissible + 64 + int(mod_u32(du, u32(q), magic_q))) == 0)
+                        continue;
+                }
                 d = dd;
                 break;
             }
@@ -417,7 +444,18 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
                 }
                 break;
             }
-            fast_setup(T, A, d, S, runs0 + b * T.max_classes, prefix0 + b * (T.max_classes + 1));
+            if (lists) {
+                fast_select(T, u32(d), S);
+                if (lane == 0) {
+                    S.runs = T.list_runs + (long long)combo * T.max_classes;
+                    S.prefix = T.list_prefix + (long long)combo * (T.max_classes + 1);
+                    S.nclass = list_n;
+                    S.next = 0;
+                    S.d = d;
+                }
+            } else {
+                fast_setup(T, A, d, S, runs0 + b * T.max_classes, prefix0 + b * (T.max_classes + 1));
+            }
             __syncwarp();
             if (lane == 0) {
                 __threadfence_block();
@@ -487,8 +525,8 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
         const u64 tag = u64(k) << 56;
 
         const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
-        const FastRun *runs = runs0 + b * T.max_classes;
-        const int *prefix = prefix0 + b * (T.max_classes + 1);
+        const FastRun *runs = S.runs;
+        const int *prefix = S.prefix;
         const int nclass = S.nclass;
         const int total_items = prefix[nclass];
         u32 step8[NS], mod8[NS];

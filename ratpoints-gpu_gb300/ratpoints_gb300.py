@@ -27,6 +27,7 @@ RPG_SIEVE_SQUARE_DENOMINATORS = 1
 RPG_SIEVE_FAST_PLAN = 2
 RPG_PLAN_REFERENCE = 0
 RPG_PLAN_FAST = 1
+RPG_SEARCH_HOST_VERIFY_ONLY = 1
 STATUS_NAMES = {0: "RPG_OK", 1: "RPG_E_ARG", 2: "RPG_E_CUDA", 3: "RPG_E_OOM",
                 4: "RPG_E_TIMEOUT", 5: "RPG_E_INTERNAL", 6: "RPG_E_NOT_SQUAREFREE"}
 
@@ -53,7 +54,7 @@ class SieveStats(ctypes.Structure):
                [(name, ctypes.c_double) for name in
                 ("basis_ms", "sieve_ms", "plan_ms", "workspace_ms", "basis_wall_ms",
                  "survivor_setup_ms", "verification_ms", "sieve_wall_ms", "initial_mask_bytes")] + \
-               [(name, ctypes.c_uint64) for name in ("h2d_bytes", "d2h_bytes")]
+               [(name, ctypes.c_uint64) for name in ("h2d_bytes", "d2h_bytes", "host_candidates")]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -71,7 +72,8 @@ class SearchOptions(ctypes.Structure):
                 ("intervals", ctypes.POINTER(Interval)), ("interval_count", ctypes.c_int32),
                 ("include_infinity", ctypes.c_int32), ("batch_size", ctypes.c_int32),
                 ("square_denominators", ctypes.c_int32), ("plan", ctypes.c_int32),
-                ("device", ctypes.c_int32), ("verify_threads", ctypes.c_int32)]
+                ("device", ctypes.c_int32), ("verify_threads", ctypes.c_int32),
+                ("flags", ctypes.c_uint32)]
 
 
 class BatchStats(ctypes.Structure):
@@ -82,7 +84,7 @@ class BatchStats(ctypes.Structure):
                  ("rectangle_sites", "plan_ms", "table_ms", "sieve_ms", "wide_ms", "narrow_ms",
                   "verify_ms", "wall_ms")] +
                 [("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
-                 ("graph", ctypes.c_int32)])
+                 ("graph", ctypes.c_int32), ("host_candidates", ctypes.c_uint64)])
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -109,6 +111,7 @@ POINT_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int64, ctypes.c_char_p, ctype
 BATCH_POINT_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int32, ctypes.c_int64, ctypes.c_char_p,
                                   ctypes.c_int64, ctypes.c_void_p)
 RPG_BATCH_NO_GRAPH = 1
+RPG_BATCH_HOST_VERIFY_ONLY = 2
 
 _lib = None
 
@@ -152,6 +155,9 @@ def load():
     lib.rpg_square_root.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
                                     ctypes.c_char_p, ctypes.c_size_t,
                                     ctypes.POINTER(ctypes.c_int32)]
+    lib.rpg_preverify.restype = S
+    lib.rpg_preverify.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
+                                  ctypes.POINTER(ctypes.c_int32)]
     lib.rpg_cli_main.restype = ctypes.c_int32
     lib.rpg_cli_main.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_char_p)]
     lib.rpg_session_create.restype = S
@@ -227,8 +233,9 @@ def sieve(coefficients, bound, first, last, square=False, plan="reference", devi
 
 def point_search(coefficients, bound, first, last, intervals=(), include_infinity=True,
                  batch_size=1 << 16, square=False, plan="fast", device=-1, verify_threads=0,
-                 stop_after=None):
-    """Verified points [(a, y, d)] in output order, plus the stats dict."""
+                 stop_after=None, preverify=True):
+    """Verified points [(a, y, d)] in output order, plus the stats dict.
+    preverify=False sends every modular survivor to the host's exact check."""
     lib = load()
     coeffs = coefficients_of(coefficients)
     points = []
@@ -241,6 +248,7 @@ def point_search(coefficients, bound, first, last, intervals=(), include_infinit
     opts = SearchOptions()
     keep = _fill_options(opts, coeffs, bound, first, last, intervals, include_infinity,
                          batch_size, square, plan, device, verify_threads)
+    opts.flags = 0 if preverify else RPG_SEARCH_HOST_VERIFY_ONLY
     stats = SieveStats()
     _check(lib.rpg_point_search(ctypes.byref(opts), on_point, None, ctypes.byref(stats)))
     del keep
@@ -270,7 +278,7 @@ def _fill_options(opts, coeffs, bound, first, last, intervals=(), include_infini
     return (ivs, cstr)
 
 
-def batch_search(curves, device=-1, graph=True, stop_after=None):
+def batch_search(curves, device=-1, graph=True, stop_after=None, preverify=True):
     """Search many curves in one batched pass.
 
     curves: list of dicts with keys coefficients, bound, first, last and
@@ -296,7 +304,8 @@ def batch_search(curves, device=-1, graph=True, stop_after=None):
     status = (ctypes.c_int32 * max(1, n))()
     survivors = (ctypes.c_uint64 * max(1, n))()
     stats = BatchStats()
-    _check(lib.rpg_batch_search(arr, n, device, 0 if graph else RPG_BATCH_NO_GRAPH, on_point, None,
+    flags = (0 if graph else RPG_BATCH_NO_GRAPH) | (0 if preverify else RPG_BATCH_HOST_VERIFY_ONLY)
+    _check(lib.rpg_batch_search(arr, n, device, flags, on_point, None,
                                 status, survivors, ctypes.byref(stats)))
     del keep
     return points, list(status)[:n], list(survivors)[:n], stats.as_dict()
@@ -368,6 +377,15 @@ def is_squarefree(coefficients):
     out = ctypes.c_int32(-1)
     _check(load().rpg_is_squarefree(_strings(coeffs), len(coeffs), ctypes.byref(out)))
     return bool(out.value)
+
+
+def preverify(coefficients, a, b):
+    """The device pre-verification test of site (a, b), evaluated on the host:
+    False only if (a, b) cannot give a point."""
+    coeffs = coefficients_of(coefficients)
+    flag = ctypes.c_int32(-1)
+    _check(load().rpg_preverify(_strings(coeffs), len(coeffs), int(a), int(b), ctypes.byref(flag)))
+    return bool(flag.value)
 
 
 def square_root(coefficients, a, b):

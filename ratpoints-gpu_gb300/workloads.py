@@ -18,6 +18,10 @@ lists c0 .. cn; sizes and distributions follow the benchmark definitions:
                  coefficient bit length uniform in [16, 128] with a random sign,
                  box a in [-H, H], b in [1, H] with H log-uniform in [10^2, 10^6],
                  30 % asking for the first point only
+  RECORD_CURVE   the genus-2 curve with the most known rational points (its
+                 points are the reference's known-answer test,
+                 tests/verify_record_curve.py): a dense curve, square modulo
+                 most small primes
 """
 
 from __future__ import annotations
@@ -26,6 +30,9 @@ import math
 import random
 
 import numpy as np
+
+
+RECORD_CURVE = "247747600 -985905640 567207969 2396040466 52485681 -470135160 82342800"
 
 
 def _squarefree(coeffs):

@@ -13,6 +13,11 @@ Run in a checkout where the reference tree is available (default
   (the line "1 14 4" in the square-denominator search).
 * record_curve: the published x-coordinates of tests/data/record_curve_x.txt
   with height <= 10^6 (tests/verify_record_curve.py:17-59).
+* record_full: the record curve at height 10^7 with default options, as the
+  reference's own measurement runs record it: denominators to 10^7 (stdout
+  SHA-256, size and exact points, and the modular survivor count of the
+  32-prime plan; docs/RTX4090-OPTIMIZATION.md:226-234) and to 10^6 (stdout
+  SHA-256 and exact points; docs/RTX4090-SCREEN.json, variant "baseline").
 * c1: a seeded degree-6 curve with coefficients in [-50, 50] on the box
   a in [-2000, 2000], b in [1, 2000]; expected output from the oracle pipeline
   (reference-plan sieve restated in C, exact verification in Python), pinned
@@ -27,6 +32,7 @@ import argparse
 import hashlib
 import json
 import random
+import re
 import sys
 from fractions import Fraction
 from pathlib import Path
@@ -98,6 +104,24 @@ def main():
     record = {"coefficients": RECORD_CURVE, "height": 10 ** 6,
               "x": [f"{x.numerator}/{x.denominator}" for x in within]}
 
+    text = (ref / "docs" / "RTX4090-OPTIMIZATION.md").read_text()
+    shas = set(re.findall(r"SHA-256\s*`([0-9a-f]{64})`", text))
+    assert len(shas) == 1, shas
+    size = int(re.search(r"The output was ([0-9,]+)\s+bytes", text).group(1).replace(",", ""))
+    row32 = re.search(r"^\| 32 \|.*\| ([0-9,]+) \|$", text, re.M).group(1)
+    exact = set(int(n) for n in re.findall(r"([0-9]+) exact points", text))
+    assert len(exact) == 1, exact
+    screen = json.loads((ref / "docs" / "RTX4090-SCREEN.json").read_text())
+    base = next(v for v in screen["variants"] if v["name"] == "baseline")
+    record_full = [
+        {"source": "docs/RTX4090-OPTIMIZATION.md:226-234", "coefficients": RECORD_CURVE,
+         "height": 10 ** 7, "last": 10 ** 7, "sha256": shas.pop(), "bytes": size,
+         "exact_survivors": exact.pop(), "reference_survivors": int(row32.replace(",", ""))},
+        {"source": "docs/RTX4090-SCREEN.json", "coefficients": RECORD_CURVE,
+         "height": base["height"], "last": base["denominator_max"], "sha256": base["output_sha256"],
+         "exact_survivors": base["exact_survivors"]},
+    ]
+
     c1 = c1_curve()
     c1_stdout = pipeline_output(c1, 2000, 1, 2000).decode()
     pin = ref_tests.oracle(c1, 2000, 1, 40).decode()
@@ -109,7 +133,7 @@ def main():
                   "pinned_sub_box_last": 40}
 
     out = {"oracle_cases": cases, "dense": dense, "square_kat": square_kat,
-           "record_curve": record, "c1": c1_fixture}
+           "record_curve": record, "record_full": record_full, "c1": c1_fixture}
     (HERE / "golden.json").write_text(json.dumps(out, indent=1) + "\n")
     print(f"wrote {HERE / 'golden.json'}: {len(cases)} oracle cases, "
           f"{len(within)} record-curve points, C1 curve {c1!r} "

@@ -96,6 +96,29 @@ def test_record_curve_published_points(rpg, golden):
     assert len(found) == 301
 
 
+@pytest.mark.parametrize("index", [0, 1], ids=["b1e7", "b1e6"])
+def test_record_curve_full_box(rpg, golden, index):
+    # the reference's own full-box runs: stdout SHA-256 and exact points at height 10^7
+    case = golden["record_full"][index]
+    result = rpg.cli([case["coefficients"], case["height"], "-du", case["last"], "-v"])
+    assert result.returncode == 0, result.stderr
+    assert hashlib.sha256(result.stdout).hexdigest() == case["sha256"]
+    if "bytes" in case:
+        assert len(result.stdout) == case["bytes"]
+    assert rpg.parse_metrics(result.stderr)["exact_survivors"] == case["exact_survivors"]
+
+
+def test_record_curve_reference_plan_survivors(rpg, golden):
+    # 32-prime plan on the full 10^7 box: the reference's modular survivor count
+    case = golden["record_full"][0]
+    result = rpg.cli([case["coefficients"], case["height"], "-v", "--sieve-plan", "reference"])
+    assert result.returncode == 0, result.stderr
+    assert hashlib.sha256(result.stdout).hexdigest() == case["sha256"]
+    metrics = rpg.parse_metrics(result.stderr)
+    assert metrics["survivors"] == case["reference_survivors"]
+    assert metrics["exact_survivors"] == case["exact_survivors"]
+
+
 def test_c1_configuration(rpg, golden):
     c1 = golden["c1"]
     for plan in ("reference", "fast"):
