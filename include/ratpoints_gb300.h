@@ -144,6 +144,20 @@ rpg_status rpg_square_root(const char *const *coefficients, int32_t coefficient_
                            int64_t numerator, int64_t denominator, char *ordinate,
                            size_t ordinate_capacity, int32_t *is_point);
 
+/* The fast plan a single-curve search uses (host only, no device needed):
+ * numerator classes modulo 64 * class_prime, and the stage-1 row moduli with
+ * their prime factors (factors[i][0..3], 0-padded) and filtering bits.  No
+ * counterpart in the reference, whose prime set is fixed. */
+typedef struct rpg_fast_plan_info {
+    int32_t class_prime;
+    int32_t modulus_count;
+    int32_t moduli[16];
+    int32_t factors[16][4];
+    double bits;
+} rpg_fast_plan_info;
+rpg_status rpg_fast_plan(const char *const *coefficients, int32_t coefficient_count, int64_t numerator_bound,
+                         rpg_fast_plan_info *plan);
+
 /* The device pre-verification test of one site, evaluated on the host:
  * *may_be_point = 0 iff gcd(a, d) != 1 or F(a, d) fails a residue test that
  * every square passes (mod 2^64, the primes 3..97, four primes below 2^31).

@@ -77,6 +77,8 @@ struct WideCurve {
     int inv64_q;                   // 64^-1 mod q (CRT)
     int smem_words;
     int list_max;                  // class-list stride: most classes of one denominator
+    int list_steps;                // classes of at most 128 words: 32-word steps per class
+                                   // (their items are kWK classes swept side by side); else 0
     int square;
     int index;                     // position in the caller's curve list
     unsigned short neg_h[kCandidatePrimes];   // (-H) mod p
@@ -303,8 +305,8 @@ __device__ __forceinline__ void select_warp(u32 du, const Candidates &cand,
 // selected primes: f(a/d) mod p must be a square.  residue(ci, p, magic)
 // returns base mod p; step_mod(ci) returns step mod p; aff holds the curve's
 // 36 candidate bitmasks in shared memory.
-template <typename Residue, typename StepMod>
-__device__ __forceinline__ u64 stage2(u64 m, const int *s_ci, const u32 *s_dinv,
+template <typename Residue, typename StepMod, typename Index, typename Inverse>
+__device__ __forceinline__ u64 stage2(u64 m, const Index *s_ci, const Inverse *s_dinv,
                                       const Candidates &cand, const u64 *aff, Residue residue,
                                       StepMod step_mod) {
     for (int s = 0; s < kSelectedPrimes && m; ++s) {
@@ -392,12 +394,16 @@ static_assert(sizeof(ClassStart) == 16, "one 16-byte load per class");
 // A denominator in flight: written by the producer warp, read by the others.
 struct WideSlot {
     long long d;                   // -1: no more work
-    const WideRun *runs;           // class list (global) or laid-out runs (shared)
+    const WideRun *runs;           // the denominator's class runs (shared memory)
     const int *prefix;             // sweep-item prefix of the runs
+    unsigned long long magic[kWideSlots];  // the curve's stage-1 moduli: mod_u32 constants,
+    u32 m[kWideSlots];             //   moduli,
+    u32 step8[kWideSlots];         //   8 ((32 kWK) mod m): byte advance per step,
+    u32 soff[kWideSlots];          //   byte offsets of the staged rows
     int curve;
     int nclass;
     int next;                      // sweep-item counter
-    int pad;
+    int steps;                     // > 0: items are groups of kWK short classes, this many steps
     unsigned char sel[kSelectedPrimes];
     unsigned short dinv[kSelectedPrimes];
 };
@@ -623,12 +629,29 @@ __global__ void __launch_bounds__(kWThreads, 2)
             const u32 du = u32(d);
             const WideCurve &C = curves[item.curve];
             select_warp(du, cand, inv_table, S.sel, S.dinv);
+            if (lane < kWideSlots) {
+                const Modulus &Md = C.mod[lane];
+                S.magic[lane] = Md.magic;
+                S.m[lane] = u32(Md.m);
+                S.step8[lane] = 8u * Md.step;
+                S.soff[lane] = 8u * u32(Md.smem_offset);
+            }
             if (lists >= 0) {
+                // the class list of d's class, copied next to the slot
+                const int lm = C.list_max;
+                const u32 *src = reinterpret_cast<const u32 *>(list_runs + C.list_runs + (long long)combo * lm);
+                WideRun *runs = runs0 + b * max_classes;
+                int *prefix = prefix0 + b * (max_classes + 1);
+                u32 *dst = reinterpret_cast<u32 *>(runs);
+                const int nwords = nlist * int(sizeof(WideRun) / 4);
+                for (int t = lane; t < nwords; t += kWarpSize) dst[t] = __ldg(src + t);
+                const int *psrc = list_prefix + C.list_prefix + (long long)combo * (lm + 1);
+                for (int t = lane; t <= nlist; t += kWarpSize) prefix[t] = __ldg(psrc + t);
                 if (lane == 0) {
-                    const int lm = C.list_max;
-                    S.runs = list_runs + C.list_runs + (long long)combo * lm;
-                    S.prefix = list_prefix + C.list_prefix + (long long)combo * (lm + 1);
+                    S.runs = runs;
+                    S.prefix = prefix;
                     S.nclass = nlist;
+                    S.steps = C.list_steps;
                 }
             } else {
                 WideRun *runs = runs0 + b * max_classes;
@@ -638,6 +661,7 @@ __global__ void __launch_bounds__(kWThreads, 2)
                     S.runs = runs;
                     S.prefix = prefix;
                     S.nclass = nclass;
+                    S.steps = 0;
                 }
             }
             __syncwarp();
@@ -716,87 +740,166 @@ __global__ void __launch_bounds__(kWThreads, 2)
         const u64 tag = u64(kc) << 56;
         const WideCurve &C = curves[S.curve];
         const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
-        u32 step8[kWideSlots], mod8[kWideSlots];
-        const unsigned char *slot_base[kWideSlots];
-#pragma unroll
-        for (int sl = 0; sl < kWideSlots; ++sl) {
-            step8[sl] = 8u * C.mod[sl].step;
-            mod8[sl] = 8u * u32(C.mod[sl].m);
-            slot_base[sl] = sbase + 8 * C.mod[sl].smem_offset;
-        }
         const u64 stride = u64(C.stride);
         const WideRun *runs = S.runs;
         const int *prefix = S.prefix;
         const int nclass = S.nclass;
-        const int total_items = prefix[nclass];
-        for (;;) {
-            int sweep = 0;
-            if (lane == 0) sweep = atomicAdd(const_cast<int *>(&S.next), 1);
-            sweep = __shfl_sync(kFullMask, sweep, 0);
-            if (sweep >= total_items) break;
-            int c = 0;
-            for (int base = 0; base < nclass; base += 32) {
-                const int cc = base + lane;
-                const u32 bb = __ballot_sync(kFullMask, cc < nclass && prefix[cc] <= sweep);
-                if (bb) c = base + 31 - __clz(bb);
-                if (bb != kFullMask) break;
-            }
-            const int w0 = (sweep - prefix[c]) * kWItemWords;
-            const WideRun run = runs[c];
-            const int wt = run.words;
-            const u64 first_mask = ~u64(0) << run.first;
-            const u64 last_mask = run.last >= 64 ? ~u64(0) : ((u64(1) << run.last) - 1);
-            const u64 pos0 = u64(run.ofs) + stride * u64(run.wbase);
-            u32 o[kWideSlots];
-#pragma unroll
-            for (int sl = 0; sl < kWideSlots; ++sl)
-                o[sl] = 8u * mod_u32(u32(run.start[sl]) + u32(w0 + lane), u32(C.mod[sl].m), C.mod[sl].magic);
-#pragma unroll 1
-            for (int step = 0; step < kWSteps; ++step) {
-                const int ws = w0 + step * kWarpSize * kWK;
-                if (ws >= wt) break;
-                // a class's last step often covers fewer than kWK groups of
-                // 32 words (short rows): the groups past its end are skipped
-                const int nk = min(kWK, (wt - ws + kWarpSize - 1) / kWarpSize);
-                u64 acc[kWK];
-#pragma unroll
-                for (int kk = 0; kk < kWK; ++kk)
-                    acc[kk] = kk < nk ? *reinterpret_cast<const u64 *>(slot_base[0] + o[0] + 256 * kk) : 0;
-#pragma unroll
-                for (int sl = 1; sl < kWideSlots; ++sl) {
-#pragma unroll
-                    for (int kk = 0; kk < kWK; ++kk)
-                        if (kk < nk) acc[kk] &= *reinterpret_cast<const u64 *>(slot_base[sl] + o[sl] + 256 * kk);
-                }
-#pragma unroll
-                for (int sl = 0; sl < kWideSlots; ++sl) {
-                    // advance (32 kWK) mod m words; unsigned min wraps into [0, m)
-                    const u32 t = o[sl] + step8[sl];
-                    o[sl] = min(t, t - mod8[sl]);
-                }
-                const u64 any = acc[0] | acc[1] | acc[2] | acc[3];
-                if (!__ballot_sync(kFullMask, any != 0)) continue;
+        const int nsteps = S.steps;
+        if (nsteps > 0) {
+            // Short classes (at most 128 words): an item is kWK classes side
+            // by side, group kk of a lane's words taken from class kk, so a
+            // step covers 32 words of each; a lane's word w of a class is row
+            // word (start + lane) mod m + 32 s, inside the row's 96-word
+            // extension.  o holds byte offsets from the slot's row base.
+            for (;;) {
+                int g = 0;
+                if (lane == 0) g = atomicAdd(const_cast<int *>(&S.next), 1);
+                g = __shfl_sync(kFullMask, g, 0);
+                if (g * kWK >= nclass) break;
+                u32 o[kWideSlots][kWK];
+                u32 meta[kWK];  // class words (bits 0..7), valid bits of its last word (8..15), ofs (16..31)
 #pragma unroll
                 for (int kk = 0; kk < kWK; ++kk) {
-                    if (kk >= nk) break;
-                    const int w = ws + kWarpSize * kk + lane;
-                    u64 a = acc[kk];
-                    if (w == 0) a &= first_mask;
-                    if (w == wt - 1) a &= last_mask;
-                    const bool live_word = a != 0 && w < wt;
-                    const u32 bb = __ballot_sync(kFullMask, live_word);
-                    if (bb) {
-                        const int at = qn + __popc(bb & lanemask_lt());
-                        if (live_word) {
-                            wq_mask[at] = a;
-                            wq_pos[at] = tag | (pos0 + stride * u64(w));
+                    const int cc = g * kWK + kk;
+                    meta[kk] = 0;
+#pragma unroll
+                    for (int sl = 0; sl < kWideSlots; ++sl) o[sl][kk] = S.soff[sl];
+                    if (cc < nclass) {
+                        const WideRun run = runs[cc];
+                        meta[kk] = u32(run.words) | (u32(run.last) << 8) | (u32(run.ofs) << 16);
+#pragma unroll
+                        for (int sl = 0; sl < kWideSlots; ++sl) {
+                            const u32 m = S.m[sl];
+                            const u32 v = u32(run.start[sl]) + u32(lane);
+                            o[sl][kk] += 8u * (m >= 32 ? (v >= m ? v - m : v) : mod_u32(v, m, S.magic[sl]));
                         }
-                        qn += __popc(bb);
-                        if (qn >= 32) {
-                            __syncwarp();
-                            wide_drain(wq_mask, wq_pos, qn - 32, 32, curves, affine, cand, ctx, out);
-                            qn -= 32;
-                            if (qn == 0) oldest = seq;
+                    }
+                }
+#pragma unroll 1
+                for (int step = 0; step < nsteps; ++step) {
+                    u64 acc[kWK];
+#pragma unroll
+                    for (int kk = 0; kk < kWK; ++kk)
+                        acc[kk] = *reinterpret_cast<const u64 *>(sbase + o[0][kk] + 256 * step);
+#pragma unroll
+                    for (int sl = 1; sl < kWideSlots; ++sl) {
+#pragma unroll
+                        for (int kk = 0; kk < kWK; ++kk)
+                            acc[kk] &= *reinterpret_cast<const u64 *>(sbase + o[sl][kk] + 256 * step);
+                    }
+                    const int w = kWarpSize * step + lane;
+#pragma unroll
+                    for (int kk = 0; kk < kWK; ++kk) {
+                        const int wk = int(meta[kk] & 0xFFu);
+                        if (w == wk - 1) {
+                            const u32 last = (meta[kk] >> 8) & 0xFFu;
+                            if (last < 64) acc[kk] &= (u64(1) << last) - 1;
+                        }
+                        if (w >= wk) acc[kk] = 0;
+                    }
+                    const u64 any = acc[0] | acc[1] | acc[2] | acc[3];
+                    if (!__ballot_sync(kFullMask, any != 0)) continue;
+#pragma unroll
+                    for (int kk = 0; kk < kWK; ++kk) {
+                        const bool live_word = acc[kk] != 0;
+                        const u32 bb = __ballot_sync(kFullMask, live_word);
+                        if (bb) {
+                            const int at = qn + __popc(bb & lanemask_lt());
+                            if (live_word) {
+                                wq_mask[at] = acc[kk];
+                                wq_pos[at] = tag | (u64(meta[kk] >> 16) + stride * u64(w));
+                            }
+                            qn += __popc(bb);
+                            if (qn >= 32) {
+                                __syncwarp();
+                                wide_drain(wq_mask, wq_pos, qn - 32, 32, curves, affine, cand, ctx, out);
+                                qn -= 32;
+                                if (qn == 0) oldest = seq;
+                            }
+                        }
+                    }
+                }
+            }
+        } else {
+            u32 step8[kWideSlots], mod8[kWideSlots];
+            const unsigned char *slot_base[kWideSlots];
+#pragma unroll
+            for (int sl = 0; sl < kWideSlots; ++sl) {
+                step8[sl] = S.step8[sl];
+                mod8[sl] = 8u * S.m[sl];
+                slot_base[sl] = sbase + S.soff[sl];
+            }
+            const int total_items = prefix[nclass];
+            int c = 0;  // this warp's items of a slot only increase: so do their classes
+            for (;;) {
+                int sweep = 0;
+                if (lane == 0) sweep = atomicAdd(const_cast<int *>(&S.next), 1);
+                sweep = __shfl_sync(kFullMask, sweep, 0);
+                if (sweep >= total_items) break;
+                // class index: largest c with prefix[c] <= sweep, from the last one on
+                for (int base = c; base < nclass; base += 32) {
+                    const int cc = base + lane;
+                    const u32 bb = __ballot_sync(kFullMask, cc < nclass && prefix[cc] <= sweep);
+                    if (bb) c = base + 31 - __clz(bb);
+                    if (bb != kFullMask) break;
+                }
+                const int w0 = (sweep - prefix[c]) * kWItemWords;
+                const WideRun run = runs[c];
+                const int wt = run.words;
+                const u64 first_mask = ~u64(0) << run.first;
+                const u64 last_mask = run.last >= 64 ? ~u64(0) : ((u64(1) << run.last) - 1);
+                const u64 pos0 = u64(run.ofs) + stride * u64(run.wbase);
+                u32 o[kWideSlots];
+#pragma unroll
+                for (int sl = 0; sl < kWideSlots; ++sl)
+                    o[sl] = 8u * mod_u32(u32(run.start[sl]) + u32(w0 + lane), S.m[sl], S.magic[sl]);
+#pragma unroll 1
+                for (int step = 0; step < kWSteps; ++step) {
+                    const int ws = w0 + step * kWarpSize * kWK;
+                    if (ws >= wt) break;
+                    // a class's last step often covers fewer than kWK groups of
+                    // 32 words (short rows): the groups past its end are skipped
+                    const int nk = min(kWK, (wt - ws + kWarpSize - 1) / kWarpSize);
+                    u64 acc[kWK];
+#pragma unroll
+                    for (int kk = 0; kk < kWK; ++kk)
+                        acc[kk] = kk < nk ? *reinterpret_cast<const u64 *>(slot_base[0] + o[0] + 256 * kk) : 0;
+#pragma unroll
+                    for (int sl = 1; sl < kWideSlots; ++sl) {
+#pragma unroll
+                        for (int kk = 0; kk < kWK; ++kk)
+                            if (kk < nk) acc[kk] &= *reinterpret_cast<const u64 *>(slot_base[sl] + o[sl] + 256 * kk);
+                    }
+#pragma unroll
+                    for (int sl = 0; sl < kWideSlots; ++sl) {
+                        // advance (32 kWK) mod m words; unsigned min wraps into [0, m)
+                        const u32 t = o[sl] + step8[sl];
+                        o[sl] = min(t, t - mod8[sl]);
+                    }
+                    const u64 any = acc[0] | acc[1] | acc[2] | acc[3];
+                    if (!__ballot_sync(kFullMask, any != 0)) continue;
+#pragma unroll
+                    for (int kk = 0; kk < kWK; ++kk) {
+                        if (kk >= nk) break;
+                        const int w = ws + kWarpSize * kk + lane;
+                        u64 a = acc[kk];
+                        if (w == 0) a &= first_mask;
+                        if (w == wt - 1) a &= last_mask;
+                        const bool live_word = a != 0 && w < wt;
+                        const u32 bb = __ballot_sync(kFullMask, live_word);
+                        if (bb) {
+                            const int at = qn + __popc(bb & lanemask_lt());
+                            if (live_word) {
+                                wq_mask[at] = a;
+                                wq_pos[at] = tag | (pos0 + stride * u64(w));
+                            }
+                            qn += __popc(bb);
+                            if (qn >= 32) {
+                                __syncwarp();
+                                wide_drain(wq_mask, wq_pos, qn - 32, 32, curves, affine, cand, ctx, out);
+                                qn -= 32;
+                                if (qn == 0) oldest = seq;
+                            }
                         }
                     }
                 }
@@ -1270,9 +1373,9 @@ int wide_classes(const std::vector<std::string> &coefficients, const dev::u64 ad
     return most2 * std::max(1, mostq);
 }
 
-// max_classes: the most classes of any wide curve with x intervals in the
-// launch (their classes are laid out in shared memory), which sizes the
-// launch's class arrays and so the share of shared memory left for rows.
+// max_classes: the most classes of a denominator of any wide curve in the
+// launch, which sizes the slots' class arrays and so the share of shared
+// memory left for rows.
 FastPlan wide_plan(const FastPlanner &planner, long double work, int max_classes) {
     int cap = int(std::min<long double>(kMaxModulus, std::max<long double>(64, std::sqrt(work / 48.0L))));
     // two slots of staged rows
@@ -1309,7 +1412,7 @@ struct BatchPlan {
     std::vector<int> list_prefix, list_count;
     long long aff_words = 0, pattern_words = 0, row_words = 0;
     int wide_smem_words = 0;
-    int wide_max_classes = 1;   // most classes of a denominator of a wide curve with x intervals
+    int wide_max_classes = 1;   // most classes of a denominator of any wide curve
 };
 
 // Validation and per-curve plans (one curve per task), then descriptors,
@@ -1360,11 +1463,10 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
         }
     });
     // wide plans: one row budget for the launch, from the largest class count
-    // of the curves whose classes are laid out in shared memory (x intervals)
-    int max_classes = 0;
+    // of its curves (each slot holds its denominator's classes)
+    int max_classes = 1;
     for (std::size_t i = 0; i < curves.size(); ++i)
-        if (P.work[i].ok && P.work[i].wide && !curves[i].intervals.empty())
-            max_classes = std::max(max_classes, P.work[i].classes);
+        if (P.work[i].ok && P.work[i].wide) max_classes = std::max(max_classes, P.work[i].classes);
     parallel_for(curves.size(), [&](std::size_t i) {
         CurveWork &cw = P.work[i];
         if (!cw.ok) return;
@@ -1564,10 +1666,14 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                         prefix[nclass] = items;
                         P.list_count[C.list_count + k] = nclass;
                     }
+                // classes of at most 128 words are swept kWK at a time
+                const long long max_words = (C.count_q + 1 + 63) >> 6;
+                C.list_steps = max_words <= 4 * dev::kWarpSize ? int((max_words + dev::kWarpSize - 1) / dev::kWarpSize) : 0;
             } else {
+                C.list_steps = 0;
                 C.list_count = -1;
-                P.wide_max_classes = std::max(P.wide_max_classes, cw.classes);
             }
+            P.wide_max_classes = std::max(P.wide_max_classes, cw.classes);
             // items of about 2^20 row words, one set per numerator range
             const long long chunk = std::max(1LL, std::min<long long>(1 << 16, (1LL << 20) / cw.words));
             for (int range = 0; range < std::max(1, C.nint); ++range)
@@ -1777,11 +1883,68 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
     BatchStats stats;
     std::vector<BatchCurveResult> results(curves.size());
     check_cuda(cudaSetDevice(device), "cudaSetDevice");
+    // Curves with huge rows fill the device on their own: batching gains them
+    // nothing, and the single-curve kernel (row count compiled in, stage 2
+    // from class-layout tables) sweeps them faster.  They are validated with
+    // the others, then searched one by one in a thread beside the batched
+    // kernels.
+    std::vector<BatchCurveSpec> batched(curves);
+    std::vector<std::size_t> solo;
+    std::vector<char> is_solo(curves.size(), 0);
+    for (std::size_t i = 0; i < curves.size(); ++i)
+        if (curves[i].last >= curves[i].first && curves[i].bound >= 1 &&
+            word_count64(curves[i].bound) >= kBatchSoloWords) {
+            solo.push_back(i);
+            is_solo[i] = 1;
+            batched[i].first = 1;
+            batched[i].last = 0;
+        }
     BatchPlan P;
     const auto t_plan = Clock::now();
-    build_plan(curves, results, P, stats);
+    build_plan(batched, results, P, stats);
     stats.plan_ms = ms_since(t_plan);
     const std::vector<CurveWork> &work = P.work;
+    std::exception_ptr solo_error;
+    std::thread solo_thread;
+    struct Joiner {
+        std::thread &t;
+        ~Joiner() {
+            if (t.joinable()) t.join();
+        }
+    } joiner{solo_thread};
+    if (!solo.empty())
+        solo_thread = std::thread([&] {
+            try {
+                check_cuda(cudaSetDevice(device), "cudaSetDevice");
+                for (std::size_t i : solo) {
+                    if (results[i].status != 0) continue;
+                    const BatchCurveSpec &c = curves[i];
+                    SearchOptions o;
+                    o.coefficients = c.coefficients;
+                    o.numerator_bound = c.bound;
+                    o.first = c.first;
+                    o.last = c.last;
+                    o.intervals = c.intervals;
+                    o.include_infinity = false;  // added below with the batched curves'
+                    o.devices = {device};
+                    o.square = c.square;
+                    o.plan = PlanKind::fast;
+                    o.device_preverify = preverify;
+                    PointSearch search(o);
+                    std::vector<PointPair> found;
+                    const SearchMetrics m = search.run([&](const PointPair &p) {
+                        found.push_back(p);
+                        return true;
+                    });
+                    results[i].points = std::move(found);
+                    results[i].survivors = m.modular_survivors;
+                    results[i].wide = true;
+                    results[i].solo = true;
+                }
+            } catch (...) {
+                solo_error = std::current_exception();
+            }
+        });
 
     if (!P.wide.empty() || !P.narrow.empty()) {
         d_wide.upload(P.wide, stream, stats.h2d_bytes, "upload wide curves");
@@ -2006,6 +2169,27 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
     }
     // the point at infinity first, as a single search reports it
     parallel_for(curves.size(), [&](std::size_t i) {
+        if (!work[i].ok || !curves[i].include_infinity || is_solo[i]) return;
+        std::string root;
+        if (work[i].poly->square_root(1, 0, root))
+            results[i].points.insert(results[i].points.begin(), PointPair{1, root, 0});
+    });
+    if (solo_thread.joinable()) solo_thread.join();
+    if (solo_error) std::rethrow_exception(solo_error);
+    for (std::size_t i : solo)
+        if (results[i].status == 0) {
+            const BatchCurveSpec &c = curves[i];
+            const long long count = c.last - c.first + 1;
+            ++stats.solo_curves;
+            ++stats.curves;
+            ++stats.wide_curves;
+            stats.survivors += results[i].survivors;
+            stats.denominators += (unsigned long long)count;
+            stats.rectangle_sites += (long double)(2 * c.bound + 1) * (long double)count;
+        }
+    // the point at infinity first, as a single search reports it
+    parallel_for(solo.size(), [&](std::size_t j) {
+        const std::size_t i = solo[j];
         if (!work[i].ok || !curves[i].include_infinity) return;
         std::string root;
         if (work[i].poly->square_root(1, 0, root))

@@ -29,6 +29,10 @@
 namespace rpg {
 
 constexpr long long kBatchWideWords = 2048;
+// Rows of at least this many words (numerator bounds above about 4.2e6) make
+// a curve fill the device alone; a batch searches such curves one by one with
+// the single-curve kernel, beside its batched kernels.
+constexpr long long kBatchSoloWords = 1LL << 17;
 constexpr int kBatchNarrowModulus = 34;
 
 struct BatchCurveSpec {
@@ -46,6 +50,7 @@ struct BatchCurveResult {
     std::vector<PointPair> points;     // the order of a single-curve search
     unsigned long long survivors = 0;  // modular survivors of the batched sieve
     bool wide = false;                 // which kernel swept the curve
+    bool solo = false;                 // huge rows: searched alone by the single-curve kernel
     int class_prime = 1;
     std::vector<int> moduli;           // stage-1 moduli the autotuner chose
 };
@@ -53,6 +58,7 @@ struct BatchCurveResult {
 struct BatchStats {
     unsigned long long curves = 0, wide_curves = 0, denominators = 0, survivors = 0, points = 0;
     unsigned long long host_candidates = 0;   // survivors given to the host's exact check
+    unsigned long long solo_curves = 0;       // curves with huge rows searched alone
     unsigned long long wide_items = 0, narrow_items = 0, launches = 0, words = 0;
     unsigned long long table_words = 0;
     unsigned long long swept_words = 0;       // 64-site words the sieve kernels sweep (no intervals)

@@ -219,6 +219,27 @@ rpg_status rpg_point_search(const rpg_search_options *o, rpg_point_cb callback, 
     });
 }
 
+rpg_status rpg_fast_plan(const char *const *coefficients, int32_t coefficient_count, int64_t numerator_bound,
+                         rpg_fast_plan_info *plan) {
+    return guarded([&]() -> rpg_status {
+        std::vector<std::string> coeffs;
+        std::string error;
+        if (!coefficients_from(coefficients, coefficient_count, coeffs, error)) return fail(RPG_E_ARG, error);
+        if (!plan) return fail(RPG_E_ARG, "output must not be NULL");
+        if (numerator_bound < 1) return fail(RPG_E_ARG, "maximum height must be positive");
+        const rpg::FastPlan p = rpg::single_curve_plan(coeffs, numerator_bound, nullptr);
+        std::memset(plan, 0, sizeof *plan);
+        plan->class_prime = p.class_prime;
+        plan->modulus_count = int32_t(p.moduli.size());
+        for (std::size_t i = 0; i < p.moduli.size() && i < 16; ++i) {
+            plan->moduli[i] = p.moduli[i];
+            for (std::size_t f = 0; f < p.slots[i].size() && f < 4; ++f) plan->factors[i][f] = p.slots[i][f];
+        }
+        plan->bits = p.bits;
+        return RPG_OK;
+    });
+}
+
 rpg_status rpg_preverify(const char *const *coefficients, int32_t coefficient_count, int64_t numerator,
                          int64_t denominator, int32_t *may_be_point) {
     return guarded([&]() -> rpg_status {

@@ -105,14 +105,17 @@ void two_adic_classes(const std::vector<std::string> &coefficients, std::uint64_
 
 FastPlanner::FastPlanner(const std::vector<std::string> &coefficients, long long bound,
                          bool class_layout, int prime_limit)
-    : prime_limit_(prime_limit) {
-    for (int q = 3; q < prime_limit; q += 2) {
-        bool prime = true;
-        for (int f = 3; f * f <= q; f += 2) prime = prime && q % f;
-        if (!prime) continue;
-        const double rate = pass_rate(q, coefficients);
-        strength_.push_back({rate > 0 ? -std::log2(rate) : 8.0, q});
-    }
+    : prime_limit_(std::min(prime_limit, kFastPrimeLimit)) {
+    auto add_primes = [&](int lo, int hi) {
+        for (int q = lo | 1; q < hi; q += 2) {
+            bool prime = q > 2;
+            for (int f = 3; f * f <= q; f += 2) prime = prime && q % f;
+            if (!prime) continue;
+            const double rate = pass_rate(q, coefficients);
+            strength_.push_back({rate > 0 ? -std::log2(rate) : 8.0, q});
+        }
+    };
+    add_primes(3, prime_limit_);
     // Class prime: the strongest of 3..13 whose classes stay long enough
     // (at least 256 words of 64 sites per class) and few enough: admissible
     // 2-adic classes times admissible residues mod q (q | d admits every
@@ -137,6 +140,14 @@ FastPlanner::FastPlanner(const std::vector<std::string> &coefficients, long long
             class_prime_ = q;
         }
     }
+    // Larger primes (rows of one prime each, about one bit) only for curves
+    // that small primes filter weakly: with at least kDenseCurveBits from six
+    // rows of small primes the cost model never takes them, and computing
+    // their pass rates is most of the planning time of high-degree curves.
+    if (prime_limit > prime_limit_ && plan(kMaxModulus, 6, 1LL << 40, false).bits < kDenseCurveBits) {
+        add_primes(prime_limit_, prime_limit);
+        prime_limit_ = prime_limit;
+    }
 }
 
 FastPlan choose_fast_plan(const std::vector<std::string> &coefficients, long long bound,
@@ -153,7 +164,8 @@ FastPlan FastPlanner::plan(int max_modulus, int max_slots, long long row_budget,
     // most headroom that it fits, else opens a new one; it is tried with the
     // primes ordered by bits and by bits per bit of size, over primes below 72,
     // 128 and the planner's limit, and the packing with the most bits is kept.
-    auto pack = [&](std::vector<std::pair<double, int>> order, int limit, bool by_density, int slots) {
+    auto pack = [&](std::vector<std::pair<double, int>> order, int limit, bool by_density, int slots,
+                    int cap) {
         if (by_density)
             std::sort(order.begin(), order.end(),
                       [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
@@ -170,13 +182,13 @@ FastPlan FastPlanner::plan(int max_modulus, int max_slots, long long row_budget,
         out.class_prime = plan.class_prime;
         for (const auto &s : order) {
             const int q = s.second;
-            if (q >= limit || q == plan.class_prime || s.first < 0.3 || q > max_modulus) continue;
+            if (q >= limit || q == plan.class_prime || s.first < 0.3 || q > cap) continue;
             int target = -1;
             long long headroom = -1;
             for (std::size_t i = 0; i < out.moduli.size(); ++i) {
                 const long long product = (long long)out.moduli[i] * q;
-                if (product <= max_modulus && (long long)max_modulus - product > headroom) {
-                    headroom = max_modulus - product;
+                if (product <= cap && (long long)cap - product > headroom) {
+                    headroom = cap - product;
                     target = int(i);
                 }
             }
@@ -192,19 +204,26 @@ FastPlan FastPlanner::plan(int max_modulus, int max_slots, long long row_budget,
         }
         return out;
     };
-    // one packing per row count; the cheapest by the cost model that fits
+    // one packing per row count, its moduli capped (from max_modulus down by
+    // 1/8 steps) until its rows fit the budget; the cheapest by the cost model
     FastPlan best_plan = plan;
     double best_cost = 0;
     bool found = false;
     for (int slots = by_cost ? 1 : std::min(max_slots, kMaxFastSlots); slots <= std::min(max_slots, kMaxFastSlots);
          ++slots) {
         FastPlan candidate = plan;
-        candidate.bits = -1;
-        for (int limit : {72, kFastPrimeLimit, prime_limit_})
-            for (bool density : {false, true}) {
-                FastPlan packed = pack(strength, std::min(limit, prime_limit_), density, slots);
-                if (packed.bits > candidate.bits) candidate = packed;
-            }
+        for (int cap = max_modulus;; cap = cap * 7 / 8) {
+            candidate = plan;
+            candidate.bits = -1;
+            for (int limit : {72, kFastPrimeLimit, prime_limit_})
+                for (bool density : {false, true}) {
+                    FastPlan packed = pack(strength, std::min(limit, prime_limit_), density, slots, cap);
+                    if (packed.bits > candidate.bits) candidate = packed;
+                }
+            long long rows = 0;
+            for (int m : candidate.moduli) rows += (m + kFastRowExtension + 1) & ~1;
+            if (rows <= row_budget || cap <= 64) break;
+        }
         if (candidate.moduli.empty()) continue;
         long long rows = 0;
         for (int m : candidate.moduli) rows += (m + kFastRowExtension + 1) & ~1;

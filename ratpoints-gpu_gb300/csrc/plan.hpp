@@ -71,8 +71,9 @@ constexpr int kMaxFastClasses = 256;
 constexpr int kFastPrimeLimit = 128;   // primes of the class prime and the batch's rows: 3 .. 127
 constexpr int kStagePrimeLimit = 512;  // primes of the single-curve rows: 3 .. 509
 constexpr int kFastRowExtension = 96;  // words a staged row extends past its period
+constexpr double kDenseCurveBits = 10.0;  // below this from six small-prime rows: try large primes
 constexpr double kStageRowCost = 0.16;
-constexpr double kSurvivorWordCost = 15.0;
+constexpr double kSurvivorWordCost = 40.0;
 struct FastPlan {
     int class_prime = 1;
     std::vector<std::vector<int>> slots;   // prime factors of each stage-1 modulus

@@ -291,6 +291,24 @@ long long fast_row_budget(int max_classes) {
     return (per_cta - (long long)fast_dynamic_smem(0, max_classes)) / (8 * dev::kFSlotCount);
 }
 
+FastPlan single_curve_plan(const std::vector<std::string> &coefficients, long long bound, int *max_classes) {
+    // the two staged row sets of a CTA, its queues and its two slots' class
+    // runs must fit shared memory at 2 CTAs/SM
+    const FastPlanner planner(coefficients, bound);
+    const int classes = max_admissible_classes(coefficients, planner.class_prime());
+    if (max_classes) *max_classes = classes;
+    const long long row_budget = fast_row_budget(classes);
+    FastPlan plan;
+    for (int cap = kMaxModulus;;) {
+        plan = planner.plan(cap, kMaxFastSlots, row_budget);
+        int row_words = 0;
+        for (int m : plan.moduli) row_words += (m + dev::kFExt + 1) & ~1;
+        if (row_words <= row_budget || cap <= 64) break;
+        cap = cap * 7 / 8;
+    }
+    return plan;
+}
+
 struct Sieve::Impl {
     SieveOptions opt;
     long long bound = 0, words = 0;
@@ -504,16 +522,7 @@ struct Sieve::Impl {
         auto t0 = Clock::now();
         // the two staged row sets of a CTA, its queues and its two slots' class
         // runs must fit shared memory at 2 CTAs/SM
-        const FastPlanner planner(coefficients, bound);
-        fast_max_classes = max_admissible_classes(coefficients, planner.class_prime());
-        const long long row_budget = fast_row_budget(fast_max_classes);
-        for (int cap = kMaxModulus;;) {
-            fast_plan = planner.plan(cap, kMaxFastSlots, row_budget);
-            int row_words = 0;
-            for (int m : fast_plan.moduli) row_words += (m + dev::kFExt + 1) & ~1;
-            if (row_words <= row_budget || cap <= 64) break;
-            cap = cap * 7 / 8;
-        }
+        fast_plan = single_curve_plan(coefficients, bound, &fast_max_classes);
         const int n = int(coefficients.size()) - 1;
         const int q = fast_plan.class_prime;
         const long long M = 64LL * q;

@@ -69,6 +69,12 @@ struct SieveTimings {
     unsigned long long d2h_bytes = 0;
 };
 
+// The fast plan a single-curve sieve uses for a curve and numerator bound
+// (host only): the autotuner's choice under the fast kernel's shared-memory
+// budget; *max_classes (optional) receives the most classes of one denominator.
+struct FastPlan;
+FastPlan single_curve_plan(const std::vector<std::string> &coefficients, long long bound, int *max_classes);
+
 // The fast plan a sieve chose for its curve (empty for the reference plan).
 struct FastPlanInfo {
     int class_prime = 0;           // numerator classes are taken mod 64 * class_prime

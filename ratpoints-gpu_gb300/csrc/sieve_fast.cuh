@@ -537,14 +537,15 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
             mod8[sl] = 8u * u32(T.mod[sl].m);
             slot_base[sl] = sbase + 8 * T.mod[sl].smem_offset;
         }
+        int c = 0;  // this warp's items of a slot only increase: so do their classes
         for (;;) {
             int item = 0;
             if (lane == 0) item = atomicAdd(const_cast<int *>(&S.next), 1);
             item = __shfl_sync(kFullMask, item, 0);
             if (item >= total_items) break;
-            // class index: largest c with prefix[c] <= item (32 classes per probe)
-            int c = 0;
-            for (int base = 0; base < nclass; base += 32) {
+            // class index: largest c with prefix[c] <= item (32 classes per
+            // probe, from the last one on)
+            for (int base = c; base < nclass; base += 32) {
                 const int cc = base + lane;
                 const u32 bb = __ballot_sync(kFullMask, cc < nclass && prefix[cc] <= item);
                 if (bb) c = base + 31 - __clz(bb);

@@ -76,6 +76,12 @@ class SearchOptions(ctypes.Structure):
                 ("flags", ctypes.c_uint32)]
 
 
+class FastPlanInfo(ctypes.Structure):
+    _fields_ = [("class_prime", ctypes.c_int32), ("modulus_count", ctypes.c_int32),
+                ("moduli", ctypes.c_int32 * 16), ("factors", (ctypes.c_int32 * 4) * 16),
+                ("bits", ctypes.c_double)]
+
+
 class BatchStats(ctypes.Structure):
     _fields_ = ([(name, ctypes.c_uint64) for name in
                  ("curves", "wide_curves", "denominators", "survivors", "points", "launches",
@@ -155,6 +161,8 @@ def load():
     lib.rpg_square_root.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
                                     ctypes.c_char_p, ctypes.c_size_t,
                                     ctypes.POINTER(ctypes.c_int32)]
+    lib.rpg_fast_plan.restype = S
+    lib.rpg_fast_plan.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.POINTER(FastPlanInfo)]
     lib.rpg_preverify.restype = S
     lib.rpg_preverify.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
                                   ctypes.POINTER(ctypes.c_int32)]
@@ -377,6 +385,17 @@ def is_squarefree(coefficients):
     out = ctypes.c_int32(-1)
     _check(load().rpg_is_squarefree(_strings(coeffs), len(coeffs), ctypes.byref(out)))
     return bool(out.value)
+
+
+def fast_plan(coefficients, bound):
+    """The single-curve fast plan for a curve and numerator bound (host only):
+    {"class_prime", "moduli", "factors", "bits"}."""
+    coeffs = coefficients_of(coefficients)
+    info = FastPlanInfo()
+    _check(load().rpg_fast_plan(_strings(coeffs), len(coeffs), int(bound), ctypes.byref(info)))
+    n = info.modulus_count
+    return {"class_prime": info.class_prime, "moduli": list(info.moduli[:n]),
+            "factors": [[f for f in info.factors[i] if f] for i in range(n)], "bits": info.bits}
 
 
 def preverify(coefficients, a, b):

@@ -217,3 +217,37 @@ def test_interval_narrowing_matches_single_search(rpg, golden):
     # one-point intervals sweep a few numerators per denominator: what survives
     # there is the points themselves and their unreduced multiples
     assert survivors[0] < full_survivors[0] and survivors[1] < full_survivors[1]
+
+
+def test_huge_rows_searched_alone(rpg, golden):
+    # numerator bounds above 2^17 words of 64 numerators go to the single-curve
+    # kernel beside the batched ones; answers stay those of a single search
+    rng = random.Random(21)
+    curves = [{"coefficients": ["1", "-1", "0", "1"], "bound": 10 ** 7, "first": 1, "last": 300},
+              {"coefficients": golden["record_curve"]["coefficients"].split(), "bound": 5 * 10 ** 6,
+               "first": 2, "last": 120, "intervals": [(None, "-0.3333"), ("0.5", "7")]},
+              {"coefficients": ["-2", "0", "1", "0", "1"], "bound": 9 * 10 ** 6, "first": 1, "last": 40,
+               "square": True, "include_infinity": False}]
+    curves += squarefree(rpg, mixed_curves(rng, 12, (100, 100000), (10, 400)))
+    points, status, survivors, stats = rpg.batch_search(curves)
+    assert all(s == 0 for s in status)
+    assert stats["curves"] == len(curves)
+    for c, got, n in zip(curves, points, survivors):
+        expected, st = rpg.point_search(c["coefficients"], c["bound"], c["first"], c["last"],
+                                        intervals=c.get("intervals", ()),
+                                        include_infinity=c.get("include_infinity", True),
+                                        square=c.get("square", False))
+        assert got == expected, c["bound"]
+    assert points[0] and points[1]
+
+
+def test_survivor_counts_repeat(rpg):
+    # work is handed out dynamically, so warps see the denominators in a
+    # different order each run; survivors per curve must not depend on it
+    rng = random.Random(77)
+    curves = squarefree(rpg, mixed_curves(rng, 48, (50, 300000), (5, 2000), bits=24))
+    first = rpg.batch_search(curves, preverify=False)
+    for _ in range(2):
+        again = rpg.batch_search(curves, preverify=False)
+        assert again[2] == first[2]
+        assert again[0] == first[0]

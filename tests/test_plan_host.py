@@ -1,0 +1,74 @@
+"""The fast plan's autotuner on the host (rpg_fast_plan, no GPU): the plan
+chosen for the C2 curve, rows of large primes for the dense record curve,
+well-formed moduli, and no filter that a known point fails."""
+
+from fractions import Fraction
+
+import pytest
+
+RECORD = "247747600 -985905640 567207969 2396040466 52485681 -470135160 82342800"
+
+
+def is_prime(n):
+    return n > 1 and all(n % f for f in range(2, int(n ** 0.5) + 1))
+
+
+def well_formed(plan):
+    assert 1 <= len(plan["moduli"]) <= 12
+    seen = set()
+    for m, factors in zip(plan["moduli"], plan["factors"]):
+        assert m <= 1500 and factors
+        product = 1
+        for q in factors:
+            assert is_prime(q) and q % 2 == 1 and q < 512
+            assert q not in seen and q != plan["class_prime"]
+            seen.add(q)
+            product *= q
+        assert product == m
+    assert plan["class_prime"] in (1, 3, 5, 7, 11, 13)
+
+
+def test_c2_plan(rpg):
+    import bench
+    plan = rpg.fast_plan(bench.c2_curve(), 5_000_000)
+    well_formed(plan)
+    # six rows of small-prime products, class prime 5 (f mod 3 is always a square)
+    assert plan["class_prime"] == 5
+    assert len(plan["moduli"]) == 6 and plan["bits"] > 13
+    assert all(q < 128 for f in plan["factors"] for q in f)
+    assert 61 in [q for f in plan["factors"] for q in f]
+
+
+def test_dense_curve_gets_large_prime_rows(rpg):
+    plan = rpg.fast_plan(RECORD, 10 ** 7)
+    well_formed(plan)
+    assert plan["class_prime"] == 1
+    assert len(plan["moduli"]) >= 10 and plan["bits"] > 10
+    assert all(len(f) == 1 and f[0] > 128 for f in plan["factors"])
+
+
+def test_known_points_pass_every_row(rpg, golden):
+    # the record curve's published points survive each stage-1 prime of its plan
+    plan = rpg.fast_plan(RECORD, 10 ** 6)
+    coeffs = [int(c) for c in RECORD.split()]
+    primes = [q for f in plan["factors"] for q in f]
+    n = len(coeffs) - 1
+    for text in golden["record_curve"]["x"][:120]:
+        x = Fraction(text)
+        a, b = x.numerator, x.denominator
+        F = sum(c * a ** i * b ** (n - i) for i, c in enumerate(coeffs))
+        for q in primes:
+            assert pow(F % q, (q - 1) // 2, q) in (0, 1), (text, q)
+
+
+@pytest.mark.parametrize("height", [10, 10 ** 3, 10 ** 9])
+def test_small_and_large_heights(rpg, height):
+    for coeffs in ("1 0 1", "1 -1 0 1", "-3 5 -7 11 2", RECORD):
+        well_formed(rpg.fast_plan(coeffs, height))
+
+
+def test_argument_errors(rpg):
+    with pytest.raises(rpg.RpgError):
+        rpg.fast_plan("1 0 1", 0)
+    with pytest.raises(rpg.RpgError):
+        rpg.fast_plan("x 1", 10)
