@@ -49,9 +49,10 @@ SMEM_BYTES_PER_CLK = 128      # lane-contiguous LDS.64, measured per SM on GB300
 # fast-plan launch of this workload, from an ncu capture of the kernel:
 #   ncu --set full --clock-control none -k regex:fast_sieve -s 1 -c 1 python bench.py
 #       --steps 1 --warmup 1 --no-cpu-baseline --reference-plan-steps 0
-#       --reference-gpu-denominators 0 --restricted 0 --serving-requests 0 --batch-curves 0
-#       --denominators 131072
-FAST_LAUNCH_DRAM_BYTES = 46_370_560 + 36_864
+#       --reference-gpu-denominators 0 --restricted 0 --serving-requests 0 --dense-height 0
+#       --batch-curves 0 --denominators 131072
+# (cold L2 in every ncu pass: most of the 97 MB of class tables is read once per launch)
+FAST_LAUNCH_DRAM_BYTES = 89_960_192 + 3_470_080
 
 
 def measured_hbm_gbs():
