@@ -602,7 +602,10 @@ def main():
         "e2e": {"value": reduced * world / e2e_s / 1e9, "unit": UNIT,
                 "seconds": e2e_s, "points": len(points),
                 "h2d_bytes_per_step": int(e2e_stats.get("h2d_bytes", 0)) if e2e_stats else 0,
-                "d2h_bytes_per_step": int(e2e_stats.get("d2h_bytes", 0)) if e2e_stats else 0},
+                "d2h_bytes_per_step": int(e2e_stats.get("d2h_bytes", 0)) if e2e_stats else 0,
+                "breakdown_ms": {k: round(float(e2e_stats.get(k, 0)), 3) for k in
+                                 ("plan_ms", "workspace_ms", "basis_wall_ms", "basis_ms", "sieve_ms",
+                                  "sieve_wall_ms", "verification_ms")} if e2e_stats else None},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clock,
     }
