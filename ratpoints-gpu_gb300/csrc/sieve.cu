@@ -540,8 +540,13 @@ struct Sieve::Impl {
             base[p] = int(affine.size());
             auto aff = affine_mask(p, coefficients);
             affine.insert(affine.end(), aff.begin(), aff.end());
-            inverse.push_back(0);
-            for (int v = 1; v < p; ++v) inverse.push_back((unsigned short)mod_inverse(v, p));
+            // v^-1 = -(p / v) (p mod v)^-1 (mod p), from p = (p / v) v + p mod v
+            const std::size_t at = inverse.size();
+            inverse.resize(at + std::size_t(p), 0);
+            if (p > 1) inverse[at + 1] = 1;
+            for (int v = 2; v < p; ++v)
+                inverse[at + std::size_t(v)] = (unsigned short)(
+                    (p - (long long)(p / v) * inverse[at + std::size_t(p % v)] % p) % p);
             if (n % 2 == 0) {
                 const int lc = decimal_mod(coefficients.back(), p);
                 bool square = false;
@@ -552,6 +557,31 @@ struct Sieve::Impl {
         std::vector<dev::TableSpec> specs;
         long long total = 0;
         int smem_words = 0;
+        // pattern rows per (prime, rho = 0 rule): step = M mod q, window start
+        // of residue x0 = x0 step^-1 mod q
+        std::vector<dev::ClassPatternSpec> pspecs;
+        long long pattern_total = 0;
+        auto pattern_of = [&](int p, int lead_ok, dev::TableSpec &Sp, int f) {
+            int found = -1;
+            for (std::size_t i = 0; i < pspecs.size(); ++i)
+                if (pspecs[i].q == p && pspecs[i].lead_ok == lead_ok) found = int(i);
+            if (found < 0) {
+                dev::ClassPatternSpec P{};
+                P.out = pattern_total;
+                P.q = p;
+                P.words = (p + 64 + 63) / 64 + 1;
+                P.factor_base = base[p];
+                P.lead_ok = lead_ok;
+                P.step = int(M % p);
+                pattern_total += (long long)p * P.words;
+                pspecs.push_back(P);
+                found = int(pspecs.size()) - 1;
+            }
+            Sp.pattern[f] = pspecs[std::size_t(found)].out;
+            Sp.pattern_words[f] = pspecs[std::size_t(found)].words;
+            Sp.s_mod[f] = int(S % p);
+            Sp.step_inv[f] = int(mod_inverse(M % p, p));
+        };
         F = dev::FastTables{};
         F.slots = int(fast_plan.moduli.size());
         for (int sl = 0; sl < F.slots; ++sl) {
@@ -560,8 +590,7 @@ struct Sieve::Impl {
             Sp.m = fast_plan.moduli[sl];
             for (int i = 0; i < Sp.nf; ++i) {
                 Sp.q[i] = fast_plan.slots[sl][i];
-                Sp.factor_base[i] = base[Sp.q[i]];
-                Sp.lead_ok[i] = lead[Sp.q[i]];
+                pattern_of(Sp.q[i], lead[Sp.q[i]], Sp, i);
             }
             Sp.length = (Sp.m + dev::kFExt + 1) & ~1;
             Sp.offset = total;
@@ -589,8 +618,7 @@ struct Sieve::Impl {
             Sp.nf = 1;
             Sp.m = p;
             Sp.q[0] = p;
-            Sp.factor_base[0] = base[p];
-            Sp.lead_ok[0] = 0;
+            pattern_of(p, 0, Sp, 0);  // rows with p | d are never read: stage 2 skips such p
             Sp.length = p;
             Sp.offset = total;
             total += (long long)p * p;
@@ -726,6 +754,8 @@ struct Sieve::Impl {
         unsigned char *d_aff = device_alloc<unsigned char>(affine.size(), "cudaMalloc(affine)");
         unsigned short *d_inv = device_alloc<unsigned short>(inverse.size(), "cudaMalloc(inverse)");
         dev::TableSpec *d_specs = device_alloc<dev::TableSpec>(specs.size(), "cudaMalloc(specs)");
+        dev::ClassPatternSpec *d_pspecs = device_alloc<dev::ClassPatternSpec>(pspecs.size(), "cudaMalloc(specs)");
+        dev::u64 *d_patterns = device_alloc<dev::u64>(std::size_t(pattern_total), "cudaMalloc(patterns)");
         timings.workspace_ms += ms_since(t1);
         cudaEvent_t e0, e1;
         check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
@@ -739,6 +769,9 @@ struct Sieve::Impl {
         check_cuda(cudaMemcpyAsync(d_specs, specs.data(), specs.size() * sizeof(dev::TableSpec),
                                    cudaMemcpyHostToDevice, stream),
                    "upload table specs");
+        check_cuda(cudaMemcpyAsync(d_pspecs, pspecs.data(), pspecs.size() * sizeof(dev::ClassPatternSpec),
+                                   cudaMemcpyHostToDevice, stream),
+                   "upload pattern specs");
         check_cuda(cudaMemcpyAsync(fast_adm, adm.data(), adm.size() * sizeof(dev::u64),
                                    cudaMemcpyHostToDevice, stream),
                    "upload admissible classes");
@@ -746,12 +779,15 @@ struct Sieve::Impl {
                                    cudaMemcpyHostToDevice, stream),
                    "upload class starts");
         timings.h2d_bytes += affine.size() + inverse.size() * sizeof(unsigned short) +
-                             specs.size() * sizeof(dev::TableSpec) + adm.size() * sizeof(dev::u64) +
-                             starts.size() * sizeof(dev::FastClassStart);
+                             specs.size() * sizeof(dev::TableSpec) + pspecs.size() * sizeof(dev::ClassPatternSpec) +
+                             adm.size() * sizeof(dev::u64) + starts.size() * sizeof(dev::FastClassStart);
         const int threads = 256;
+        dev::pattern_rows_kernel<<<unsigned((pattern_total + threads - 1) / threads), threads, 0, stream>>>(
+            d_patterns, d_pspecs, int(pspecs.size()), d_aff, d_inv, pattern_total);
+        check_cuda(cudaGetLastError(), "pattern_rows_kernel launch");
         const long long blocks = (total + threads - 1) / threads;
-        dev::class_table_kernel<<<unsigned(blocks), threads, 0, stream>>>(
-            fast_rows, d_specs, int(specs.size()), d_aff, d_inv, S, int(M), total);
+        dev::class_table_kernel<<<unsigned(blocks), threads, 0, stream>>>(fast_rows, d_specs, int(specs.size()),
+                                                                          d_patterns, total);
         check_cuda(cudaGetLastError(), "class_table_kernel launch");
         check_cuda(cudaEventRecord(e1, stream), "cudaEventRecord");
         check_cuda(cudaEventSynchronize(e1), "class table build");
@@ -763,6 +799,8 @@ struct Sieve::Impl {
         cudaFree(d_aff);
         cudaFree(d_inv);
         cudaFree(d_specs);
+        cudaFree(d_pspecs);
+        cudaFree(d_patterns);
         F.rows = fast_rows;
         F.prime_rows = fast_rows;
         F.admissible = fast_adm;

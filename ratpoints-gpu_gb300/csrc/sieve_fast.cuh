@@ -127,45 +127,86 @@ __device__ __forceinline__ bool prime_bit(const unsigned char *affine, const uns
     return affine[(x * inverse[rho]) % q] != 0;
 }
 
+// Bit patterns of one prime q used by the class-layout tables: for each
+// rho in [0, q), bit k of row rho is prime_bit(.., rho, (k step) mod q) for
+// k in [0, q + 64), step = M mod q (k taken mod q), `words` words per row.
+// Bit j of a table word whose first site has residue x0 is then bit
+// (x0 step^-1 mod q) + j of the row: one 64-bit window instead of 64 tests.
+struct ClassPatternSpec {
+    long long out;                 // word offset of row 0
+    int q;
+    int words;                     // words per row: ceil((q + 64) / 64) + 1
+    int factor_base;               // offset of q's affine/inverse arrays
+    int lead_ok;
+    int step;                      // M mod q
+    int pad;
+};
+
+__global__ void pattern_rows_kernel(u64 *patterns, const ClassPatternSpec *specs, int nspecs,
+                                    const unsigned char *affine, const unsigned short *inverse,
+                                    long long total) {
+    const long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (id >= total) return;
+    int lo = 0, hi = nspecs - 1;  // last spec with out <= id
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (specs[mid].out <= id) lo = mid;
+        else hi = mid - 1;
+    }
+    const ClassPatternSpec &P = specs[lo];
+    const long long rel = id - P.out;
+    const int rho = int(rel / P.words);
+    const int wi = int(rel % P.words);
+    const unsigned char *aff = affine + P.factor_base;
+    const unsigned short *inv = inverse + P.factor_base;
+    u64 word = 0;
+    int k = (64 * wi) % P.q;
+    for (int j = 0; j < 64; ++j) {
+        const int x = int((long long)k * P.step % P.q);
+        if (prime_bit(aff, inv, P.q, rho, P.lead_ok, x)) word |= u64(1) << j;
+        if (++k == P.q) k = 0;
+    }
+    patterns[id] = word;
+}
+
 // Description of one class-layout table: m rows of `length` words, bit j of
 // word u of row rho = AND over the prime factors q of
-// prime_bit(.., rho mod q, (S u + M j) mod q).
+// prime_bit(.., rho mod q, (S u + M j) mod q), read from q's pattern rows.
 struct TableSpec {
     long long offset;
     int m;
     int nf;
     int q[kFastMaxFactors];
     int length;
-    int factor_base[kFastMaxFactors];   // offset of q's affine/inverse arrays
-    int lead_ok[kFastMaxFactors];
+    long long pattern[kFastMaxFactors];  // word offset of q's pattern row 0
+    int pattern_words[kFastMaxFactors];
+    int s_mod[kFastMaxFactors];          // S mod q
+    int step_inv[kFastMaxFactors];       // (M mod q)^-1 mod q
 };
 
-__global__ void class_table_kernel(u64 *rows, const TableSpec *specs, int nspecs,
-                                   const unsigned char *affine, const unsigned short *inverse,
-                                   long long stride, int class_mod, long long total) {
+__global__ void class_table_kernel(u64 *rows, const TableSpec *specs, int nspecs, const u64 *patterns,
+                                   long long total) {
     const long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (id >= total) return;
-    int t = 0;
-    while (t + 1 < nspecs && specs[t + 1].offset <= id) ++t;
-    const TableSpec &S = specs[t];
+    int lo = 0, hi = nspecs - 1;  // last spec with offset <= id
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (specs[mid].offset <= id) lo = mid;
+        else hi = mid - 1;
+    }
+    const TableSpec &S = specs[lo];
     const long long rel = id - S.offset;
     const int rho = int(rel / S.length);
     const int u = int(rel % S.length) % S.m;
     u64 word = ~u64(0);
     for (int f = 0; f < S.nf; ++f) {
         const int q = S.q[f];
-        const unsigned char *aff = affine + S.factor_base[f];
-        const unsigned short *inv = inverse + S.factor_base[f];
-        const int rq = rho % q;
-        int x = int((stride % q) * u % q);
-        const int step = class_mod % q;
-        u64 bits = 0;
-        for (int j = 0; j < 64; ++j) {
-            if (prime_bit(aff, inv, q, rq, S.lead_ok[f], x)) bits |= u64(1) << j;
-            x += step;
-            if (x >= q) x -= q;
-        }
-        word &= bits;
+        const int x0 = int((long long)S.s_mod[f] * u % q);
+        const int k0 = int((long long)x0 * S.step_inv[f] % q);
+        const u64 *row = patterns + S.pattern[f] + (long long)(rho % q) * S.pattern_words[f];
+        const int w = k0 >> 6, sh = k0 & 63;
+        const u64 lo_word = __ldg(row + w), hi_word = __ldg(row + w + 1);
+        word &= sh ? (lo_word >> sh) | (hi_word << (64 - sh)) : lo_word;
     }
     rows[id] = word;
 }
@@ -528,7 +569,11 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
         const FastRun *runs = S.runs;
         const int *prefix = S.prefix;
         const int nclass = S.nclass;
-        const int total_items = prefix[nclass];
+        // up to 31 classes: lane c keeps prefix[c] (lane nclass the total), so
+        // finding an item's class takes no memory access
+        const bool lane_prefix = nclass < kWarpSize;
+        const int my_prefix = lane_prefix && lane <= nclass ? prefix[lane] : 0;
+        const int total_items = lane_prefix ? __shfl_sync(kFullMask, my_prefix, nclass) : prefix[nclass];
         u32 step8[NS], mod8[NS];
         const unsigned char *slot_base[NS];
 #pragma unroll
@@ -545,13 +590,21 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
             if (item >= total_items) break;
             // class index: largest c with prefix[c] <= item (32 classes per
             // probe, from the last one on)
-            for (int base = c; base < nclass; base += 32) {
-                const int cc = base + lane;
-                const u32 bb = __ballot_sync(kFullMask, cc < nclass && prefix[cc] <= item);
-                if (bb) c = base + 31 - __clz(bb);
-                if (bb != kFullMask) break;
+            int first_item;
+            if (lane_prefix) {
+                const u32 bb = __ballot_sync(kFullMask, lane < nclass && my_prefix <= item);
+                c = 31 - __clz(bb);
+                first_item = __shfl_sync(kFullMask, my_prefix, c);
+            } else {
+                for (int base = c; base < nclass; base += 32) {
+                    const int cc = base + lane;
+                    const u32 bb = __ballot_sync(kFullMask, cc < nclass && prefix[cc] <= item);
+                    if (bb) c = base + 31 - __clz(bb);
+                    if (bb != kFullMask) break;
+                }
+                first_item = prefix[c];
             }
-            const int w0 = (item - prefix[c]) * kFItemWords;
+            const int w0 = (item - first_item) * kFItemWords;
             const FastRun run = runs[c];
             const int wt = int(run.words_last & 0xFFFFFFu);
             const int last_word = (run.words_last >> 24) & 1u ? wt - 1 : -1;
@@ -561,9 +614,12 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
             const u64 pos0 = u64(run.ofs) + u64(T.stride) * u64(A.w_lo);
             u32 o[NS];  // byte offset of this lane's word inside each staged row
 #pragma unroll
-            for (int sl = 0; sl < NS; ++sl)
-                o[sl] = 8u * mod_u32(u32(run.start[sl]) + u32(w0 + lane), u32(T.mod[sl].m),
-                                     T.mod[sl].magic);
+            for (int sl = 0; sl < NS; ++sl) {
+                const u32 m = u32(T.mod[sl].m);
+                const u32 v = u32(run.start[sl]) + u32(w0 + lane);
+                // a class's first item: start < m and lane < 32 <= m, one subtraction
+                o[sl] = 8u * (w0 == 0 && m >= 32 ? (v >= m ? v - m : v) : mod_u32(v, m, T.mod[sl].magic));
+            }
 #pragma unroll 1
             for (int step = 0; step < kFSteps; ++step) {
                 const int ws = w0 + step * kWarpSize * kFK;
