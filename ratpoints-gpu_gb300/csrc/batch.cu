@@ -951,6 +951,7 @@ __global__ void __launch_bounds__(kNThreads, 3)
     __shared__ int s_abort;
     __shared__ int s_ci[kNWarps][kSelectedPrimes];
     __shared__ u32 s_dinv[kNWarps][kSelectedPrimes];
+    __shared__ unsigned char s_lane_at[kNarrowSlots][kWarpSize];  // (shift + kNK lane) mod m
     __shared__ __align__(8) unsigned long long s_bar;
 
     const int lane = threadIdx.x & 31;
@@ -985,6 +986,11 @@ __global__ void __launch_bounds__(kNThreads, 3)
             for (int i = threadIdx.x; i < int(sizeof(NarrowCurve) / 4); i += kNThreads) dst[i] = src[i];
             cur = item.curve;
             __syncthreads();
+            // each lane's first table word per modulus for rows swept from word 0
+            for (int t = threadIdx.x; t < kNarrowSlots * kWarpSize; t += kNThreads) {
+                const int s = t / kWarpSize, l = t % kWarpSize;
+                s_lane_at[s][l] = (unsigned char)((C.shift[s] + u32(kNK * l)) % u32(C.m[s]));
+            }
             if (threadIdx.x == 0) {
                 fence_proxy_async_shared();
                 mbar_arrive_expect_tx(bar, u32(C.table_words + kAffWords) * 8u);
@@ -1046,7 +1052,8 @@ __global__ void __launch_bounds__(kNThreads, 3)
                     mods[s] = m;
                     steps[s] = C.step[s];
                     base[s] = u32(C.off[s]) + rho[s] * u32(C.len[s]);
-                    at[s] = mod_u32(C.shift[s] + u32(w_lo + kNK * lane), m, C.magic[s]);
+                    at[s] = w_lo == 0 ? u32(s_lane_at[s][lane])
+                                      : mod_u32(C.shift[s] + u32(w_lo + kNK * lane), m, C.magic[s]);
                 }
                 bool selected = false;
                 int qn = 0;
@@ -1499,6 +1506,7 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
         return (long double)P.work[a].words * P.work[a].count >
                (long double)P.work[b].words * P.work[b].count;
     });
+    std::vector<std::pair<std::size_t, std::size_t>> list_curves;  // (descriptor, curve) with class lists
     for (std::size_t i : order) {
         const BatchCurveSpec &c = curves[i];
         CurveWork &cw = P.work[i];
@@ -1624,8 +1632,7 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             device_intervals(c.intervals, C.nint, C.lo, C.hi);
             C.list_max = std::max(1, cw.classes);
             if (C.nint == 0) {
-                // class lists by denominator class k = (d mod 64) q + (d mod q),
-                // in the order the producer lays out classes for interval curves
+                // room for the curve's class lists (64 q denominator classes)
                 const int lm = C.list_max;
                 const std::size_t ncombo = std::size_t(64) * std::size_t(q);
                 C.list_count = (long long)P.list_count.size();
@@ -1634,38 +1641,7 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 P.list_count.resize(P.list_count.size() + ncombo, 0);
                 P.list_runs.resize(P.list_runs.size() + ncombo * std::size_t(lm));
                 P.list_prefix.resize(P.list_prefix.size() + ncombo * std::size_t(lm + 1), 0);
-                for (int dd = 0; dd < 64; ++dd)
-                    for (int dq = 0; dq < q; ++dq) {
-                        const std::size_t k = std::size_t(dd) * std::size_t(q) + std::size_t(dq);
-                        const dev::u64 classes2 = cw.adm2[dd];
-                        const dev::u64 classesq = q > 1 ? C.admissible[64 + dq] : dev::u64(1);
-                        const int nq = __builtin_popcountll(classesq);
-                        const int nclass = __builtin_popcountll(classes2) * nq;
-                        if (nclass > lm) throw std::logic_error("class list longer than its stride");
-                        dev::WideRun *runs = P.list_runs.data() + C.list_runs + k * std::size_t(lm);
-                        int *prefix = P.list_prefix.data() + C.list_prefix + k * std::size_t(lm + 1);
-                        int items = 0;
-                        for (int cidx = 0; cidx < nclass; ++cidx) {
-                            const int r64 = nth_bit_host(classes2, cidx / nq);
-                            int r = r64;
-                            if (q > 1)
-                                r = r64 + 64 * int(C.crt[C.mod_q[r64] * 13 + nth_bit_host(classesq, cidx % nq)]);
-                            const dev::ClassStart &cs = P.class_starts[std::size_t(C.cls + r)];
-                            const long long count = C.count_q + (cs.ofs <= C.count_r ? 1 : 0);
-                            const long long words = (count + 63) >> 6;
-                            dev::WideRun &run = runs[cidx];
-                            run.wbase = 0;
-                            run.words = int(words);
-                            run.ofs = cs.ofs;
-                            run.first = 0;
-                            run.last = (unsigned char)(words > 0 ? count - 64 * (words - 1) : 64);
-                            for (int sl = 0; sl < dev::kWideSlots; ++sl) run.start[sl] = cs.start[sl];
-                            prefix[cidx] = items;
-                            items += int((words + dev::kWItemWords - 1) / dev::kWItemWords);
-                        }
-                        prefix[nclass] = items;
-                        P.list_count[C.list_count + k] = nclass;
-                    }
+                list_curves.push_back({P.wide.size(), i});  // filled below, in parallel
                 // classes of at most 128 words are swept kWK at a time
                 const long long max_words = (C.count_q + 1 + 63) >> 6;
                 C.list_steps = max_words <= 4 * dev::kWarpSize ? int((max_words + dev::kWarpSize - 1) / dev::kWarpSize) : 0;
@@ -1778,6 +1754,45 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
         }
         stats.curves += 1;
     }
+    // class lists by denominator class k = (d mod 64) q + (d mod q), in the
+    // order the producer lays out classes for interval curves
+    parallel_for(list_curves.size(), [&](std::size_t j) {
+        const dev::WideCurve &C = P.wide[list_curves[j].first];
+        const CurveWork &cw = P.work[list_curves[j].second];
+        const int q = C.class_prime;
+        const int lm = C.list_max;
+        for (int dd = 0; dd < 64; ++dd)
+            for (int dq = 0; dq < q; ++dq) {
+                const std::size_t k = std::size_t(dd) * std::size_t(q) + std::size_t(dq);
+                const dev::u64 classes2 = cw.adm2[dd];
+                const dev::u64 classesq = q > 1 ? C.admissible[64 + dq] : dev::u64(1);
+                const int nq = __builtin_popcountll(classesq);
+                const int nclass = __builtin_popcountll(classes2) * nq;
+                if (nclass > lm) throw std::logic_error("class list longer than its stride");
+                dev::WideRun *runs = P.list_runs.data() + C.list_runs + k * std::size_t(lm);
+                int *prefix = P.list_prefix.data() + C.list_prefix + k * std::size_t(lm + 1);
+                int items = 0;
+                for (int cidx = 0; cidx < nclass; ++cidx) {
+                    const int r64 = nth_bit_host(classes2, cidx / nq);
+                    int r = r64;
+                    if (q > 1) r = r64 + 64 * int(C.crt[C.mod_q[r64] * 13 + nth_bit_host(classesq, cidx % nq)]);
+                    const dev::ClassStart &cs = P.class_starts[std::size_t(C.cls + r)];
+                    const long long count = C.count_q + (cs.ofs <= C.count_r ? 1 : 0);
+                    const long long words = (count + 63) >> 6;
+                    dev::WideRun &run = runs[cidx];
+                    run.wbase = 0;
+                    run.words = int(words);
+                    run.ofs = cs.ofs;
+                    run.first = 0;
+                    run.last = (unsigned char)(words > 0 ? count - 64 * (words - 1) : 64);
+                    for (int sl = 0; sl < dev::kWideSlots; ++sl) run.start[sl] = cs.start[sl];
+                    prefix[cidx] = items;
+                    items += int((words + dev::kWItemWords - 1) / dev::kWItemWords);
+                }
+                prefix[nclass] = items;
+                P.list_count[std::size_t(C.list_count) + k] = nclass;
+            }
+    });
     stats.wide_items = P.wide_items.size();
     stats.narrow_items = P.narrow_items.size();
     stats.table_words = (unsigned long long)P.row_words;

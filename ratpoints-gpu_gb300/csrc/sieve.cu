@@ -343,6 +343,7 @@ struct Sieve::Impl {
         // [0] survivors, [1] work counter, [2] error word, [3] pre-verified survivors
         unsigned long long *count = nullptr;
         cudaEvent_t begin = nullptr, end = nullptr;
+        cudaEvent_t copied = nullptr;  // the counter words are in pinned host memory
         long long first = 0, last = 0;
         bool busy = false;
     };
@@ -374,6 +375,7 @@ struct Sieve::Impl {
             cudaFree(b.count);
             if (b.begin) cudaEventDestroy(b.begin);
             if (b.end) cudaEventDestroy(b.end);
+            if (b.copied) cudaEventDestroy(b.copied);
             b = Buffer{};
         }
         cudaFree(rows);
@@ -501,6 +503,7 @@ struct Sieve::Impl {
             b.count = device_alloc<unsigned long long>(4, "cudaMalloc(count)");
             check_cuda(cudaEventCreate(&b.begin), "cudaEventCreate");
             check_cuda(cudaEventCreate(&b.end), "cudaEventCreate");
+            check_cuda(cudaEventCreateWithFlags(&b.copied, cudaEventDisableTiming), "cudaEventCreate");
         }
         check_cuda(cudaMallocHost(&h_count, 8 * sizeof(unsigned long long)), "cudaMallocHost");
         check_cuda(cudaMallocHost(&h_a, std::size_t(initial) * sizeof(long long)), "cudaMallocHost");
@@ -922,6 +925,7 @@ struct Sieve::Impl {
         check_cuda(cudaMemcpyAsync(h_count + 4 * which, b.count, 4 * sizeof(unsigned long long),
                                    cudaMemcpyDeviceToHost, stream),
                    "download survivor count");
+        check_cuda(cudaEventRecord(b.copied, stream), "cudaEventRecord");
         timings.d2h_bytes += 4 * sizeof(unsigned long long);
         ++timings.launches;
     }
@@ -1053,7 +1057,8 @@ struct Sieve::Impl {
             launch(which, p.first, p.last, p.w_lo, p.w_hi);
             check_cuda(cudaStreamSynchronize(stream), "sieve kernel");
             buf[which].busy = false;
-            check_error_word(which);
+            // the counter words came back with the launch: [2] is its error word
+            if (h_count[4 * which + 2]) throw DeviceTimeout("sieve kernel: bounded wait for a row copy timed out");
             const unsigned long long n = h_count[4 * which], kept = h_count[4 * which + 3];
             const float ms = elapsed(buf[which]);
             timings.sieve_ms += ms;
@@ -1084,16 +1089,12 @@ struct Sieve::Impl {
         const int which = order.front();
         order.pop_front();
         Buffer &b = buf[which];
-        // The count download is queued right after the kernel on the compute stream.
-        check_cuda(cudaEventSynchronize(b.end), "sieve kernel");
-        check_cuda(cudaStreamWaitEvent(copy_stream, b.end, 0), "cudaStreamWaitEvent");
-        unsigned long long counts[4] = {};
-        check_cuda(cudaMemcpyAsync(counts, b.count, sizeof counts, cudaMemcpyDeviceToHost, copy_stream),
-                   "download survivor count");
-        check_cuda(cudaStreamSynchronize(copy_stream), "download survivor count");
-        timings.d2h_bytes += sizeof counts;
+        // The counter words were copied to pinned memory right after the launch.
+        check_cuda(cudaEventSynchronize(b.copied), "sieve kernel");
+        unsigned long long counts[4];
+        for (int i = 0; i < 4; ++i) counts[i] = h_count[4 * which + i];
+        if (counts[2]) throw DeviceTimeout("sieve kernel: bounded wait for a row copy timed out");
         const unsigned long long n = counts[0];
-        check_error_word(which);
         const float ms = elapsed(b);
         timings.sieve_ms += ms;
         if (n > (unsigned long long)b.cap) {
