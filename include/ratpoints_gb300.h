@@ -154,6 +154,7 @@ typedef struct rpg_fast_plan_info {
     int32_t moduli[16];
     int32_t factors[16][4];
     double bits;
+    int32_t slots;             /* denominators staged per CTA by the single-curve kernel (2 or 3) */
 } rpg_fast_plan_info;
 rpg_status rpg_fast_plan(const char *const *coefficients, int32_t coefficient_count, int64_t numerator_bound,
                          rpg_fast_plan_info *plan);

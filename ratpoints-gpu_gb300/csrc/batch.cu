@@ -26,6 +26,7 @@ constexpr int kWK = 4;                             // words per lane per step (l
 constexpr int kWWarps = 12;                        // warp 0 produces, the others sweep
 constexpr int kWThreads = kWWarps * kWarpSize;
 constexpr int kWConsumers = kWWarps - 1;
+constexpr int kWSlotCount = 2;                     // denominators in flight per CTA
 constexpr int kWSteps = 4;
 constexpr int kWItemWords = kWarpSize * kWK * kWSteps;  // class words per sweep item
 constexpr int kWExt = kWarpSize * (kWK - 1);            // row extension
@@ -539,19 +540,19 @@ __global__ void __launch_bounds__(kWThreads, 2)
                 const unsigned short *__restrict__ inv_table, Candidates cand, BatchOut out,
                 int row_stride, int max_classes, unsigned long long *work) {
     extern __shared__ __align__(16) u64 smem[];
-    u64 *qmask = smem + 2 * row_stride;
+    u64 *qmask = smem + kWSlotCount * row_stride;
     u64 *qpos = qmask + kWConsumers * kQueue;
-    WideRun *runs0 = reinterpret_cast<WideRun *>(qpos + kWConsumers * kQueue);  // [2][max_classes]
-    int *prefix0 = reinterpret_cast<int *>(runs0 + 2 * max_classes);            // [2][max_classes + 1]
-    __shared__ WideSlot slot[2];
+    WideRun *runs0 = reinterpret_cast<WideRun *>(qpos + kWConsumers * kQueue);  // [slots][max_classes]
+    int *prefix0 = reinterpret_cast<int *>(runs0 + kWSlotCount * max_classes);  // [slots][max_classes + 1]
+    __shared__ WideSlot slot[kWSlotCount];
     __shared__ WideCtx s_ctx[kWConsumers][kWCtx];
-    __shared__ __align__(8) unsigned long long s_full[2];
-    __shared__ __align__(8) unsigned long long s_empty[2];
+    __shared__ __align__(8) unsigned long long s_full[kWSlotCount];
+    __shared__ __align__(8) unsigned long long s_empty[kWSlotCount];
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < kWSlotCount; ++b) {
             mbar_init(smem_addr(&s_full[b]), 1);
             mbar_init(smem_addr(&s_empty[b]), kWConsumers);
         }
@@ -565,7 +566,8 @@ __global__ void __launch_bounds__(kWThreads, 2)
 
     if (warp == 0) {
         // ---- producer ----
-        int b = 0, uses0 = 0, uses1 = 0;
+        int b = 0;
+        int uses[kWSlotCount] = {};  // fills of each slot so far
         bool failed = false;
         BatchItem item{};
         int i = 0, count = 0;
@@ -610,7 +612,9 @@ __global__ void __launch_bounds__(kWThreads, 2)
                 break;
             }
             // slot b must be released by every consumer before it is refilled
-            const int used = b ? uses1 : uses0;
+            int used = 0;
+#pragma unroll
+            for (int t = 0; t < kWSlotCount; ++t) used = t == b ? uses[t] : used;
             if (used > 0 && !mbar_wait(smem_addr(&s_empty[b]), u32(used - 1) & 1u)) {
                 failed = true;
                 break;
@@ -683,15 +687,16 @@ __global__ void __launch_bounds__(kWThreads, 2)
                 }
             }
             __syncwarp();
-            if (b) ++uses1;
-            else ++uses0;
-            b ^= 1;
+#pragma unroll
+            for (int t = 0; t < kWSlotCount; ++t) uses[t] += t == b ? 1 : 0;
+            b = b + 1 == kWSlotCount ? 0 : b + 1;
         }
         if (failed) {
             if (out.error && lane == 0) atomicOr(out.error, 1ull);
             // let the copies already issued land (bounded) before leaving
-            if (lane == 0 && uses0 > 0) mbar_wait(smem_addr(&s_full[0]), u32(uses0 - 1) & 1u);
-            if (lane == 0 && uses1 > 0) mbar_wait(smem_addr(&s_full[1]), u32(uses1 - 1) & 1u);
+#pragma unroll
+            for (int t = 0; t < kWSlotCount; ++t)
+                if (lane == 0 && uses[t] > 0) mbar_wait(smem_addr(&s_full[t]), u32(uses[t] - 1) & 1u);
         }
         return;
     }
@@ -908,7 +913,7 @@ __global__ void __launch_bounds__(kWThreads, 2)
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_addr(&s_empty[b]));  // this warp is done with slot b
         ++seq;
-        b ^= 1;
+        b = b + 1 == kWSlotCount ? 0 : b + 1;
     }
 }
 
@@ -1348,7 +1353,8 @@ long long wide_row_budget(int max_classes) {
     const long long per_cta = 228 * 1024 / 2 - 1024;
     const long long fixed = 6 * 1024 +  // static shared memory of the kernel (5 KB) and slack
                             (long long)dev::kWConsumers * dev::kQueue * 16 +
-                            2LL * max_classes * (long long)sizeof(dev::WideRun) + 2LL * (max_classes + 1) * 4;
+                            (long long)dev::kWSlotCount * max_classes * (long long)sizeof(dev::WideRun) +
+                            (long long)dev::kWSlotCount * (max_classes + 1) * 4;
     return std::max(2LL * 64, (per_cta - fixed) / 8);
 }
 
@@ -1386,7 +1392,8 @@ int wide_classes(const std::vector<std::string> &coefficients, const dev::u64 ad
 FastPlan wide_plan(const FastPlanner &planner, long double work, int max_classes) {
     int cap = int(std::min<long double>(kMaxModulus, std::max<long double>(64, std::sqrt(work / 48.0L))));
     // two slots of staged rows
-    const long long smem_budget = std::min<long long>(dev::kWMaxSmemWords, wide_row_budget(max_classes) / 2);
+    const long long smem_budget =
+        std::min<long long>(dev::kWMaxSmemWords, wide_row_budget(max_classes) / dev::kWSlotCount);
     for (;;) {
         FastPlan plan = planner.plan(cap, dev::kWideSlots, 1LL << 40, false);
         long long smem = 0;
@@ -1988,10 +1995,11 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
 
         const int wide_smem_words = P.wide_smem_words;
         const int wide_max_classes = P.wide_max_classes;
-        const std::size_t wide_smem = 2 * std::size_t(wide_smem_words) * 8 +
+        const std::size_t wide_smem = std::size_t(dev::kWSlotCount) * std::size_t(wide_smem_words) * 8 +
                                       std::size_t(dev::kWConsumers) * dev::kQueue * 16 +
-                                      2 * std::size_t(wide_max_classes) * sizeof(dev::WideRun) +
-                                      2 * std::size_t(wide_max_classes + 1) * 4;
+                                      std::size_t(dev::kWSlotCount) * std::size_t(wide_max_classes) *
+                                          sizeof(dev::WideRun) +
+                                      std::size_t(dev::kWSlotCount) * std::size_t(wide_max_classes + 1) * 4;
         const std::size_t narrow_smem = std::size_t(dev::kNarrowTableWords + dev::kAffWords) * 8 +
                                         std::size_t(dev::kNWarps) * dev::kQueue * 12;
         int wide_grid = 0, narrow_grid = 0;

@@ -236,6 +236,7 @@ rpg_status rpg_fast_plan(const char *const *coefficients, int32_t coefficient_co
             for (std::size_t f = 0; f < p.slots[i].size() && f < 4; ++f) plan->factors[i][f] = p.slots[i][f];
         }
         plan->bits = p.bits;
+        plan->slots = p.row_slots;
         return RPG_OK;
     });
 }

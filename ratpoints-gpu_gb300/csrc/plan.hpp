@@ -79,6 +79,7 @@ struct FastPlan {
     std::vector<std::vector<int>> slots;   // prime factors of each stage-1 modulus
     std::vector<int> moduli;               // their products
     double bits = 0;                       // expected filtering of the stage-1 rows (bits)
+    int row_slots = 2;                     // single-curve kernel: denominators staged per CTA (2 or 3)
 };
 // max_modulus caps each stage-1 modulus (table size grows as its square);
 // class_prime false keeps the plan to 2-adic classes (the dense layout of the

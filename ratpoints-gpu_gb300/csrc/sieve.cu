@@ -275,38 +275,49 @@ int max_admissible_classes(const std::vector<std::string> &coefficients, int q) 
     return std::max(1, most2 * std::max(1, most_q));
 }
 
-// Dynamic shared memory of the fast kernel: two staged row sets, the
-// consumer queues, and the two slots' class runs and item prefixes.
-std::size_t fast_dynamic_smem(int row_words, int max_classes) {
-    const std::size_t runs = (std::size_t(dev::kFSlotCount) * max_classes * sizeof(dev::FastRun) + 7) & ~std::size_t(7);
-    return std::size_t(dev::kFSlotCount) * std::size_t(row_words) * 8 +
-           std::size_t(dev::kFConsumers) * dev::kFQueue * 16 + runs +
-           std::size_t(dev::kFSlotCount) * std::size_t(max_classes + 1) * 4;
+// Dynamic shared memory of the fast kernel: `slots` staged row sets, the
+// consumer queues, and the slots' class runs and item prefixes.
+std::size_t fast_dynamic_smem(int row_words, int max_classes, int slots) {
+    const std::size_t runs = (std::size_t(slots) * max_classes * sizeof(dev::FastRun) + 7) & ~std::size_t(7);
+    return std::size_t(slots) * std::size_t(row_words) * 8 + std::size_t(dev::kFConsumers) * dev::kFQueue * 16 +
+           runs + std::size_t(slots) * std::size_t(max_classes + 1) * 4;
 }
 
 // Staged row words per slot that keep a CTA within half an SM's shared
 // memory (2 CTAs/SM, 1 KiB reserved each, 2 KiB of static shared memory).
-long long fast_row_budget(int max_classes) {
+long long fast_row_budget(int max_classes, int slots) {
     const long long per_cta = 228 * 1024 / 2 - 1024 - 2048;
-    return (per_cta - (long long)fast_dynamic_smem(0, max_classes)) / (8 * dev::kFSlotCount);
+    return (per_cta - (long long)fast_dynamic_smem(0, max_classes, slots)) / (8LL * slots);
 }
 
 FastPlan single_curve_plan(const std::vector<std::string> &coefficients, long long bound, int *max_classes) {
-    // the two staged row sets of a CTA, its queues and its two slots' class
-    // runs must fit shared memory at 2 CTAs/SM
+    // the staged row sets of a CTA, its queues and its slots' class runs must
+    // fit shared memory at 2 CTAs/SM.  Three slots stage a denominator ahead
+    // further with less shared memory per row set: they pay when sweeping a
+    // denominator is short against copying its rows (rows of at most 2^20
+    // words) and their plan filters within a quarter bit of the two-slot plan
+    // (the C2 curve: 13.22 bits either way, 30.4 ms against 31.4 ms per step;
+    // cubics with 31 M-word rows: 2 slots).
     const FastPlanner planner(coefficients, bound);
     const int classes = max_admissible_classes(coefficients, planner.class_prime());
     if (max_classes) *max_classes = classes;
-    const long long row_budget = fast_row_budget(classes);
-    FastPlan plan;
-    for (int cap = kMaxModulus;;) {
-        plan = planner.plan(cap, kMaxFastSlots, row_budget);
-        int row_words = 0;
-        for (int m : plan.moduli) row_words += (m + dev::kFExt + 1) & ~1;
-        if (row_words <= row_budget || cap <= 64) break;
-        cap = cap * 7 / 8;
-    }
-    return plan;
+    auto plan_for = [&](int slots) {
+        const long long row_budget = fast_row_budget(classes, slots);
+        FastPlan plan;
+        for (int cap = kMaxModulus;;) {
+            plan = planner.plan(cap, kMaxFastSlots, row_budget);
+            int row_words = 0;
+            for (int m : plan.moduli) row_words += (m + dev::kFExt + 1) & ~1;
+            if (row_words <= row_budget || cap <= 64) break;
+            cap = cap * 7 / 8;
+        }
+        plan.row_slots = slots;
+        return plan;
+    };
+    const FastPlan two = plan_for(2);
+    if (word_count64(bound) > (1LL << 20)) return two;
+    const FastPlan three = plan_for(dev::kFMaxSlotCount);
+    return three.bits >= two.bits - 0.25 ? three : two;
 }
 
 struct Sieve::Impl {
@@ -812,8 +823,8 @@ struct Sieve::Impl {
         F.list_runs = list_runs;
         F.list_prefix = list_prefix;
         F.list_count = list_count;
-        fast_smem = fast_dynamic_smem(F.smem_words, fast_max_classes);
-        const void *kernel = fast_kernel_ptr(F.slots);
+        fast_smem = fast_dynamic_smem(F.smem_words, fast_max_classes, fast_plan.row_slots);
+        const void *kernel = fast_kernel_ptr(F.slots, fast_plan.row_slots);
         check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(fast_smem)),
                    "cudaFuncSetAttribute");
@@ -831,34 +842,25 @@ struct Sieve::Impl {
         timings.table_wall_ms += ms_since(t0);
     }
 
-    static const void *fast_kernel_ptr(int slots) {
-        switch (slots) {
-        case 1: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<1>);
-        case 2: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<2>);
-        case 3: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<3>);
-        case 4: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<4>);
-        case 5: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<5>);
-        case 6: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<6>);
-        case 7: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<7>);
-        case 8: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<8>);
-        case 9: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<9>);
-        case 10: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<10>);
-        case 11: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<11>);
-        default: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<12>);
+    static const void *fast_kernel_ptr(int rows, int slots) {
+        switch (rows * 4 + slots) {
+#define RPG_FAST_PTR(n)                                                                       \
+    case n * 4 + 2: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<n, 2>);   \
+    case n * 4 + 3: return reinterpret_cast<const void *>(&dev::fast_sieve_kernel<n, 3>);
+        RPG_FAST_PTR(1) RPG_FAST_PTR(2) RPG_FAST_PTR(3) RPG_FAST_PTR(4) RPG_FAST_PTR(5) RPG_FAST_PTR(6)
+        RPG_FAST_PTR(7) RPG_FAST_PTR(8) RPG_FAST_PTR(9) RPG_FAST_PTR(10) RPG_FAST_PTR(11) RPG_FAST_PTR(12)
+#undef RPG_FAST_PTR
+        default: throw std::logic_error("no fast kernel for this row and slot count");
         }
     }
 
     void launch_fast(const dev::FastTables &Fl, const dev::SieveArgs &A, unsigned long long *work,
                      cudaStream_t st) const {
         const int blocks = int(std::min<long long>(grid, (A.k_count + dev::kFChunk - 1) / dev::kFChunk));
-        switch (Fl.slots) {
-#define RPG_FAST_CASE(n)                                                                 \
-    case n: dev::fast_sieve_kernel<n><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
-        RPG_FAST_CASE(1) RPG_FAST_CASE(2) RPG_FAST_CASE(3) RPG_FAST_CASE(4) RPG_FAST_CASE(5) RPG_FAST_CASE(6)
-        RPG_FAST_CASE(7) RPG_FAST_CASE(8) RPG_FAST_CASE(9) RPG_FAST_CASE(10) RPG_FAST_CASE(11)
-        default: dev::fast_sieve_kernel<12><<<blocks, dev::kFThreads, fast_smem, st>>>(Fl, A, work); break;
-#undef RPG_FAST_CASE
-        }
+        const void *kernel = fast_kernel_ptr(Fl.slots, fast_plan.row_slots);
+        void *params[] = {const_cast<dev::FastTables *>(&Fl), const_cast<dev::SieveArgs *>(&A), &work};
+        check_cuda(cudaLaunchKernel(kernel, dim3(unsigned(blocks)), dim3(dev::kFThreads), params, fast_smem, st),
+                   "fast sieve kernel launch");
     }
 
     dev::SieveArgs args(int which, long long first, long long last, long long w_lo, long long w_hi) {

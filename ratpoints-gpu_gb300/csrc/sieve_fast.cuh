@@ -39,7 +39,7 @@ constexpr int kFK = 4;                     // words per lane per step (lanes 32 
 constexpr int kFWarps = 12;                // warp 0 produces, the others sweep
 constexpr int kFThreads = kFWarps * kWarpSize;
 constexpr int kFConsumers = kFWarps - 1;
-constexpr int kFSlotCount = 2;                             // denominators in flight per CTA
+constexpr int kFMaxSlotCount = 3;                          // denominators in flight per CTA: 2 or 3
 constexpr int kFChunk = 32;                                // parameters per producer fetch
 constexpr int kFSteps = 4;                                 // steps per work item
 constexpr int kFItemWords = kWarpSize * kFK * kFSteps;     // 512 words per item
@@ -401,25 +401,25 @@ __device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs 
     (void)M;
 }
 
-template <int NS>
+template <int NS, int SLOTS>
 __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, SieveArgs A,
                                                                unsigned long long *work) {
     extern __shared__ __align__(16) u64 smem[];
     const int row_stride = T.smem_words;  // even: buffers stay 16-byte aligned
-    u64 *qmask = smem + kFSlotCount * row_stride;
+    u64 *qmask = smem + SLOTS * row_stride;
     u64 *qpos = qmask + kFConsumers * kFQueue;
     FastRun *runs0 = reinterpret_cast<FastRun *>(qpos + kFConsumers * kFQueue);  // [slots][max_classes]
-    int *prefix0 = reinterpret_cast<int *>(runs0 + kFSlotCount * T.max_classes);  // [slots][max_classes + 1]
+    int *prefix0 = reinterpret_cast<int *>(runs0 + SLOTS * T.max_classes);  // [slots][max_classes + 1]
 
-    __shared__ FastSlot slot[kFSlotCount];
+    __shared__ FastSlot slot[SLOTS];
     __shared__ FastCtx s_ctx[kFConsumers][kFCtx];
-    __shared__ __align__(8) unsigned long long s_full[kFSlotCount];
-    __shared__ __align__(8) unsigned long long s_empty[kFSlotCount];
+    __shared__ __align__(8) unsigned long long s_full[SLOTS];
+    __shared__ __align__(8) unsigned long long s_empty[SLOTS];
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
-        for (int b = 0; b < kFSlotCount; ++b) {
+        for (int b = 0; b < SLOTS; ++b) {
             mbar_init(smem_addr(&s_full[b]), 1);
             mbar_init(smem_addr(&s_empty[b]), kFConsumers);
         }
@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
         const bool lists = T.list_count != nullptr;
         long long chunk = 0;
         int j = kFChunk;                 // position inside the fetched chunk
-        int uses0 = 0, uses1 = 0;        // fills of each slot so far
+        int uses[SLOTS] = {};      // fills of each slot so far
         int b = 0;
         bool failed = false;
         for (;;) {
@@ -469,7 +469,9 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
                 break;
             }
             // slot b must be released by every consumer before it is refilled
-            const int used = b ? uses1 : uses0;
+            int used = 0;
+#pragma unroll
+            for (int t = 0; t < SLOTS; ++t) used = t == b ? uses[t] : used;
             if (used > 0 && !mbar_wait(smem_addr(&s_empty[b]), u32(used - 1) & 1u)) {
                 failed = true;
                 break;
@@ -513,15 +515,16 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
                                         u32(Md.length) * 8u, full);
                 }
             }
-            if (b) ++uses1;
-            else ++uses0;
-            b ^= 1;
+#pragma unroll
+            for (int t = 0; t < SLOTS; ++t) uses[t] += t == b ? 1 : 0;
+            b = b + 1 == SLOTS ? 0 : b + 1;
         }
         if (failed) {
             if (A.error && lane == 0) atomicOr(A.error, 1ull);
             // let the copies already issued land (bounded) before leaving
-            if (lane == 0 && uses0 > 0) mbar_wait(smem_addr(&s_full[0]), u32(uses0 - 1) & 1u);
-            if (lane == 0 && uses1 > 0) mbar_wait(smem_addr(&s_full[1]), u32(uses1 - 1) & 1u);
+#pragma unroll
+            for (int t = 0; t < SLOTS; ++t)
+                if (lane == 0 && uses[t] > 0) mbar_wait(smem_addr(&s_full[t]), u32(uses[t] - 1) & 1u);
         }
         return;
     }
@@ -669,7 +672,7 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_addr(&s_empty[b]));  // this warp is done with slot b
         ++seq;
-        b ^= 1;
+        b = b + 1 == SLOTS ? 0 : b + 1;
     }
 }
 

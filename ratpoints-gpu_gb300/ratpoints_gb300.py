@@ -79,7 +79,7 @@ class SearchOptions(ctypes.Structure):
 class FastPlanInfo(ctypes.Structure):
     _fields_ = [("class_prime", ctypes.c_int32), ("modulus_count", ctypes.c_int32),
                 ("moduli", ctypes.c_int32 * 16), ("factors", (ctypes.c_int32 * 4) * 16),
-                ("bits", ctypes.c_double)]
+                ("bits", ctypes.c_double), ("slots", ctypes.c_int32)]
 
 
 class BatchStats(ctypes.Structure):
@@ -395,7 +395,8 @@ def fast_plan(coefficients, bound):
     _check(load().rpg_fast_plan(_strings(coeffs), len(coeffs), int(bound), ctypes.byref(info)))
     n = info.modulus_count
     return {"class_prime": info.class_prime, "moduli": list(info.moduli[:n]),
-            "factors": [[f for f in info.factors[i] if f] for i in range(n)], "bits": info.bits}
+            "factors": [[f for f in info.factors[i] if f] for i in range(n)], "bits": info.bits,
+            "slots": info.slots}
 
 
 def preverify(coefficients, a, b):
