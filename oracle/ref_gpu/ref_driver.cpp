@@ -1,6 +1,6 @@
 // ref_driver.cpp - host driver for the reference's own GPU sieve kernels.
 //
-// BASELINE AND CHECKER INFRASTRUCTURE ONLY (tests/ and bench.py load it; no
+// REFERENCE-ARM AND CHECKER INFRASTRUCTURE ONLY (tests/ and bench.py load it; no
 // product path does).  oracle/_ref/ref_sieve.cubin is the reference's
 // src/sieve.cu compiled unchanged for sm_103a (oracle/ref_gpu/build_ref.py).
 // This file loads that cubin through the CUDA driver API, finds its
