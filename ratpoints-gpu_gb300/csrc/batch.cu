@@ -228,48 +228,67 @@ __device__ __forceinline__ int find_spec(const Spec *specs, int nspecs, long lon
     return lo;
 }
 
+constexpr int kPatternWords = 4;  // words per thread (see composite_kernel)
+
 __global__ void pattern_kernel(const PatternSpec *specs, int nspecs, const u64 *affine,
                                const unsigned short *inv_table, u64 *patterns, long long total) {
-    const long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (id >= total) return;
-    const PatternSpec S = specs[find_spec(specs, nspecs, id)];
-    const int q = S.q;
-    const int rel = int(id - S.offset);
-    const int rho = rel / q;
-    const int u = rel % q;
-    const u64 *aff = affine + S.aff;
-    const int inv = rho ? inv_table[q * kMaximumPrime + rho] : 0;
-    int x = (S.s * u) % q;
-    u64 word = 0;
-    for (int j = 0; j < 64; ++j) {
-        bool ok;
-        if (rho == 0) {
-            ok = x != 0 && S.lead_ok;  // q | d: q !| a, and c_n a square mod q for even degree
-        } else {
-            const int y = (x * inv) % q;
-            ok = (__ldg(aff + (y >> 6)) >> (y & 63)) & 1;
+    const long long base = (long long)blockIdx.x * blockDim.x * kPatternWords + threadIdx.x;
+    if (base >= total) return;
+    int s = find_spec(specs, nspecs, base);
+    for (int i = 0; i < kPatternWords; ++i) {
+        const long long id = base + (long long)i * blockDim.x;
+        if (id >= total) break;
+        while (s + 1 < nspecs && specs[s + 1].offset <= id) ++s;
+        const PatternSpec S = specs[s];
+        const int q = S.q;
+        const int rel = int(id - S.offset);
+        const int rho = rel / q;
+        const int u = rel % q;
+        const u64 *aff = affine + S.aff;
+        const int inv = rho ? inv_table[q * kMaximumPrime + rho] : 0;
+        int x = (S.s * u) % q;
+        u64 word = 0;
+        for (int j = 0; j < 64; ++j) {
+            bool ok;
+            if (rho == 0) {
+                ok = x != 0 && S.lead_ok;  // q | d: q !| a, and c_n a square mod q for even degree
+            } else {
+                const int y = (x * inv) % q;
+                ok = (__ldg(aff + (y >> 6)) >> (y & 63)) & 1;
+            }
+            if (ok) word |= u64(1) << j;
+            x += S.t;
+            if (x >= q) x -= q;
         }
-        if (ok) word |= u64(1) << j;
-        x += S.t;
-        if (x >= q) x -= q;
+        patterns[id] = word;
     }
-    patterns[id] = word;
 }
+
+// kCompositeWords words per thread, a block's threads interleaved (stores
+// stay coalesced): one binary search over the specs per thread, then the
+// spec index only moves forward.
+constexpr int kCompositeWords = 16;
 
 __global__ void composite_kernel(const CompositeSpec *specs, int nspecs, const u64 *patterns,
                                  u64 *rows, long long total) {
-    const long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (id >= total) return;
-    const CompositeSpec &S = specs[find_spec(specs, nspecs, id)];
-    const long long rel = id - S.offset;
-    const int rho = int(rel / S.length);
-    const int u = int(rel % S.length) % S.m;
-    u64 word = ~u64(0);
-    for (int f = 0; f < S.nf; ++f) {
-        const int q = S.q[f];
-        word &= __ldg(patterns + S.pattern[f] + (rho % q) * q + (u % q));
+    const long long base = (long long)blockIdx.x * blockDim.x * kCompositeWords + threadIdx.x;
+    if (base >= total) return;
+    int s = find_spec(specs, nspecs, base);
+    for (int i = 0; i < kCompositeWords; ++i) {
+        const long long id = base + (long long)i * blockDim.x;
+        if (id >= total) break;
+        while (s + 1 < nspecs && specs[s + 1].offset <= id) ++s;
+        const CompositeSpec &S = specs[s];
+        const long long rel = id - S.offset;
+        const int rho = int(rel / S.length);
+        const int u = int(rel % S.length) % S.m;
+        u64 word = ~u64(0);
+        for (int f = 0; f < S.nf; ++f) {
+            const int q = S.q[f];
+            word &= __ldg(patterns + S.pattern[f] + (rho % q) * q + (u % q));
+        }
+        rows[id] = word;
     }
-    rows[id] = word;
 }
 
 // ---------------------------------------------------------------------------
@@ -2075,12 +2094,16 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
                 check_cuda(cudaGetLastError(), "affine_kernel launch");
             }
             if (P.pattern_words) {
-                dev::pattern_kernel<<<unsigned((P.pattern_words + 255) / 256), 256, 0, stream>>>(
+                dev::pattern_kernel<<<unsigned((P.pattern_words + 256 * dev::kPatternWords - 1) /
+                                               (256 * dev::kPatternWords)),
+                                      256, 0, stream>>>(
                     d_pspecs.p, int(P.pspecs.size()), d_aff.p, d_inv.p, d_patterns.p, P.pattern_words);
                 check_cuda(cudaGetLastError(), "pattern_kernel launch");
             }
             if (P.row_words) {
-                dev::composite_kernel<<<unsigned((P.row_words + 255) / 256), 256, 0, stream>>>(
+                dev::composite_kernel<<<unsigned((P.row_words + 256 * dev::kCompositeWords - 1) /
+                                                 (256 * dev::kCompositeWords)),
+                                        256, 0, stream>>>(
                     d_cspecs.p, int(P.cspecs.size()), d_patterns.p, d_rows.p, P.row_words);
                 check_cuda(cudaGetLastError(), "composite_kernel launch");
             }
