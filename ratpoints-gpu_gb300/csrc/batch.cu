@@ -1533,6 +1533,27 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                (long double)P.work[b].words * P.work[b].count;
     });
     std::vector<std::pair<std::size_t, std::size_t>> list_curves;  // (descriptor, curve) with class lists
+    // items: about 2^21 row words each (wide), about 2^18 swept words and at
+    // least one denominator per warp (narrow), one set per numerator range
+    auto item_chunk = [&](const CurveWork &cw) -> long long {
+        return cw.wide ? std::max(1LL, std::min<long long>(1 << 16, (1LL << 21) / cw.words))
+                       : std::max<long long>(dev::kNWarps,
+                                             std::min<long long>(1 << 16, (1LL << 18) / std::max(1LL, cw.swept)));
+    };
+    {
+        // sizes first, so that the vectors grow once
+        std::size_t wide_items = 0, narrow_items = 0;
+        for (std::size_t i : order) {
+            const CurveWork &cw = P.work[i];
+            const std::size_t n = curves[i].intervals.size();
+            const long long ranges = n > 0 && n <= std::size_t(dev::kMaxIntervals) ? (long long)n : 1;
+            const long long chunk = item_chunk(cw);
+            (cw.wide ? wide_items : narrow_items) += std::size_t(ranges * ((cw.count + chunk - 1) / chunk));
+        }
+        P.wide_items.reserve(wide_items);
+        P.narrow_items.reserve(narrow_items);
+    }
+    long long list_count_total = 0, list_runs_total = 0, list_prefix_total = 0;
     for (std::size_t i : order) {
         const BatchCurveSpec &c = curves[i];
         CurveWork &cw = P.work[i];
@@ -1661,12 +1682,12 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 // room for the curve's class lists (64 q denominator classes)
                 const int lm = C.list_max;
                 const std::size_t ncombo = std::size_t(64) * std::size_t(q);
-                C.list_count = (long long)P.list_count.size();
-                C.list_runs = (long long)P.list_runs.size();
-                C.list_prefix = (long long)P.list_prefix.size();
-                P.list_count.resize(P.list_count.size() + ncombo, 0);
-                P.list_runs.resize(P.list_runs.size() + ncombo * std::size_t(lm));
-                P.list_prefix.resize(P.list_prefix.size() + ncombo * std::size_t(lm + 1), 0);
+                C.list_count = list_count_total;
+                C.list_runs = list_runs_total;
+                C.list_prefix = list_prefix_total;
+                list_count_total += (long long)ncombo;
+                list_runs_total += (long long)ncombo * lm;
+                list_prefix_total += (long long)ncombo * (lm + 1);
                 list_curves.push_back({P.wide.size(), i});  // filled below, in parallel
                 // classes of at most 128 words are swept kWK at a time
                 const long long max_words = (C.count_q + 1 + 63) >> 6;
@@ -1676,8 +1697,7 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 C.list_count = -1;
             }
             P.wide_max_classes = std::max(P.wide_max_classes, cw.classes);
-            // items of about 2^20 row words, one set per numerator range
-            const long long chunk = std::max(1LL, std::min<long long>(1 << 16, (1LL << 20) / cw.words));
+            const long long chunk = item_chunk(cw);
             for (int range = 0; range < std::max(1, C.nint); ++range)
                 for (long long f = c.first; f <= c.last; f += chunk)
                     P.wide_items.push_back({f, int(P.wide.size()), int(std::min(chunk, c.last - f + 1)),
@@ -1741,20 +1761,14 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             // dense layout: bit j of a word holds a = -H + 64 w + j, so a = j - H (mod 64)
             const dev::u64 *by_class = cw.adm2;
             const int h64 = int(H % 64);
-            for (int dd = 0; dd < 64; ++dd) {
-                dev::u64 mask = 0;
-                for (int j = 0; j < 64; ++j)
-                    if ((by_class[dd] >> ((j - h64 + 64) % 64)) & 1) mask |= dev::u64(1) << j;
-                C.dense2[dd] = mask;
-            }
+            for (int dd = 0; dd < 64; ++dd)  // bit j = class bit (j - H) mod 64: a rotation
+                C.dense2[dd] = h64 ? (by_class[dd] << h64) | (by_class[dd] >> (64 - h64)) : by_class[dd];
             for (int ci = 0; ci < kCandidatePrimes; ++ci) {
                 const int p = cands[ci];
                 C.neg_h[ci] = (unsigned short)((p - H % p) % p);
             }
             device_intervals(c.intervals, C.nint, C.lo, C.hi);
-            // items of about 2^16 swept words, at least one denominator per warp
-            const long long chunk = std::max<long long>(
-                dev::kNWarps, std::min<long long>(1 << 14, (1LL << 16) / std::max(1LL, cw.swept)));
+            const long long chunk = item_chunk(cw);
             for (int range = 0; range < std::max(1, C.nint); ++range)
                 for (long long f = c.first; f <= c.last; f += chunk)
                     P.narrow_items.push_back({f, int(P.narrow.size()),
@@ -1782,6 +1796,9 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
     }
     // class lists by denominator class k = (d mod 64) q + (d mod q), in the
     // order the producer lays out classes for interval curves
+    P.list_count.resize(std::size_t(list_count_total));
+    P.list_runs.resize(std::size_t(list_runs_total));
+    P.list_prefix.resize(std::size_t(list_prefix_total));
     parallel_for(list_curves.size(), [&](std::size_t j) {
         const dev::WideCurve &C = P.wide[list_curves[j].first];
         const CurveWork &cw = P.work[list_curves[j].second];
