@@ -1533,12 +1533,23 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                (long double)P.work[b].words * P.work[b].count;
     });
     std::vector<std::pair<std::size_t, std::size_t>> list_curves;  // (descriptor, curve) with class lists
-    // items: about 2^21 row words each (wide), about 2^18 swept words and at
-    // least one denominator per warp (narrow), one set per numerator range
+    // items: large enough that building and fetching them stays cheap, small
+    // enough that a small batch still spreads over the device (about 8,192
+    // items per kernel): up to 2^21 row words (wide) and 2^18 swept words
+    // (narrow), at least one denominator per warp; one set per numerator range
+    long double wide_work = 0, narrow_work = 0;
+    for (std::size_t i : order) {
+        const CurveWork &cw = P.work[i];
+        (cw.wide ? wide_work : narrow_work) += (long double)(cw.wide ? cw.words : cw.swept) * cw.count;
+    }
+    const long long wide_item =
+        (long long)std::min<long double>(1LL << 21, std::max<long double>(1LL << 14, wide_work / 8192));
+    const long long narrow_item =
+        (long long)std::min<long double>(1LL << 18, std::max<long double>(1LL << 12, narrow_work / 8192));
     auto item_chunk = [&](const CurveWork &cw) -> long long {
-        return cw.wide ? std::max(1LL, std::min<long long>(1 << 16, (1LL << 21) / cw.words))
+        return cw.wide ? std::max(1LL, std::min<long long>(1 << 16, wide_item / cw.words))
                        : std::max<long long>(dev::kNWarps,
-                                             std::min<long long>(1 << 16, (1LL << 18) / std::max(1LL, cw.swept)));
+                                             std::min<long long>(1 << 16, narrow_item / std::max(1LL, cw.swept)));
     };
     {
         // sizes first, so that the vectors grow once
