@@ -164,20 +164,18 @@ FastPlan FastPlanner::plan(int max_modulus, int max_slots, long long row_budget,
     // most headroom that it fits, else opens a new one; it is tried with the
     // primes ordered by bits and by bits per bit of size, over primes below 72,
     // 128 and the planner's limit, and the packing with the most bits is kept.
-    auto pack = [&](std::vector<std::pair<double, int>> order, int limit, bool by_density, int slots,
-                    int cap) {
-        if (by_density)
-            std::sort(order.begin(), order.end(),
-                      [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
-                          const double da = a.first / std::log2(double(a.second));
-                          const double db = b.first / std::log2(double(b.second));
-                          return da != db ? da > db : a.second < b.second;
-                      });
-        else
-            std::sort(order.begin(), order.end(),
-                      [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
-                          return a.first != b.first ? a.first > b.first : a.second < b.second;
-                      });
+    // the two orders, sorted once for every packing below
+    std::vector<std::pair<double, int>> by_bits(strength), by_density(strength);
+    std::sort(by_bits.begin(), by_bits.end(), [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+        return a.first != b.first ? a.first > b.first : a.second < b.second;
+    });
+    std::sort(by_density.begin(), by_density.end(),
+              [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+                  const double da = a.first / std::log2(double(a.second));
+                  const double db = b.first / std::log2(double(b.second));
+                  return da != db ? da > db : a.second < b.second;
+              });
+    auto pack = [&](const std::vector<std::pair<double, int>> &order, int limit, int slots, int cap) {
         FastPlan out;
         out.class_prime = plan.class_prime;
         for (const auto &s : order) {
@@ -216,8 +214,8 @@ FastPlan FastPlanner::plan(int max_modulus, int max_slots, long long row_budget,
             candidate = plan;
             candidate.bits = -1;
             for (int limit : {72, kFastPrimeLimit, prime_limit_})
-                for (bool density : {false, true}) {
-                    FastPlan packed = pack(strength, std::min(limit, prime_limit_), density, slots, cap);
+                for (const auto *order : {&by_bits, &by_density}) {
+                    FastPlan packed = pack(*order, std::min(limit, prime_limit_), slots, cap);
                     if (packed.bits > candidate.bits) candidate = packed;
                 }
             long long rows = 0;
