@@ -318,6 +318,14 @@ rpg_status rpg_server_wait(rpg_server *server, uint64_t request_id, double timeo
 /* Finishes the admitted work, then releases the server. */
 void rpg_server_destroy(rpg_server *server);
 
+/* Self-test of the bounded mbarrier wait the pipelined sieve kernels use: one
+ * thread waits up to polls (1..2^20) polls on a barrier phase that completes
+ * only if arrive is non-zero.  Returns RPG_OK when the wait succeeded and
+ * RPG_E_TIMEOUT when it gave up (the kernel returns normally and the context
+ * stays usable), as a sieve launch reports a row copy that never landed.
+ * No reference counterpart: the reference's kernels have no waits. */
+rpg_status rpg_bounded_wait_selftest(int32_t device, int32_t polls, int32_t arrive);
+
 int32_t rpg_device_count(void);
 int32_t rpg_abi_version(void);
 const char *rpg_last_error(void);

@@ -78,8 +78,9 @@ __device__ __forceinline__ bool mbar_try_wait(u32 bar, u32 parity) {
     return done != 0;
 }
 // Bounded wait for the phase with the given parity; false if the limit ran out.
-__device__ __forceinline__ bool mbar_wait(u32 bar, u32 parity) {
-    for (int i = 0; i < (1 << 24); ++i)
+constexpr int kMbarPolls = 1 << 24;
+__device__ __forceinline__ bool mbar_wait(u32 bar, u32 parity, int polls = kMbarPolls) {
+    for (int i = 0; i < polls; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }

@@ -166,6 +166,8 @@ def load():
     lib.rpg_preverify.restype = S
     lib.rpg_preverify.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
                                   ctypes.POINTER(ctypes.c_int32)]
+    lib.rpg_bounded_wait_selftest.restype = S
+    lib.rpg_bounded_wait_selftest.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
     lib.rpg_cli_main.restype = ctypes.c_int32
     lib.rpg_cli_main.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_char_p)]
     lib.rpg_session_create.restype = S
@@ -406,6 +408,12 @@ def preverify(coefficients, a, b):
     flag = ctypes.c_int32(-1)
     _check(load().rpg_preverify(_strings(coeffs), len(coeffs), int(a), int(b), ctypes.byref(flag)))
     return bool(flag.value)
+
+
+def bounded_wait_selftest(polls, arrive, device=0):
+    """Runs the bounded mbarrier wait self-test; raises RpgError with status
+    RPG_E_TIMEOUT (4) when the wait gave up."""
+    _check(load().rpg_bounded_wait_selftest(int(device), int(polls), int(bool(arrive))))
 
 
 def square_root(coefficients, a, b):

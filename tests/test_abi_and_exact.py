@@ -130,3 +130,11 @@ def test_cli_help(rpg):
     result = rpg.cli(["--help"])
     assert result.returncode == 0 and b"Usage: ratpoints_gpu" in result.stdout
     assert rpg.cli([]).returncode == 1
+
+
+def test_bounded_wait_selftest_rejects_bad_polls(rpg):
+    # argument checks come before any CUDA call
+    for polls in (0, -5, (1 << 20) + 1):
+        with pytest.raises(rpg.RpgError) as err:
+            rpg.bounded_wait_selftest(polls, arrive=True)
+        assert err.value.status == 1
