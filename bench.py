@@ -7,8 +7,9 @@ uniform in [-2^32, 2^32), box a in [-5,000,000, 5,000,000], b in
 One step = one full sieve pass over the box with the per-curve tables already
 resident on the device (value), timed with CUDA events on the sieve stream;
 e2e = the same search through the C ABI rpg_point_search (coefficient strings
-in, verified points out, host<->device copies and exact verification inside
-the timed region).  Sites are counted as reduced pairs gcd(a, b) = 1, the
+in, verified points out; planning, table build, host<->device copies and
+exact verification inside the timed region), median of three searches after
+two untimed ones.  Sites are counted as reduced pairs gcd(a, b) = 1, the
 metric's definition; the rectangle count is in config.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -476,7 +477,10 @@ def main():
     parser.add_argument("--reference-plan-steps", type=int, default=2)
     parser.add_argument("--reference-gpu-denominators", type=int, default=655360)
     parser.add_argument("--denominators", type=int, default=DENOMINATORS)
-    parser.add_argument("--e2e-steps", type=int, default=1, choices=range(1, 100), metavar="N")
+    parser.add_argument("--e2e-steps", type=int, default=3, choices=range(1, 100), metavar="N",
+                        help="timed searches through rpg_point_search (median reported)")
+    parser.add_argument("--e2e-warmup", type=int, default=2, choices=range(0, 100), metavar="N",
+                        help="untimed searches through rpg_point_search before them")
     parser.add_argument("--cpu-seconds", type=float, default=12.0)
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--batch-curves", type=int, default=4096,
@@ -560,11 +564,12 @@ def main():
 
     # e2e through the C ABI: host strings in, verified points out
     e2e_times, e2e_stats, points = [], None, None
-    for _ in range(args.e2e_steps):
+    for i in range(args.e2e_warmup + args.e2e_steps):
         t0 = time.perf_counter()
         points, e2e_stats = rpg.point_search(coeffs, HEIGHT, first_b, last_b, plan=args.plan,
                                              include_infinity=True)
-        e2e_times.append(time.perf_counter() - t0)
+        if i >= args.e2e_warmup:
+            e2e_times.append(time.perf_counter() - t0)
     e2e_s = sorted(e2e_times)[len(e2e_times) // 2]
     if rank != 0:
         return

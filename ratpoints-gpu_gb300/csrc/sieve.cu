@@ -22,6 +22,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <future>
+#include <tuple>
+#include <utility>
 
 #include "plan.hpp"
 #include "preverify.hpp"
@@ -324,7 +327,10 @@ struct Sieve::Impl {
     SieveOptions opt;
     long long bound = 0, words = 0;
     int device = 0, grid = 0;
-    cudaStream_t stream = nullptr, copy_stream = nullptr;
+    // stream: table builds and launches; copy_stream: survivor downloads;
+    // count_stream: each launch's counter words, so that their small copy
+    // does not sit between two launches on the launch stream.
+    cudaStream_t stream = nullptr, copy_stream = nullptr, count_stream = nullptr;
     dev::RefTables T{};
     dev::u64 *rows = nullptr;
     // fast plan
@@ -411,7 +417,8 @@ struct Sieve::Impl {
         h_d = nullptr;
         if (stream) cudaStreamDestroy(stream);
         if (copy_stream) cudaStreamDestroy(copy_stream);
-        stream = copy_stream = nullptr;
+        if (count_stream) cudaStreamDestroy(count_stream);
+        stream = copy_stream = count_stream = nullptr;
     }
 
     void build_tables(const std::vector<std::string> &coefficients) {
@@ -479,10 +486,20 @@ struct Sieve::Impl {
 
     void init(const std::vector<std::string> &coefficients) {
         auto t0 = Clock::now();
+        // The fast plan needs only the coefficients and the bound: choose it
+        // on a host thread while the streams and buffers are created.
+        PlannedRows planned;
+        if (opt.plan == PlanKind::fast)
+            planned = std::async(std::launch::async, [&coefficients, h = bound] {
+                int max_classes = 0;
+                FastPlan p = single_curve_plan(coefficients, h, &max_classes);
+                return std::make_pair(std::move(p), max_classes);
+            });
         if (opt.device >= 0) check_cuda(cudaSetDevice(opt.device), "cudaSetDevice");
         check_cuda(cudaGetDevice(&device), "cudaGetDevice");
         check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
         check_cuda(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(cudaStreamCreateWithFlags(&count_stream, cudaStreamNonBlocking), "cudaStreamCreate");
         check_cuda(cudaFuncSetAttribute(dev::ref_sieve_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(dev::kRefSmem)),
@@ -521,7 +538,7 @@ struct Sieve::Impl {
         check_cuda(cudaMallocHost(&h_d, std::size_t(initial) * sizeof(int)), "cudaMallocHost");
         host_capacity = initial;
         timings.workspace_ms += ms_since(t0);
-        if (opt.plan == PlanKind::fast) build_fast_tables(coefficients);
+        if (opt.plan == PlanKind::fast) build_fast_tables(coefficients, planned);
         else build_tables(coefficients);
         if (opt.preverify) {
             preverifier.prepare({&coefficients}, stream);
@@ -532,11 +549,12 @@ struct Sieve::Impl {
     // Fast plan: the per-curve plan (class prime, stage-1 moduli), class-layout
     // tables for the stage-1 moduli and the 36 reference candidates, and the
     // admissible-class tables (2-adic by d mod 64, residues mod q by d mod q).
-    void build_fast_tables(const std::vector<std::string> &coefficients) {
+    using PlannedRows = std::future<std::pair<FastPlan, int>>;
+
+    void build_fast_tables(const std::vector<std::string> &coefficients, PlannedRows &planned) {
         auto t0 = Clock::now();
-        // the two staged row sets of a CTA, its queues and its two slots' class
-        // runs must fit shared memory at 2 CTAs/SM
-        fast_plan = single_curve_plan(coefficients, bound, &fast_max_classes);
+        // the plan was started on a host thread while the buffers were set up
+        std::tie(fast_plan, fast_max_classes) = planned.get();
         const int n = int(coefficients.size()) - 1;
         const int q = fast_plan.class_prime;
         const long long M = 64LL * q;
@@ -924,10 +942,13 @@ struct Sieve::Impl {
             ++timings.launches;
         }
         check_cuda(cudaEventRecord(b.end, stream), "cudaEventRecord");
+        // The buffer is launched into again only after the host has waited
+        // for b.copied, so this copy ends before the memset of its next launch.
+        check_cuda(cudaStreamWaitEvent(count_stream, b.end, 0), "cudaStreamWaitEvent");
         check_cuda(cudaMemcpyAsync(h_count + 4 * which, b.count, 4 * sizeof(unsigned long long),
-                                   cudaMemcpyDeviceToHost, stream),
+                                   cudaMemcpyDeviceToHost, count_stream),
                    "download survivor count");
-        check_cuda(cudaEventRecord(b.copied, stream), "cudaEventRecord");
+        check_cuda(cudaEventRecord(b.copied, count_stream), "cudaEventRecord");
         timings.d2h_bytes += 4 * sizeof(unsigned long long);
         ++timings.launches;
     }
@@ -1057,7 +1078,7 @@ struct Sieve::Impl {
             const int which = buf[0].busy ? 1 : 0;
             if (buf[which].busy) throw std::logic_error("no free survivor buffer");
             launch(which, p.first, p.last, p.w_lo, p.w_hi);
-            check_cuda(cudaStreamSynchronize(stream), "sieve kernel");
+            check_cuda(cudaEventSynchronize(buf[which].copied), "sieve kernel");
             buf[which].busy = false;
             // the counter words came back with the launch: [2] is its error word
             if (h_count[4 * which + 2]) throw DeviceTimeout("sieve kernel: bounded wait for a row copy timed out");

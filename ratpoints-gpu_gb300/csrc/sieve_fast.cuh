@@ -40,7 +40,7 @@ constexpr int kFWarps = 12;                // warp 0 produces, the others sweep
 constexpr int kFThreads = kFWarps * kWarpSize;
 constexpr int kFConsumers = kFWarps - 1;
 constexpr int kFMaxSlotCount = 3;                          // denominators in flight per CTA: 2 or 3
-constexpr int kFChunk = 32;                                // parameters per producer fetch
+constexpr int kFChunk = 4;                                 // parameters per producer fetch
 constexpr int kFSteps = 4;                                 // steps per work item
 constexpr int kFItemWords = kWarpSize * kFK * kFSteps;     // 512 words per item
 constexpr int kFExt = kWarpSize * (kFK - 1);               // row extension
