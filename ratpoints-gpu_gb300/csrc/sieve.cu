@@ -327,10 +327,18 @@ struct Sieve::Impl {
     SieveOptions opt;
     long long bound = 0, words = 0;
     int device = 0, grid = 0;
-    // stream: table builds and launches; copy_stream: survivor downloads;
-    // count_stream: each launch's counter words, so that their small copy
-    // does not sit between two launches on the launch stream.
-    cudaStream_t stream = nullptr, copy_stream = nullptr, count_stream = nullptr;
+    // stream: table builds and the launches into buffer 0; stream2: the
+    // launches into buffer 1, so that a launch's first CTAs take the SMs that
+    // the previous launch's last CTAs leave idle; copy_stream: survivor
+    // downloads; count_stream: each launch's counter words, so that their
+    // small copy does not sit between two launches.
+    cudaStream_t stream = nullptr, stream2 = nullptr, copy_stream = nullptr, count_stream = nullptr;
+    cudaEvent_t fork_event = nullptr, join_event = nullptr;  // count_only across both launch streams
+    // Device time of a search: launches on the two streams overlap, so each
+    // batch adds the part of its [begin, end] interval after the previous
+    // batch's end, both measured from an origin recorded at start().
+    cudaEvent_t origin = nullptr;
+    float last_end_ms = 0;
     dev::RefTables T{};
     dev::u64 *rows = nullptr;
     // fast plan
@@ -418,7 +426,13 @@ struct Sieve::Impl {
         if (stream) cudaStreamDestroy(stream);
         if (copy_stream) cudaStreamDestroy(copy_stream);
         if (count_stream) cudaStreamDestroy(count_stream);
-        stream = copy_stream = count_stream = nullptr;
+        if (stream2) cudaStreamDestroy(stream2);
+        if (fork_event) cudaEventDestroy(fork_event);
+        if (join_event) cudaEventDestroy(join_event);
+        if (origin) cudaEventDestroy(origin);
+        origin = nullptr;
+        stream = stream2 = copy_stream = count_stream = nullptr;
+        fork_event = join_event = nullptr;
     }
 
     void build_tables(const std::vector<std::string> &coefficients) {
@@ -500,6 +514,10 @@ struct Sieve::Impl {
         check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
         check_cuda(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
         check_cuda(cudaStreamCreateWithFlags(&count_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(cudaEventCreateWithFlags(&fork_event, cudaEventDisableTiming), "cudaEventCreate");
+        check_cuda(cudaEventCreateWithFlags(&join_event, cudaEventDisableTiming), "cudaEventCreate");
+        check_cuda(cudaEventCreate(&origin), "cudaEventCreate");
         check_cuda(cudaFuncSetAttribute(dev::ref_sieve_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(dev::kRefSmem)),
@@ -898,16 +916,21 @@ struct Sieve::Impl {
         return A;
     }
 
-    // Counting pass: survivors accumulate in buffer 0's counter across launches.
-    void launch_counting(long long first, long long last, long long w_lo, long long w_hi) {
+    cudaStream_t launch_stream(int which) const { return which ? stream2 : stream; }
+
+    // Counting pass: survivors accumulate in buffer 0's counter across
+    // launches; launch i runs on launch stream i mod 2 with that buffer's
+    // work counter.
+    void launch_counting(int which, long long first, long long last, long long w_lo, long long w_hi) {
         const dev::SieveArgs A = args(0, first, last, w_lo, w_hi);
-        check_cuda(cudaMemsetAsync(buf[0].count + 1, 0, sizeof(unsigned long long), stream),
+        const cudaStream_t st = launch_stream(which);
+        check_cuda(cudaMemsetAsync(buf[which].count + 1, 0, sizeof(unsigned long long), st),
                    "cudaMemsetAsync");
-        launch_kernel(A, buf[0].count + 1);
+        launch_kernel(A, buf[which].count + 1, st);
         ++timings.launches;
     }
 
-    void launch_kernel(const dev::SieveArgs &A, unsigned long long *work) {
+    void launch_kernel(const dev::SieveArgs &A, unsigned long long *work, cudaStream_t st) {
         if (opt.plan == PlanKind::fast) {
             dev::FastTables Fl = F;
             for (int i = 0; i < kCandidatePrimes; ++i)
@@ -918,10 +941,10 @@ struct Sieve::Impl {
                 Fl.list_prefix = nullptr;
                 Fl.list_count = nullptr;
             }
-            launch_fast(Fl, A, work, stream);
+            launch_fast(Fl, A, work, st);
         } else {
             const int blocks = int(std::min<long long>(grid, A.k_count));
-            dev::ref_sieve_kernel<<<blocks, dev::kThreads, dev::kRefSmem, stream>>>(T, A);
+            dev::ref_sieve_kernel<<<blocks, dev::kThreads, dev::kRefSmem, st>>>(T, A);
         }
         check_cuda(cudaGetLastError(), "sieve kernel launch");
     }
@@ -932,16 +955,16 @@ struct Sieve::Impl {
         b.last = last;
         b.busy = true;
         const dev::SieveArgs A = args(which, first, last, w_lo, w_hi);
-        check_cuda(cudaMemsetAsync(b.count, 0, 4 * sizeof(unsigned long long), stream),
-                   "cudaMemsetAsync");
-        check_cuda(cudaEventRecord(b.begin, stream), "cudaEventRecord");
-        launch_kernel(A, b.count + 1);
+        const cudaStream_t st = launch_stream(which);
+        check_cuda(cudaMemsetAsync(b.count, 0, 4 * sizeof(unsigned long long), st), "cudaMemsetAsync");
+        check_cuda(cudaEventRecord(b.begin, st), "cudaEventRecord");
+        launch_kernel(A, b.count + 1, st);
         if (opt.preverify) {
             preverifier.launch(b.a, b.d, nullptr, b.count, (unsigned long long)b.cap, b.pa, b.pd, nullptr,
-                               b.count + 3, nullptr, stream);
+                               b.count + 3, nullptr, st);
             ++timings.launches;
         }
-        check_cuda(cudaEventRecord(b.end, stream), "cudaEventRecord");
+        check_cuda(cudaEventRecord(b.end, st), "cudaEventRecord");
         // The buffer is launched into again only after the host has waited
         // for b.copied, so this copy ends before the memset of its next launch.
         check_cuda(cudaStreamWaitEvent(count_stream, b.end, 0), "cudaStreamWaitEvent");
@@ -976,9 +999,13 @@ struct Sieve::Impl {
         if (err) throw DeviceTimeout("sieve kernel: bounded wait for a row copy timed out");
     }
 
+    // Device time a completed batch adds (see origin).
     float elapsed(const Buffer &b) {
-        float ms = 0;
-        cudaEventElapsedTime(&ms, b.begin, b.end);
+        float t0 = 0, t1 = 0;
+        cudaEventElapsedTime(&t0, origin, b.begin);
+        cudaEventElapsedTime(&t1, origin, b.end);
+        const float ms = std::max(0.0f, t1 - std::max(t0, last_end_ms));
+        last_end_ms = std::max(last_end_ms, t1);
         return ms;
     }
 
@@ -1019,6 +1046,7 @@ struct Sieve::Impl {
         const long long cap = std::min<long long>(capacity, (long long)(n + n / 4 + 1024));
         const auto t0 = Clock::now();
         check_cuda(cudaStreamSynchronize(stream), "sieve stream");
+        check_cuda(cudaStreamSynchronize(stream2), "sieve stream");
         cudaFree(b.a);
         cudaFree(b.d);
         cudaFree(b.pa);
@@ -1161,6 +1189,8 @@ void Sieve::start(long long first, long long last, long long batch_size) {
     if (impl_->opt.square && last > 46340) throw std::invalid_argument("invalid denominator range");
     if (last > 2147483647LL) throw std::invalid_argument("invalid denominator range");
     cancel();
+    check_cuda(cudaEventRecord(impl_->origin, impl_->stream), "cudaEventRecord");
+    impl_->last_end_ms = 0;
     impl_->q_next = first;
     impl_->q_last = last;
     impl_->q_batch = std::max<long long>(1, batch_size);
@@ -1170,6 +1200,7 @@ bool Sieve::next(BatchView &out) { return impl_->next(out); }
 
 void Sieve::cancel() {
     check_cuda(cudaStreamSynchronize(impl_->stream), "sieve stream");
+    check_cuda(cudaStreamSynchronize(impl_->stream2), "sieve stream");
     for (auto &b : impl_->buf) b.busy = false;
     impl_->order.clear();
     impl_->pieces.clear();
@@ -1268,11 +1299,17 @@ unsigned long long Sieve::count_only(long long first, long long last, long long 
     auto &b = I.buf[0];
     check_cuda(cudaMemsetAsync(b.count, 0, 3 * sizeof(unsigned long long), I.stream),
                "cudaMemsetAsync");
+    // the second launch stream starts after the reset and joins before the read
+    check_cuda(cudaEventRecord(I.fork_event, I.stream), "cudaEventRecord");
+    check_cuda(cudaStreamWaitEvent(I.stream2, I.fork_event, 0), "cudaStreamWaitEvent");
+    int which = 0;
     for (long long f = first; f <= last; f += batch_size) {
         const long long l = std::min(last, f + batch_size - 1);
-        for (long long w = 0; w < I.words; w += I.max_tile)
-            I.launch_counting(f, l, w, std::min(I.words, w + I.max_tile));
+        for (long long w = 0; w < I.words; w += I.max_tile, which ^= 1)
+            I.launch_counting(which, f, l, w, std::min(I.words, w + I.max_tile));
     }
+    check_cuda(cudaEventRecord(I.join_event, I.stream2), "cudaEventRecord");
+    check_cuda(cudaStreamWaitEvent(I.stream, I.join_event, 0), "cudaStreamWaitEvent");
     unsigned long long total = 0;
     check_cuda(cudaMemcpyAsync(&total, b.count, sizeof total, cudaMemcpyDeviceToHost, I.stream),
                "download survivor count");
