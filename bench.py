@@ -49,11 +49,11 @@ SMEM_BYTES_PER_CLK = 128      # lane-contiguous LDS.64, measured per SM on GB300
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 65,536-denominator
 # fast-plan launch of this workload, from an ncu capture of the kernel:
 #   ncu --set full --clock-control none -k regex:fast_sieve -s 1 -c 1 python bench.py
-#       --steps 1 --warmup 1 --no-cpu-baseline --reference-plan-steps 0
-#       --reference-gpu-denominators 0 --restricted 0 --serving-requests 0 --dense-height 0
-#       --batch-curves 0 --denominators 131072
+#       --steps 1 --warmup 1 --e2e-warmup 0 --e2e-steps 1 --no-cpu-baseline
+#       --reference-plan-steps 0 --reference-gpu-denominators 0 --restricted 0
+#       --serving-requests 0 --dense-height 0 --batch-curves 0 --denominators 131072
 # (cold L2 in every ncu pass: the class tables are read once per launch)
-FAST_LAUNCH_DRAM_BYTES = 39_281_664 + 7_168
+FAST_LAUNCH_DRAM_BYTES = 39_281_664 + 31_744
 
 
 def measured_hbm_gbs():
