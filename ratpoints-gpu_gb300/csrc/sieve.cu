@@ -23,6 +23,7 @@
 #include <cstring>
 #include <deque>
 #include <future>
+#include <mutex>
 #include <tuple>
 #include <utility>
 
@@ -239,9 +240,44 @@ T *device_alloc(std::size_t count, const char *what) {
     return static_cast<T *>(p);
 }
 
-}  // namespace
-
 constexpr long long kInitialSurvivors = 1 << 16;  // survivors per buffer before any growth
+
+// The streams, events, survivor buffers and pinned staging of a finished
+// search, kept for the next search on the same device so that it does not
+// create and allocate them again.  Nothing in them outlives a search as
+// content: every launch resets its counter words first, survivor arrays are
+// written before they are read, and every table is built anew per search.
+struct PooledPipeline {
+    struct Buf {
+        long long *a = nullptr, *pa = nullptr;
+        int *d = nullptr, *pd = nullptr;
+        long long cap = 0;
+        unsigned long long *count = nullptr;
+        cudaEvent_t begin = nullptr, end = nullptr, copied = nullptr;
+    };
+    int device = -1;
+    cudaStream_t streams[4] = {};
+    cudaEvent_t events[3] = {};
+    Buf buf[2];
+    unsigned long long *h_count = nullptr;
+    long long *h_a = nullptr;
+    int *h_d = nullptr;
+    long long host_capacity = 0;
+};
+constexpr std::size_t kPooledPipelines = 4;                   // per process
+constexpr long long kPooledSurvivors = 4 * kInitialSurvivors;  // larger buffers are freed
+
+// Never destroyed: static destructors may run after the CUDA runtime is gone.
+std::mutex &pipeline_pool_mutex() {
+    static auto *m = new std::mutex();
+    return *m;
+}
+std::vector<PooledPipeline> &pipeline_pool() {
+    static auto *pool = new std::vector<PooledPipeline>();
+    return *pool;
+}
+
+}  // namespace
 
 // Most admissible numerator classes of any denominator under the fast plan:
 // 2-adic classes (by d mod 64) times residues mod the class prime q (by d mod q).
@@ -391,7 +427,118 @@ struct Sieve::Impl {
 
     ~Impl() { release(); }
 
+    // Take a pooled pipeline of this device, if there is one.
+    bool adopt_pipeline() {
+        PooledPipeline p;
+        {
+            std::lock_guard<std::mutex> lock(pipeline_pool_mutex());
+            auto &pool = pipeline_pool();
+            auto it = std::find_if(pool.begin(), pool.end(),
+                                   [&](const PooledPipeline &q) { return q.device == device; });
+            if (it == pool.end()) return false;
+            p = *it;
+            pool.erase(it);
+        }
+        stream = p.streams[0];
+        stream2 = p.streams[1];
+        copy_stream = p.streams[2];
+        count_stream = p.streams[3];
+        fork_event = p.events[0];
+        join_event = p.events[1];
+        origin = p.events[2];
+        for (int i = 0; i < 2; ++i) {
+            Buffer &b = buf[i];
+            const PooledPipeline::Buf &q = p.buf[i];
+            b.a = q.a;
+            b.d = q.d;
+            b.pa = q.pa;
+            b.pd = q.pd;
+            b.cap = q.cap;
+            b.count = q.count;
+            b.begin = q.begin;
+            b.end = q.end;
+            b.copied = q.copied;
+        }
+        h_count = p.h_count;
+        h_a = p.h_a;
+        h_d = p.h_d;
+        host_capacity = p.host_capacity;
+        return true;
+    }
+
+    // Hand the pipeline to the pool if every stream finished without error
+    // and the pool has room; release() then frees only what was not handed on.
+    void offer_pipeline() {
+        if (device < 0 || !stream || !stream2 || !copy_stream || !count_stream || !fork_event ||
+            !join_event || !origin || !h_count)
+            return;
+        for (cudaStream_t s : {stream, stream2, copy_stream, count_stream})
+            if (cudaStreamSynchronize(s) != cudaSuccess) return;
+        for (const auto &b : buf)
+            if (!b.count || !b.begin || !b.end || !b.copied) return;
+        {
+            std::lock_guard<std::mutex> lock(pipeline_pool_mutex());
+            if (pipeline_pool().size() >= kPooledPipelines) return;
+        }
+        for (auto &b : buf)
+            if (b.cap > kPooledSurvivors) {
+                cudaFree(b.a);
+                cudaFree(b.d);
+                cudaFree(b.pa);
+                cudaFree(b.pd);
+                b.a = b.pa = nullptr;
+                b.d = b.pd = nullptr;
+                b.cap = 0;
+            }
+        if (host_capacity > kPooledSurvivors) {
+            cudaFreeHost(h_a);
+            cudaFreeHost(h_d);
+            h_a = nullptr;
+            h_d = nullptr;
+            host_capacity = 0;
+        }
+        PooledPipeline p;
+        p.device = device;
+        p.streams[0] = stream;
+        p.streams[1] = stream2;
+        p.streams[2] = copy_stream;
+        p.streams[3] = count_stream;
+        p.events[0] = fork_event;
+        p.events[1] = join_event;
+        p.events[2] = origin;
+        for (int i = 0; i < 2; ++i) {
+            const Buffer &b = buf[i];
+            PooledPipeline::Buf &q = p.buf[i];
+            q.a = b.a;
+            q.d = b.d;
+            q.pa = b.pa;
+            q.pd = b.pd;
+            q.cap = b.cap;
+            q.count = b.count;
+            q.begin = b.begin;
+            q.end = b.end;
+            q.copied = b.copied;
+        }
+        p.h_count = h_count;
+        p.h_a = h_a;
+        p.h_d = h_d;
+        p.host_capacity = host_capacity;
+        {
+            std::lock_guard<std::mutex> lock(pipeline_pool_mutex());
+            if (pipeline_pool().size() >= kPooledPipelines) return;
+            pipeline_pool().push_back(p);
+        }
+        stream = stream2 = copy_stream = count_stream = nullptr;
+        fork_event = join_event = origin = nullptr;
+        for (auto &b : buf) b = Buffer{};
+        h_count = nullptr;
+        h_a = nullptr;
+        h_d = nullptr;
+        host_capacity = 0;
+    }
+
     void release() {
+        offer_pipeline();
         for (auto &b : buf) {
             cudaFree(b.a);
             cudaFree(b.d);
@@ -511,13 +658,15 @@ struct Sieve::Impl {
             });
         if (opt.device >= 0) check_cuda(cudaSetDevice(opt.device), "cudaSetDevice");
         check_cuda(cudaGetDevice(&device), "cudaGetDevice");
-        check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        check_cuda(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        check_cuda(cudaStreamCreateWithFlags(&count_stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        check_cuda(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking), "cudaStreamCreate");
-        check_cuda(cudaEventCreateWithFlags(&fork_event, cudaEventDisableTiming), "cudaEventCreate");
-        check_cuda(cudaEventCreateWithFlags(&join_event, cudaEventDisableTiming), "cudaEventCreate");
-        check_cuda(cudaEventCreate(&origin), "cudaEventCreate");
+        if (!adopt_pipeline()) {
+            check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            check_cuda(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            check_cuda(cudaStreamCreateWithFlags(&count_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            check_cuda(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking), "cudaStreamCreate");
+            check_cuda(cudaEventCreateWithFlags(&fork_event, cudaEventDisableTiming), "cudaEventCreate");
+            check_cuda(cudaEventCreateWithFlags(&join_event, cudaEventDisableTiming), "cudaEventCreate");
+            check_cuda(cudaEventCreate(&origin), "cudaEventCreate");
+        }
         check_cuda(cudaFuncSetAttribute(dev::ref_sieve_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(dev::kRefSmem)),
@@ -538,23 +687,47 @@ struct Sieve::Impl {
         if (const char *env = std::getenv("RPG_SURVIVOR_CAPACITY")) initial = capacity = std::atoll(env);
         capacity = std::max<long long>(capacity, 64);
         initial = std::max<long long>(initial, 64);
+        // A pooled buffer is kept if its capacity lies in [initial, capacity];
+        // pa and pd, when present, always have the capacity of a and d.
         for (auto &b : buf) {
-            b.a = device_alloc<long long>(std::size_t(initial), "cudaMalloc(survivors)");
-            b.d = device_alloc<int>(std::size_t(initial), "cudaMalloc(survivors)");
-            if (opt.preverify) {
-                b.pa = device_alloc<long long>(std::size_t(initial), "cudaMalloc(survivors)");
-                b.pd = device_alloc<int>(std::size_t(initial), "cudaMalloc(survivors)");
+            if (b.cap < initial || b.cap > capacity || !b.a || !b.d) {
+                cudaFree(b.a);
+                cudaFree(b.d);
+                cudaFree(b.pa);
+                cudaFree(b.pd);
+                b.a = b.pa = nullptr;
+                b.d = b.pd = nullptr;
+                b.cap = 0;
+                b.a = device_alloc<long long>(std::size_t(initial), "cudaMalloc(survivors)");
+                b.d = device_alloc<int>(std::size_t(initial), "cudaMalloc(survivors)");
+                b.cap = initial;
             }
-            b.cap = initial;
-            b.count = device_alloc<unsigned long long>(4, "cudaMalloc(count)");
-            check_cuda(cudaEventCreate(&b.begin), "cudaEventCreate");
-            check_cuda(cudaEventCreate(&b.end), "cudaEventCreate");
-            check_cuda(cudaEventCreateWithFlags(&b.copied, cudaEventDisableTiming), "cudaEventCreate");
+            if (opt.preverify && (!b.pa || !b.pd)) {
+                cudaFree(b.pa);
+                cudaFree(b.pd);
+                b.pa = nullptr;
+                b.pd = nullptr;
+                b.pa = device_alloc<long long>(std::size_t(b.cap), "cudaMalloc(survivors)");
+                b.pd = device_alloc<int>(std::size_t(b.cap), "cudaMalloc(survivors)");
+            }
+            if (!b.count) b.count = device_alloc<unsigned long long>(4, "cudaMalloc(count)");
+            if (!b.begin) check_cuda(cudaEventCreate(&b.begin), "cudaEventCreate");
+            if (!b.end) check_cuda(cudaEventCreate(&b.end), "cudaEventCreate");
+            if (!b.copied)
+                check_cuda(cudaEventCreateWithFlags(&b.copied, cudaEventDisableTiming), "cudaEventCreate");
+            b.busy = false;
         }
-        check_cuda(cudaMallocHost(&h_count, 8 * sizeof(unsigned long long)), "cudaMallocHost");
-        check_cuda(cudaMallocHost(&h_a, std::size_t(initial) * sizeof(long long)), "cudaMallocHost");
-        check_cuda(cudaMallocHost(&h_d, std::size_t(initial) * sizeof(int)), "cudaMallocHost");
-        host_capacity = initial;
+        if (!h_count) check_cuda(cudaMallocHost(&h_count, 8 * sizeof(unsigned long long)), "cudaMallocHost");
+        if (!h_a || !h_d || host_capacity < initial) {
+            if (h_a) cudaFreeHost(h_a);
+            if (h_d) cudaFreeHost(h_d);
+            h_a = nullptr;
+            h_d = nullptr;
+            host_capacity = 0;
+            check_cuda(cudaMallocHost(&h_a, std::size_t(initial) * sizeof(long long)), "cudaMallocHost");
+            check_cuda(cudaMallocHost(&h_d, std::size_t(initial) * sizeof(int)), "cudaMallocHost");
+            host_capacity = initial;
+        }
         timings.workspace_ms += ms_since(t0);
         if (opt.plan == PlanKind::fast) build_fast_tables(coefficients, planned);
         else build_tables(coefficients);
