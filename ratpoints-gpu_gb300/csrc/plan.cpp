@@ -175,63 +175,84 @@ FastPlan FastPlanner::plan(int max_modulus, int max_slots, long long row_budget,
                   const double db = b.first / std::log2(double(b.second));
                   return da != db ? da > db : a.second < b.second;
               });
-    auto pack = [&](const std::vector<std::pair<double, int>> &order, int limit, int slots, int cap) {
-        FastPlan out;
-        out.class_prime = plan.class_prime;
+    // A packing in fixed arrays (no allocation: the search below runs a few
+    // hundred of them); odd primes multiply past 2^31 after eight factors.
+    struct Packing {
+        int count = 0;
+        int modulus[kMaxFastSlots];
+        int factors[kMaxFastSlots];
+        int factor[kMaxFastSlots][8];
+        double bits = 0;
+    };
+    auto pack = [&](const std::vector<std::pair<double, int>> &order, int limit, int slots, int cap,
+                    Packing &out) {
+        out.count = 0;
+        out.bits = 0;
         for (const auto &s : order) {
             const int q = s.second;
             if (q >= limit || q == plan.class_prime || s.first < 0.3 || q > cap) continue;
             int target = -1;
             long long headroom = -1;
-            for (std::size_t i = 0; i < out.moduli.size(); ++i) {
-                const long long product = (long long)out.moduli[i] * q;
+            for (int i = 0; i < out.count; ++i) {
+                const long long product = (long long)out.modulus[i] * q;
                 if (product <= cap && (long long)cap - product > headroom) {
                     headroom = cap - product;
-                    target = int(i);
+                    target = i;
                 }
             }
             if (target < 0) {
-                if ((int)out.moduli.size() == slots) continue;
-                out.moduli.push_back(1);
-                out.slots.push_back({});
-                target = int(out.moduli.size()) - 1;
+                if (out.count == slots) continue;
+                target = out.count++;
+                out.modulus[target] = 1;
+                out.factors[target] = 0;
             }
-            out.moduli[target] *= q;
-            out.slots[target].push_back(q);
+            out.modulus[target] *= q;
+            out.factor[target][out.factors[target]++] = q;
             out.bits += s.first;
         }
-        return out;
+    };
+    auto row_words = [](const Packing &p) {
+        long long rows = 0;
+        for (int i = 0; i < p.count; ++i) rows += (p.modulus[i] + kFastRowExtension + 1) & ~1;
+        return rows;
     };
     // one packing per row count, its moduli capped (from max_modulus down by
     // 1/8 steps) until its rows fit the budget; the cheapest by the cost model
-    FastPlan best_plan = plan;
+    // (limits that coincide give the same packing: each is tried once)
+    const int limits[3] = {std::min(72, prime_limit_), std::min(kFastPrimeLimit, prime_limit_), prime_limit_};
+    Packing best, candidate, packed;
     double best_cost = 0;
     bool found = false;
-    for (int slots = by_cost ? 1 : std::min(max_slots, kMaxFastSlots); slots <= std::min(max_slots, kMaxFastSlots);
-         ++slots) {
-        FastPlan candidate = plan;
+    const int top = std::min(max_slots, kMaxFastSlots);
+    for (int slots = by_cost ? 1 : top; slots <= top; ++slots) {
         for (int cap = max_modulus;; cap = cap * 7 / 8) {
-            candidate = plan;
+            candidate.count = 0;
             candidate.bits = -1;
-            for (int limit : {72, kFastPrimeLimit, prime_limit_})
+            for (int li = 0; li < 3; ++li) {
+                if (li > 0 && limits[li] == limits[li - 1]) continue;
                 for (const auto *order : {&by_bits, &by_density}) {
-                    FastPlan packed = pack(*order, std::min(limit, prime_limit_), slots, cap);
+                    pack(*order, limits[li], slots, cap, packed);
                     if (packed.bits > candidate.bits) candidate = packed;
                 }
-            long long rows = 0;
-            for (int m : candidate.moduli) rows += (m + kFastRowExtension + 1) & ~1;
-            if (rows <= row_budget || cap <= 64) break;
+            }
+            if (row_words(candidate) <= row_budget || cap <= 64) break;
         }
-        if (candidate.moduli.empty()) continue;
-        long long rows = 0;
-        for (int m : candidate.moduli) rows += (m + kFastRowExtension + 1) & ~1;
-        if (rows > row_budget) continue;
+        if (candidate.count == 0) continue;
+        if (row_words(candidate) > row_budget) continue;
         const double word_survives = 1.0 - std::pow(1.0 - std::exp2(-candidate.bits), 64.0);
-        const double cost = kStageRowCost * double(candidate.moduli.size()) + kSurvivorWordCost * word_survives;
+        const double cost = kStageRowCost * double(candidate.count) + kSurvivorWordCost * word_survives;
         if (!found || cost < best_cost - 1e-9) {
-            best_plan = candidate;
+            best = candidate;
             best_cost = cost;
             found = true;
+        }
+    }
+    FastPlan best_plan = plan;
+    if (found) {
+        best_plan.bits = best.bits;
+        for (int i = 0; i < best.count; ++i) {
+            best_plan.moduli.push_back(best.modulus[i]);
+            best_plan.slots.emplace_back(best.factor[i], best.factor[i] + best.factors[i]);
         }
     }
     plan = best_plan;
