@@ -45,17 +45,63 @@ long long mod_inverse(long long value, long long modulus) {
     return (s0 % modulus + modulus) % modulus;
 }
 
+void modular_inverses(int p, unsigned short *out) {
+    out[0] = 0;
+    if (p > 1) out[1] = 1;
+    // v^-1 = -(p / v) (p mod v)^-1 (mod p), from p = (p / v) v + p mod v
+    for (int v = 2; v < p; ++v) {
+        const int t = int((long long)(p / v) * out[p % v] % p);
+        out[v] = (unsigned short)(t ? p - t : 0);
+    }
+}
+
+bool square_mod(long long value, int p) {
+    long long v = value % p;
+    if (v < 0) v += p;
+    if (v == 0 || p == 2) return true;
+    long long result = 1;  // Euler's criterion: v^((p-1)/2) = 1
+    for (long long e = (p - 1) / 2, b = v; e; e >>= 1, b = b * b % p)
+        if (e & 1) result = result * b % p;
+    return result == 1;
+}
+
 std::vector<std::uint8_t> affine_mask(int prime, const std::vector<std::string> &coefficients) {
     std::vector<int> residues(coefficients.size());
     for (std::size_t i = 0; i < coefficients.size(); ++i)
         residues[i] = decimal_mod(coefficients[i], prime);
     std::vector<std::uint8_t> square(prime, 0);
-    for (long long v = 0; v < prime; ++v) square[v * v % prime] = 1;
+    // v^2 mod p for v <= p / 2 (the rest repeat them): (v + 1)^2 = v^2 + 2v + 1
+    for (long long v = 0, sq = 0; 2 * v <= prime; ++v) {
+        square[sq] = 1;
+        sq += 2 * v + 1;
+        while (sq >= prime) sq -= prime;
+    }
     std::vector<std::uint8_t> affine(prime, 0);
-    for (int x = 0; x < prime; ++x) {
+    auto evaluate = [&](long long x) {
         long long value = 0;
         for (std::size_t i = residues.size(); i-- > 0;) value = (value * x + residues[i]) % prime;
-        affine[x] = square[value];
+        return value;
+    };
+    const int degree = int(residues.size()) - 1;
+    if (prime <= 2 * (degree + 1)) {
+        for (int x = 0; x < prime; ++x) affine[x] = square[evaluate(x)];
+        return affine;
+    }
+    // Forward differences: f(x + 1) from f(x) with degree additions mod p
+    // instead of a Horner evaluation (a division per coefficient) at every x.
+    std::vector<long long> diff(std::size_t(degree) + 1);
+    for (int x = 0; x <= degree; ++x) diff[std::size_t(x)] = evaluate(x);
+    for (int k = 1; k <= degree; ++k)  // diff[k] = k-th difference at 0
+        for (int x = degree; x >= k; --x) {
+            long long v = diff[std::size_t(x)] - diff[std::size_t(x) - 1];
+            diff[std::size_t(x)] = v < 0 ? v + prime : v;
+        }
+    for (int x = 0; x < prime; ++x) {
+        affine[x] = square[diff[0]];
+        for (int k = 0; k < degree; ++k) {
+            long long v = diff[std::size_t(k)] + diff[std::size_t(k) + 1];
+            diff[std::size_t(k)] = v >= prime ? v - prime : v;
+        }
     }
     return affine;
 }

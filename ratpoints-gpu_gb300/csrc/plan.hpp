@@ -33,6 +33,10 @@ const std::array<int, kCandidatePrimes> &candidate_primes();  // ascending, 293 
 // Residue of a decimal integer modulo m (m < 2^31), sign folded into [0, m).
 int decimal_mod(const std::string &text, int modulus);
 long long mod_inverse(long long value, long long modulus);
+// out[v] = v^-1 mod p for 0 < v < p and out[0] = 0, for a prime p < 65536.
+void modular_inverses(int p, unsigned short *out);
+// value mod p is a square (0 included), for a prime p < 2^31.
+bool square_mod(long long value, int p);
 
 // affine[x] = 1 iff f(x) mod p is a square (0 included), for x in [0, p).
 std::vector<std::uint8_t> affine_mask(int prime, const std::vector<std::string> &coefficients);

@@ -601,8 +601,7 @@ struct Sieve::Impl {
             const int p = primes[i];
             auto aff = affine_mask(p, coefficients);
             std::copy(aff.begin(), aff.end(), affine.begin() + std::size_t(i) * kMaximumPrime);
-            for (int v = 1; v < p; ++v)
-                inverse[std::size_t(i) * kMaximumPrime + v] = (unsigned short)mod_inverse(v, p);
+            modular_inverses(p, inverse.data() + std::size_t(i) * kMaximumPrime);
             neg_h[i] = int((p - bound % p) % p);
         }
         timings.plan_ms += ms_since(t0);
@@ -763,18 +762,11 @@ struct Sieve::Impl {
             base[p] = int(affine.size());
             auto aff = affine_mask(p, coefficients);
             affine.insert(affine.end(), aff.begin(), aff.end());
-            // v^-1 = -(p / v) (p mod v)^-1 (mod p), from p = (p / v) v + p mod v
             const std::size_t at = inverse.size();
             inverse.resize(at + std::size_t(p), 0);
-            if (p > 1) inverse[at + 1] = 1;
-            for (int v = 2; v < p; ++v)
-                inverse[at + std::size_t(v)] = (unsigned short)(
-                    (p - (long long)(p / v) * inverse[at + std::size_t(p % v)] % p) % p);
+            modular_inverses(p, inverse.data() + at);
             if (n % 2 == 0) {
-                const int lc = decimal_mod(coefficients.back(), p);
-                bool square = false;
-                for (int v = 0; v < p && !square; ++v) square = (v * v) % p == lc;
-                lead[p] = square ? 1 : 0;
+                lead[p] = square_mod(decimal_mod(coefficients.back(), p), p) ? 1 : 0;
             }
         }
         std::vector<dev::TableSpec> specs;
