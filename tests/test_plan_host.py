@@ -83,3 +83,19 @@ def test_huge_rows_keep_two_slots(rpg):
     plan = rpg.fast_plan("-9876543210 1234567 0 1", 10 ** 9)
     well_formed(plan)
     assert plan["slots"] == 2
+
+
+def test_plans_match_the_regression_fixture(rpg):
+    # tests/golden/plans.json (tests/golden/make_plans.py): the autotuner's
+    # decisions for 60 seeded curves; speed-ups of the planner keep them
+    import json
+    from pathlib import Path
+
+    rows = json.loads((Path(__file__).parent / "golden" / "plans.json").read_text())
+    assert len(rows) == 60
+    for row in rows:
+        plan = rpg.fast_plan(row["coefficients"], row["height"])
+        want = row["plan"]
+        assert (plan["class_prime"], plan["moduli"], plan["factors"], plan["slots"]) == \
+            (want["class_prime"], want["moduli"], want["factors"], want["slots"]), row
+        assert plan["bits"] == pytest.approx(want["bits"], abs=1e-9)
