@@ -326,6 +326,14 @@ void rpg_server_destroy(rpg_server *server);
  * No reference counterpart: the reference's kernels have no waits. */
 rpg_status rpg_bounded_wait_selftest(int32_t device, int32_t polls, int32_t arrive);
 
+/* A finished rpg_sieve_run or rpg_point_search leaves its streams, events,
+ * survivor buffers (up to 262,144 survivors) and pinned staging for the next
+ * search on the same device (at most four such sets per process, about 16 MB
+ * each).  This call frees them for `device` (-1: every device); a caller that
+ * resets a device (cudaDeviceReset) calls it first.  Searches still running
+ * are not affected.  No reference counterpart. */
+rpg_status rpg_release_cached_resources(int32_t device);
+
 int32_t rpg_device_count(void);
 int32_t rpg_abi_version(void);
 const char *rpg_last_error(void);

@@ -518,6 +518,13 @@ int32_t rpg_device_count(void) {
 
 int32_t rpg_abi_version(void) { return RPG_ABI_VERSION; }
 
+rpg_status rpg_release_cached_resources(int32_t device) {
+    return guarded([&]() -> rpg_status {
+        rpg::release_pooled_pipelines(device < 0 ? -1 : device);
+        return RPG_OK;
+    });
+}
+
 const char *rpg_last_error(void) { return g_last_error.c_str(); }
 
 }  // extern "C"

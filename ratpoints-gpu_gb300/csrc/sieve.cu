@@ -1349,6 +1349,41 @@ Sieve::Sieve(const std::vector<std::string> &coefficients, long long bound,
 
 Sieve::~Sieve() = default;
 
+void release_pooled_pipelines(int device) {
+    std::vector<PooledPipeline> taken;
+    {
+        std::lock_guard<std::mutex> lock(pipeline_pool_mutex());
+        auto &pool = pipeline_pool();
+        for (auto it = pool.begin(); it != pool.end();) {
+            if (device < 0 || it->device == device) {
+                taken.push_back(*it);
+                it = pool.erase(it);
+            } else {
+                ++it;
+            }
+        }
+    }
+    for (const auto &p : taken) {
+        for (const auto &b : p.buf) {
+            cudaFree(b.a);
+            cudaFree(b.d);
+            cudaFree(b.pa);
+            cudaFree(b.pd);
+            cudaFree(b.count);
+            if (b.begin) cudaEventDestroy(b.begin);
+            if (b.end) cudaEventDestroy(b.end);
+            if (b.copied) cudaEventDestroy(b.copied);
+        }
+        if (p.h_count) cudaFreeHost(p.h_count);
+        if (p.h_a) cudaFreeHost(p.h_a);
+        if (p.h_d) cudaFreeHost(p.h_d);
+        for (cudaEvent_t e : p.events)
+            if (e) cudaEventDestroy(e);
+        for (cudaStream_t s : p.streams)
+            if (s) cudaStreamDestroy(s);
+    }
+}
+
 void Sieve::start(long long first, long long last, long long batch_size) {
     if (first < 1 || last < first) throw std::invalid_argument("invalid denominator range");
     if (impl_->opt.square && last > 46340) throw std::invalid_argument("invalid denominator range");

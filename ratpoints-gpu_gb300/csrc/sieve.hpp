@@ -69,6 +69,11 @@ struct SieveTimings {
     unsigned long long d2h_bytes = 0;
 };
 
+// Frees the idle search pipelines (streams, events, survivor buffers, pinned
+// staging) that finished sieves left for reuse on `device` (-1: every
+// device).  A process that resets a device must call it first.
+void release_pooled_pipelines(int device);
+
 // The fast plan a single-curve sieve uses for a curve and numerator bound
 // (host only): the autotuner's choice under the fast kernel's shared-memory
 // budget; *max_classes (optional) receives the most classes of one denominator.

@@ -166,6 +166,8 @@ def load():
     lib.rpg_preverify.restype = S
     lib.rpg_preverify.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
                                   ctypes.POINTER(ctypes.c_int32)]
+    lib.rpg_release_cached_resources.restype = S
+    lib.rpg_release_cached_resources.argtypes = [ctypes.c_int32]
     lib.rpg_bounded_wait_selftest.restype = S
     lib.rpg_bounded_wait_selftest.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
     lib.rpg_cli_main.restype = ctypes.c_int32
@@ -408,6 +410,12 @@ def preverify(coefficients, a, b):
     flag = ctypes.c_int32(-1)
     _check(load().rpg_preverify(_strings(coeffs), len(coeffs), int(a), int(b), ctypes.byref(flag)))
     return bool(flag.value)
+
+
+def release_cached_resources(device=-1):
+    """Frees the pooled streams and buffers that finished searches left for
+    reuse on `device` (-1: every device)."""
+    _check(load().rpg_release_cached_resources(int(device)))
 
 
 def bounded_wait_selftest(polls, arrive, device=0):

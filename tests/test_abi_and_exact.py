@@ -138,3 +138,9 @@ def test_bounded_wait_selftest_rejects_bad_polls(rpg):
         with pytest.raises(rpg.RpgError) as err:
             rpg.bounded_wait_selftest(polls, arrive=True)
         assert err.value.status == 1
+
+
+def test_release_cached_resources_without_searches(rpg):
+    # nothing pooled yet in this process: no CUDA call is made
+    rpg.release_cached_resources()
+    rpg.release_cached_resources(0)

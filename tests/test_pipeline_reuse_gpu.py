@@ -39,3 +39,12 @@ def test_results_independent_of_earlier_searches(rpg, oracle, golden, monkeypatc
         assert again == expected, (plan, preverify)
         if plan == "fast":
             assert s["survivor_count"] == stats["survivor_count"]
+
+
+def test_search_after_releasing_the_pool(rpg, oracle):
+    expected = expected_points(oracle)
+    assert rpg.point_search(CONIC, 2000, 1, 300)[0] == expected
+    rpg.release_cached_resources(0)
+    rpg.release_cached_resources()  # already empty
+    assert rpg.point_search(CONIC, 2000, 1, 300)[0] == expected
+    assert rpg.point_search(CONIC, 2000, 1, 300, plan="reference")[0] == expected
