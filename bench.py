@@ -102,6 +102,23 @@ def reduced_sites(height, last, mu=None):
     return int(terms.sum())
 
 
+def rank_block(rank, per_rank):
+    """Denominators [first, last] that `rank` sieves under weak scaling: each
+    rank takes its own block of per_rank consecutive denominators."""
+    return rank * per_rank + 1, (rank + 1) * per_rank
+
+
+def max_over_ranks(value, dist):
+    """The largest of the ranks' values (the step time of the slowest rank)."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks/throttle reasons sampled every 200 ms during a region."""
 
@@ -520,7 +537,7 @@ def main():
     coeffs = c2_curve()
     last = args.denominators
     # weak scaling: rank r sieves its own block of `last` denominators
-    first_b, last_b = rank * last + 1, (rank + 1) * last
+    first_b, last_b = rank_block(rank, last)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
     def measure(plan, steps, warmup, sampler=None):
@@ -541,11 +558,7 @@ def main():
         assert len(set(counts)) == 1, "survivor count changed between steps"
         words, per_word = session.work(first_b, last_b)
         session.close()
-        step_ms = sum(times) / len(times)
-        if dist:
-            t = torch.tensor([step_ms], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            step_ms = float(t.item())
+        step_ms = max_over_ranks(sum(times) / len(times), dist)
         return {"ms": step_ms, "survivors": counts[0], "words": words, "bytes_per_word": per_word}
 
     clocks = ClockSampler(local)
