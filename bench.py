@@ -77,28 +77,38 @@ def c2_curve(seed=C2_SEED):
 
 
 def mobius(limit):
+    """mu(n) for n <= limit: signs flipped by the primes up to sqrt(limit),
+    zeros at their squares, and one more flip where a prime above sqrt(limit)
+    is left over (at most one such factor fits)."""
     import numpy as np
+    from math import isqrt
 
+    root = isqrt(limit)
+    small = np.ones(root + 1, dtype=bool)
+    small[:2] = False
+    for p in range(2, isqrt(root) + 1):
+        if small[p]:
+            small[p * p::p] = False
     mu = np.ones(limit + 1, dtype=np.int8)
-    is_composite = np.zeros(limit + 1, dtype=bool)
-    for p in range(2, limit + 1):
-        if is_composite[p]:
-            continue
-        is_composite[p * p::p] = True
+    rest = np.arange(limit + 1, dtype=np.int64)
+    for p in np.flatnonzero(small).tolist():
         mu[p::p] *= -1
         mu[p * p::p * p] = 0
+        rest[p::p] //= p
+    mu[rest > 1] *= -1
     mu[0] = 0
     return mu
 
 
-def reduced_sites(height, last, mu=None):
-    """#{(a, b): |a| <= height, 1 <= b <= last, gcd(a, b) = 1}
-    = sum_d mu(d) floor(last/d) (2 floor(height/d) + 1)."""
+def reduced_sites(height, last, mu=None, first=1):
+    """#{(a, b): |a| <= height, first <= b <= last, gcd(a, b) = 1}
+    = sum_d mu(d) (floor(last/d) - floor((first-1)/d)) (2 floor(height/d) + 1)."""
     import numpy as np
 
     mu = mobius(last) if mu is None else mu
     d = np.arange(1, last + 1, dtype=np.int64)
-    terms = mu[1:last + 1].astype(np.int64) * (last // d) * (2 * (height // d) + 1)
+    multiples = last // d - (first - 1) // d
+    terms = mu[1:last + 1].astype(np.int64) * multiples * (2 * (height // d) + 1)
     return int(terms.sum())
 
 
@@ -106,6 +116,17 @@ def rank_block(rank, per_rank):
     """Denominators [first, last] that `rank` sieves under weak scaling: each
     rank takes its own block of per_rank consecutive denominators."""
     return rank * per_rank + 1, (rank + 1) * per_rank
+
+
+def sum_over_ranks(value, dist):
+    """The ranks' integer counts added up."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([int(value)], dtype=torch.int64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return int(t.item())
 
 
 def max_over_ranks(value, dist):
@@ -568,11 +589,11 @@ def main():
     if args.plan != "reference" and args.reference_plan_steps > 0:
         ref = measure("reference", args.reference_plan_steps, 1)
 
-    mu = mobius(last)
-    reduced = reduced_sites(HEIGHT, last, mu)
-    rect = (2 * HEIGHT + 1) * last
+    # sites of the whole job: every rank's own block
+    reduced = sum_over_ranks(reduced_sites(HEIGHT, last_b, mobius(last_b), first=first_b), dist)
+    rect = (2 * HEIGHT + 1) * last * world
     step_ms = fast["ms"]
-    value = reduced * world / (step_ms / 1e3) / 1e9
+    value = reduced / (step_ms / 1e3) / 1e9
     launches_per_step = (last + BATCH - 1) // BATCH
 
     # e2e through the C ABI: host strings in, verified points out
@@ -583,7 +604,7 @@ def main():
                                              include_infinity=True)
         if i >= args.e2e_warmup:
             e2e_times.append(time.perf_counter() - t0)
-    e2e_s = sorted(e2e_times)[len(e2e_times) // 2]
+    e2e_s = max_over_ranks(sorted(e2e_times)[len(e2e_times) // 2], dist)
     if rank != 0:
         return
     sm_hz = (clock.get("sm_mhz") or 1965.0) * 1e6
@@ -598,7 +619,7 @@ def main():
                 "coefficients uniform in [-2^32, 2^32)",
         "config": {**workload_config(), "denominators": last, "rectangle_sites": rect,
                    "reduced_sites": reduced, "plan": args.plan,
-                   "rectangle_gsites_per_s": rect * world / (step_ms / 1e3) / 1e9,
+                   "rectangle_gsites_per_s": rect / (step_ms / 1e3) / 1e9,
                    "modular_survivors": fast["survivors"],
                    "words_swept_per_step": fast["words"]},
         "roofline": {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -618,7 +639,7 @@ def main():
                                     f"/ {launches_per_step} launches",
                      "peak_source": "152 SMs x 128 B/clk (LDS.64 lane-contiguous, measured on "
                                     "GB300) x median SM clock sampled in the timed region"},
-        "e2e": {"value": reduced * world / e2e_s / 1e9, "unit": UNIT,
+        "e2e": {"value": reduced / e2e_s / 1e9, "unit": UNIT,
                 "seconds": e2e_s, "points": len(points),
                 "h2d_bytes_per_step": int(e2e_stats.get("h2d_bytes", 0)) if e2e_stats else 0,
                 "d2h_bytes_per_step": int(e2e_stats.get("d2h_bytes", 0)) if e2e_stats else 0,
@@ -632,7 +653,7 @@ def main():
         line["reference_gpu"] = reference_gpu(coeffs, args.reference_gpu_denominators, rpg)
     if ref is not None:
         line["reference_plan"] = {
-            "value": reduced * world / (ref["ms"] / 1e3) / 1e9, "unit": UNIT,
+            "value": reduced / (ref["ms"] / 1e3) / 1e9, "unit": UNIT,
             "ms_per_step": ref["ms"], "modular_survivors": ref["survivors"],
             "note": "same kernel family with the reference's 32-prime plan: survivor set "
                     "identical to the reference implementation's"}

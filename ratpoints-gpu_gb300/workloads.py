@@ -125,14 +125,25 @@ def serving_stream(count=1000, rate=200.0, seed=5, first_fraction=0.3):
 
 
 def mobius(limit):
+    """mu(n) for n <= limit: signs flipped by the primes up to sqrt(limit),
+    zeros at their squares, and one more flip where a prime above sqrt(limit)
+    is left over (at most one such factor fits)."""
+    import numpy as np
+    from math import isqrt
+
+    root = isqrt(limit)
+    small = np.ones(root + 1, dtype=bool)
+    small[:2] = False
+    for p in range(2, isqrt(root) + 1):
+        if small[p]:
+            small[p * p::p] = False
     mu = np.ones(limit + 1, dtype=np.int8)
-    is_composite = np.zeros(limit + 1, dtype=bool)
-    for p in range(2, limit + 1):
-        if is_composite[p]:
-            continue
-        is_composite[p * p::p] = True
+    rest = np.arange(limit + 1, dtype=np.int64)
+    for p in np.flatnonzero(small).tolist():
         mu[p::p] *= -1
         mu[p * p::p * p] = 0
+        rest[p::p] //= p
+    mu[rest > 1] *= -1
     mu[0] = 0
     return mu
 

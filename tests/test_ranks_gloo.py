@@ -58,3 +58,34 @@ def test_single_process_helpers():
     assert bench.rank_block(0, 5_000_000) == (1, 5_000_000)
     assert bench.rank_block(3, 10) == (31, 40)
     assert bench.max_over_ranks(4.5, None) == 4.5
+
+
+def test_site_counts_of_rank_blocks():
+    # the whole job's reduced sites are the sum over the ranks' blocks
+    import math
+
+    import numpy as np
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    limit = 100_000
+    slow = np.ones(limit + 1, dtype=np.int8)
+    composite = np.zeros(limit + 1, dtype=bool)
+    for p in range(2, limit + 1):
+        if not composite[p]:
+            composite[p * p::p] = True
+            slow[p::p] *= -1
+            slow[p * p::p * p] = 0
+    slow[0] = 0
+    assert np.array_equal(bench.mobius(limit), slow)
+    height, per_rank, world = 37, 30, 4
+    total = 0
+    for rank in range(world):
+        first, last = bench.rank_block(rank, per_rank)
+        brute = sum(1 for b in range(first, last + 1) for a in range(-height, height + 1)
+                    if math.gcd(a, b) == 1)
+        block = bench.reduced_sites(height, last, bench.mobius(last), first=first)
+        assert block == brute
+        total += block
+    assert total == bench.reduced_sites(height, world * per_rank)
