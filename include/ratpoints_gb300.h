@@ -195,22 +195,33 @@ void rpg_session_destroy(rpg_session *session);
 
 /*
  * Sieve [first, last] with the session's resident tables without allocating
- * any memory.  No counterpart in the reference; it exists for callers that
- * cannot allocate when they sieve: code running under CUDA graph capture,
- * engines that own their device memory through their own pool, host
- * callbacks that must not enter the allocator.
+ * any memory.  No counterpart in the reference.  It exists for callers that
+ * cannot allocate when they sieve: engines that reserve all of their device
+ * memory up front and hand it out from their own pool, so that a further
+ * cudaMalloc would fail or bypass their accounting, and latency-bound loops
+ * that cannot afford cudaMalloc/cudaFree, which may synchronize the device.
  *
  * Survivors go to the caller's device arrays (capacity entries each); the
  * caller's *device_count receives the total, which exceeds capacity when the
  * arrays were too small (entries past capacity are not written).  Work is
  * enqueued on `stream` (a cudaStream_t, NULL for the legacy default stream)
  * and the call returns without waiting; read the count after synchronizing.
- * At most 16,777,216 denominators (256 launches of 65536) per call: larger
- * ranges fail with RPG_E_ARG.  The launches' scheduling counters live in one
- * fixed 2 KiB device array per GPU, shared by all calls: calls that overlap
- * on the GPU race on it, so serialize them (one stream, or events).  The
- * first call on a device looks up that array's device address; make that
- * first call before any stream capture.
+ * If a bounded device wait of a launch gives up (the launch then stops early
+ * and its survivor set is incomplete), *device_count is set to UINT64_MAX
+ * instead: the status returned cannot report it, because the call returns
+ * before the GPU runs.  The calling thread's current device is left as it was.
+ *
+ * Limits, each rejected with RPG_E_ARG: at most 16,777,216 denominators (256
+ * launches of 65536) per call; and each row must fit one launch, which fails
+ * only for very large numerator bounds (above about 1.7e10 times the class
+ * prime for a fast-plan session, above about 3.4e10 for a reference-plan one;
+ * rpg_sieve_run has no such limit).
+ * The error word and the launches' scheduling counters live in one fixed
+ * 2,056-byte device array per GPU, held until the process exits and shared by
+ * all calls, which clear it first: calls that overlap on the GPU race on it,
+ * so serialize them (one stream, or events).  The first call on a device
+ * looks up that array's device address; make that first call before any
+ * stream capture.
  */
 rpg_status rpg_session_sieve_noalloc(rpg_session *session, int32_t first, int32_t last,
                                      int64_t *device_numerators, int32_t *device_denominators,

@@ -1455,11 +1455,13 @@ FastPlanInfo Sieve::fast_plan_info() const {
 
 int Sieve::device() const { return impl_->device; }
 
+bool Sieve::fits_one_launch() const { return impl_->words <= impl_->max_tile; }
+
 bool Sieve::launch_into(long long first, long long last, long long *out_a, int *out_d,
                         unsigned long long capacity, unsigned long long *out_count,
-                        unsigned long long *work, cudaStream_t stream) {
+                        unsigned long long *work, unsigned long long *error, cudaStream_t stream) {
     const auto &I = *impl_;
-    if (I.words > I.max_tile || last < first || last - first + 1 > (1 << 16)) return false;
+    if (!fits_one_launch() || last < first || last - first + 1 > (1 << 16)) return false;
     dev::SieveArgs A{};
     A.bound = I.bound;
     A.words = I.words;
@@ -1472,7 +1474,7 @@ bool Sieve::launch_into(long long first, long long last, long long *out_a, int *
     A.out_d = out_d;
     A.out_count = out_count;
     A.capacity = capacity;
-    A.error = nullptr;  // the caller's launch reports no timeouts
+    A.error = error;  // a bounded wait that gives up sets it
     if (I.opt.plan == PlanKind::fast) {
         I.launch_fast(I.F, A, work, stream);
     } else {

@@ -116,14 +116,19 @@ public:
     unsigned smem_bytes_per_word() const;
     FastPlanInfo fast_plan_info() const;
 
+    // Whether a whole row (all numerators of a denominator) fits one launch:
+    // false only for very large H (fast plan: more than 2^23 class words,
+    // reference plan: more than 2^30 words).
+    bool fits_one_launch() const;
     // Enqueue one sieve launch for parameters [first, last] (at most one batch
     // of 65536) on `stream`, writing survivors into caller-owned device arrays
     // and counting them in *out_count; `work` is a zeroed device counter the
-    // launch uses for dynamic scheduling.  Allocates nothing; returns false if
-    // a row does not fit one launch (very large H).
+    // launch uses for dynamic scheduling, and *error (a device word) becomes
+    // nonzero if a bounded wait of the launch gives up.  Allocates nothing;
+    // returns false if a row does not fit one launch or the range is invalid.
     bool launch_into(long long first, long long last, long long *out_a, int *out_d,
                      unsigned long long capacity, unsigned long long *out_count,
-                     unsigned long long *work, cudaStream_t stream);
+                     unsigned long long *work, unsigned long long *error, cudaStream_t stream);
     int device() const;
 
 private:

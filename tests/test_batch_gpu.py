@@ -251,3 +251,56 @@ def test_survivor_counts_repeat(rpg):
         again = rpg.batch_search(curves, preverify=False)
         assert again[2] == first[2]
         assert again[0] == first[0]
+
+
+def _oracle_points(oracle, c):
+    from fractions import Fraction
+
+    ivs = [oracle.Interval(None if lo is None else Fraction(lo), None if hi is None else Fraction(hi))
+           for lo, hi in c.get("intervals", ())]
+    o = oracle.Options(coefficients=list(c["coefficients"]), height=c["bound"], first=c["first"],
+                       last=c["last"], intervals=ivs,
+                       include_infinity=c.get("include_infinity", True),
+                       square=c.get("square", False))
+    expected = []
+    oracle.search(o, lambda a, y, d: expected.append((a, int(y), d)) or True)
+    return expected
+
+
+def test_wide_kernel_matches_oracle(rpg, oracle):
+    """Curves whose rows have at least 2,048 words of 64 numerators (bound >=
+    65,504) go to the class-layout wide kernel; each curve's points must equal
+    the oracle's restatement of the reference pipeline (its 32-prime sieve and
+    exact verification), with x intervals, square denominators and a first
+    denominator above 1 in the mix."""
+    mordell = ["17", "0", "0", "1"]          # y^2 = x^3 + 17
+    cubic = ["1", "0", "0", "1"]             # y^2 = x^3 + 1
+    curves = [
+        {"coefficients": mordell, "bound": 70000, "first": 1, "last": 6},
+        {"coefficients": mordell, "bound": 100000, "first": 2, "last": 5,
+         "intervals": [("-3", "-1"), ("0.5", "5e1")]},
+        {"coefficients": cubic, "bound": 90000, "first": 1, "last": 4, "square": True},
+        {"coefficients": ["-2", "0", "1", "0", "1"], "bound": 66000, "first": 1, "last": 6,
+         "square": True, "include_infinity": False},
+    ]
+    rng = random.Random(4242)
+    while len(curves) < 12:
+        degree = rng.choice([3, 4, 5, 6, 8])
+        coeffs = [str(rng.randint(-9, 9)) for _ in range(degree + 1)]
+        coeffs[-1] = str(rng.choice([1, 4, 9, -1]))
+        c = {"coefficients": coeffs, "bound": rng.randint(65504, 160000), "first": 1,
+             "last": rng.randint(2, 5)}
+        if rng.random() < 0.4:
+            lo = rng.uniform(-6, 2)
+            c["intervals"] = [(f"{lo:.3f}", f"{lo + rng.uniform(0.5, 4):.3f}")]
+        if rpg.is_squarefree(coeffs):
+            curves.append(c)
+    points, status, _, stats = rpg.batch_search(curves)
+    assert status == [0] * len(curves)
+    assert stats["wide_curves"] == len(curves)
+    found = 0
+    for c, got in zip(curves, points):
+        expected = _oracle_points(oracle, c)
+        assert got == expected, c
+        found += len(expected)
+    assert found >= 20

@@ -59,3 +59,31 @@ def test_random_large_coefficients(rpg, oracle):
 def test_c2_sample(rpg, oracle):
     import bench
     compare(rpg, oracle, bench.c2_curve(), 5_000_000, 1, 2048)
+
+
+def test_c2_full_box(rpg, oracle):
+    """The benchmark workload's whole box, a in [-5e6, 5e6], b in [1, 5e6]
+    (5e13 sites): the reference kernels' survivor multiset equals this
+    project's reference plan, and the command line's -v survivor count is the
+    same number; the fast and reference plans print identical stdout."""
+    import bench
+    coeffs = bench.c2_curve()
+    ref = compare(rpg, oracle, coeffs, 5_000_000, 1, 5_000_000)
+    assert ref["survivors"] > 1000
+    text = " ".join(coeffs)
+    runs = {plan: rpg.cli([text, "5000000", "-v", "--sieve-plan", plan])
+            for plan in ("reference", "fast")}
+    for plan, result in runs.items():
+        assert result.returncode == 0, (plan, result.stderr)
+    assert runs["fast"].stdout == runs["reference"].stdout
+    ref_metrics = rpg.parse_metrics(runs["reference"].stderr)
+    fast_metrics = rpg.parse_metrics(runs["fast"].stderr)
+    assert ref_metrics["survivors"] == ref["survivors"]
+    assert ref_metrics["exact_survivors"] == fast_metrics["exact_survivors"]
+    assert ref_metrics["denominators"] == fast_metrics["denominators"] == 5_000_000
+
+
+def test_record_curve_at_full_height(rpg, oracle):
+    # the record curve at its published height 10^7 (a dense curve: the
+    # reference's fast launch overflows and its streaming rerun runs)
+    compare(rpg, oracle, RECORD, 10_000_000, 1, 6000, batch=3000)
