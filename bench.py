@@ -45,15 +45,16 @@ HEIGHT = 5_000_000
 DENOMINATORS = 5_000_000
 BATCH = 1 << 16
 SMS = 152
-SMEM_BYTES_PER_CLK = 128      # lane-contiguous LDS.64, measured per SM on GB300
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 65,536-denominator
-# fast-plan launch of this workload, from an ncu capture of the kernel:
-#   ncu --set full --clock-control none -k regex:fast_sieve -s 1 -c 1 python bench.py
-#       --steps 1 --warmup 1 --e2e-warmup 0 --e2e-steps 1 --no-cpu-baseline
-#       --reference-plan-steps 0 --reference-gpu-denominators 0 --restricted 0
-#       --serving-requests 0 --dense-height 0 --batch-curves 0 --denominators 131072
-# (cold L2 in every ncu pass: the class tables are read once per launch)
-FAST_LAUNCH_DRAM_BYTES = 39_281_664 + 31_744
+NOMINAL_SMEM_BYTES_PER_CLK = 128   # LDS bandwidth per SM, for comparison with the probe
+# Dated ncu capture of one 65,536-denominator fast-plan launch of this workload
+# (profiles/fast_sieve_kernel_c2.md gives the command): DRAM bytes
+# (dram__bytes_read.sum + dram__bytes_write.sum) and the ALU-pipe share.  ncu
+# runs every pass with a cold L2, so the DRAM figure is an upper bound for the
+# timed launches, whose class tables stay in L2 between launches.
+FAST_LAUNCH_PROFILE = {"dram_bytes": 39_281_664 + 31_744, "alu_pipe_frac": 0.550,
+                       "issue_active_frac": 0.771,
+                       "source": "profiles/fast_sieve_kernel_c2.md (ncu --set full, "
+                                 "fast_sieve_kernel<7,3>, one launch)"}
 
 
 def measured_hbm_gbs():
@@ -253,25 +254,33 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def reference_gpu(coeffs, denominators, rpg):
-    """The reference's own sieve kernels (src/sieve.cu compiled unchanged for
-    sm_103a) on the first `denominators` denominators of the workload, with the
-    reference's host loop restated; parity against this project's reference
-    plan on the same sample."""
+def _ref_gpu_module():
     sys.path.insert(0, str(ROOT / "oracle" / "ref_gpu"))
     import ref_gpu
+
+    return ref_gpu
+
+
+def reference_gpu(coeffs, denominators, rpg, steps=3):
+    """The reference's own sieve kernels (src/sieve.cu compiled unchanged for
+    sm_103a) over denominators [1, denominators] of the workload, with the
+    reference's host loop restated: kernel event time, median of `steps`
+    passes after a short warm-up; survivor multiset (count and digest)
+    compared with this project's reference plan over the same box."""
+    ref_gpu = _ref_gpu_module()
     import ratpoints_oracle as oracle
 
     if not ref_gpu.available():
         return {"unavailable": "reference cubin not built (needs the reference tree at build time)"}
     ref_gpu.run(coeffs, HEIGHT, 1, min(denominators, 4096))  # warm-up
-    ref = ref_gpu.run(coeffs, HEIGHT, 1, denominators)
+    runs = [ref_gpu.run(coeffs, HEIGHT, 1, denominators) for _ in range(max(1, steps))]
+    ref = sorted(runs, key=lambda r: r["sieve_ms"])[len(runs) // 2]
     a, d, _ = rpg.sieve(coeffs, HEIGHT, 1, denominators, plan="reference")
     digest = sum(oracle.mix_pair(x, y) for x, y in zip(a.tolist(), d.tolist())) % 2**64
     reduced = reduced_sites(HEIGHT, denominators)
     rect = (2 * HEIGHT + 1) * denominators
-    return {"denominators": denominators, "kernel_ms": ref["sieve_ms"], "basis_ms": ref["basis_ms"],
-            "wall_ms": ref["wall_ms"],
+    return {"denominators": denominators, "steps": len(runs), "kernel_ms": ref["sieve_ms"],
+            "basis_ms": ref["basis_ms"], "wall_ms": ref["wall_ms"],
             "value": reduced / (ref["sieve_ms"] / 1e3) / 1e9, "unit": UNIT,
             "rectangle_gsites_per_s": rect / (ref["sieve_ms"] / 1e3) / 1e9,
             "survivors": ref["survivors"],
@@ -279,6 +288,45 @@ def reference_gpu(coeffs, denominators, rpg):
                                                                         ref["digest"]),
             "note": "reference src/sieve.cu compiled for sm_103a, kernel event time; basis built "
                     "once (the reference rebuilds it per batch)"}
+
+
+def record_curve_kernels(rpg, torch, flush, height=10 ** 7, denominators=10 ** 6, steps=3):
+    """The record curve (the reference's own benchmark curve, a dense one) over
+    a in [-H, H], b in [1, denominators]: the reference's kernels against this
+    project's fast and reference plans, kernel time only (tables resident),
+    median of `steps` passes; the reference plan's survivor count must equal
+    the reference kernels'."""
+    import workloads
+
+    ref_gpu = _ref_gpu_module()
+    reduced = workloads.reduced_sites(height, 1, denominators, workloads.mobius(denominators))
+    out = {"workload": f"record curve, a in [-{height:g}, {height:g}], b in [1, {denominators:g}]",
+           "reduced_sites": reduced}
+    coeffs = workloads.RECORD_CURVE.split()
+    for plan in ("fast", "reference"):
+        session = rpg.Session(coeffs, height, plan=plan)
+        session.count(1, min(denominators, 4096))
+        times, counts = [], []
+        for step in range(steps):
+            flush_l2(torch, flush, step)
+            n, ms = session.count(1, denominators)
+            times.append(ms)
+            counts.append(n)
+        session.close()
+        ms = sorted(times)[len(times) // 2]
+        out[plan] = {"kernel_ms": ms, "value": reduced / (ms / 1e3) / 1e9, "unit": UNIT,
+                     "survivors": counts[0]}
+    if ref_gpu.available():
+        ref_gpu.run(coeffs, height, 1, min(denominators, 4096))
+        runs = [ref_gpu.run(coeffs, height, 1, denominators) for _ in range(steps)]
+        ref = sorted(runs, key=lambda r: r["sieve_ms"])[len(runs) // 2]
+        out["reference_kernels"] = {"kernel_ms": ref["sieve_ms"],
+                                    "value": reduced / (ref["sieve_ms"] / 1e3) / 1e9, "unit": UNIT,
+                                    "survivors": ref["survivors"]}
+        out["survivor_count_matches_reference_plan"] = ref["survivors"] == out["reference"]["survivors"]
+        out["ratio_fast"] = out["fast"]["value"] / out["reference_kernels"]["value"]
+        out["ratio_same_survivors"] = out["reference"]["value"] / out["reference_kernels"]["value"]
+    return out
 
 
 def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2, shape="all", smem_peak_gbs=None):
@@ -495,6 +543,52 @@ def serving_benchmark(rpg, count=1000, rate=200.0, lanes=2, check=40):
             "identical_to_single_search": {"checked": len(sample), "all": identical}}
 
 
+def summary(line):
+    """The headline comparisons, kept short and last on the line."""
+    def r(x, nd=3):
+        return None if x is None else round(float(x), nd)
+
+    out = {"value": r(line["value"], 0), "e2e": r(line["e2e"]["value"], 0),
+           "roofline_frac": r(line["roofline"]["frac"])}
+    g = line.get("reference_gpu") or {}
+    if g.get("value"):
+        out["reference_kernels"] = {
+            "denominators": g["denominators"], "value": r(g["value"], 0),
+            "ratio_fast": r(line["value"] / g["value"], 1),
+            "ratio_e2e": r(line["e2e"]["value"] / g["value"], 1),
+            "ratio_same_survivors": r(line["reference_plan"]["value"] / g["value"], 2)
+            if line.get("reference_plan") else None,
+            "survivors_match": g.get("survivor_set_matches_reference_plan")}
+    rc = line.get("record_curve_kernels") or {}
+    if rc.get("ratio_fast"):
+        out["record_curve_kernels"] = {"ratio_fast": r(rc["ratio_fast"], 2),
+                                       "ratio_same_survivors": r(rc["ratio_same_survivors"], 2),
+                                       "survivors_match": rc.get("survivor_count_matches_reference_plan")}
+    b = line.get("batch") or {}
+    if b:
+        out["batch"] = {"speedup_vs_plain": r(b.get("speedup_vs_plain"), 2),
+                        "points_identical": b.get("points_identical"),
+                        "roofline_frac": r((b.get("roofline") or {}).get("frac"))}
+    sv = line.get("serving") or {}
+    if sv:
+        out["serving"] = {"p50_ms": r(sv.get("p50_ms")), "p99_ms": r(sv.get("p99_ms")),
+                          "identical": (sv.get("identical_to_single_search") or {}).get("all")}
+        if sv.get("saturation"):
+            out["serving"]["saturation"] = {k: r(sv["saturation"].get(k)) for k in
+                                            ("value", "p50_ms", "p99_ms", "offered_rate")}
+    dc = line.get("dense_curve") or {}
+    if dc:
+        out["dense_curve_sha_ok"] = all(v.get("sha256_matches_reference") for v in dc["runs"].values())
+    rs = line.get("restricted") or {}
+    if rs:
+        out["restricted_identical"] = all(v.get("points_identical") for v in rs.values())
+    cb = line.get("cpu_baseline") or {}
+    if cb:
+        out["cpu_baseline"] = {"value": r(cb.get("value")), "kind": cb.get("kind"),
+                               "cores": cb.get("cores")}
+    return out
+
+
 def workload_config():
     rect = (2 * HEIGHT + 1) * DENOMINATORS
     return {"workload": "degree-6 curve, coefficients uniform in [-2^32, 2^32), "
@@ -513,7 +607,12 @@ def main():
     parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
     parser.add_argument("--plan", choices=["reference", "fast"], default="fast")
     parser.add_argument("--reference-plan-steps", type=int, default=2)
-    parser.add_argument("--reference-gpu-denominators", type=int, default=655360)
+    parser.add_argument("--reference-gpu-denominators", type=int, default=DENOMINATORS,
+                        help="denominators of the box the reference's kernels sieve (0: skip)")
+    parser.add_argument("--reference-gpu-steps", type=int, default=3,
+                        help="timed passes of the reference's kernels (median reported)")
+    parser.add_argument("--record-denominators", type=int, default=10 ** 6,
+                        help="denominators of the record-curve kernel comparison (0: skip)")
     parser.add_argument("--denominators", type=int, default=DENOMINATORS)
     parser.add_argument("--e2e-steps", type=int, default=3, choices=range(1, 100), metavar="N",
                         help="timed searches through rpg_point_search (median reported)")
@@ -582,6 +681,11 @@ def main():
         step_ms = max_over_ranks(sum(times) / len(times), dist)
         return {"ms": step_ms, "survivors": counts[0], "words": words, "bytes_per_word": per_word}
 
+    probe_clocks = ClockSampler(local)
+    with probe_clocks:
+        probe = rpg.smem_read_probe(device=local)
+    probe_clock_mhz = probe_clocks.summary().get("sm_mhz")
+    probe["sm_mhz"] = probe_clock_mhz
     clocks = ClockSampler(local)
     fast = measure(args.plan, args.steps, args.warmup, clocks)
     clock = clocks.summary()
@@ -607,10 +711,13 @@ def main():
     e2e_s = max_over_ranks(sorted(e2e_times)[len(e2e_times) // 2], dist)
     if rank != 0:
         return
-    sm_hz = (clock.get("sm_mhz") or 1965.0) * 1e6
     total_bytes = fast["words"] * fast["bytes_per_word"]
     achieved = total_bytes / (step_ms / 1e3) / 1e9
-    peak = SMS * SMEM_BYTES_PER_CLK * sm_hz / 1e9
+    sm_hz = (clock.get("sm_mhz") or probe_clock_mhz or 2070.0) * 1e6
+    nominal = SMS * NOMINAL_SMEM_BYTES_PER_CLK * sm_hz / 1e9
+    peak = probe["gbs"]
+    launch_s = step_ms / launches_per_step / 1e3
+    dram = FAST_LAUNCH_PROFILE["dram_bytes"] if args.plan == "fast" else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
@@ -624,21 +731,26 @@ def main():
                    "words_swept_per_step": fast["words"]},
         "roofline": {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
-                     "traffic": FAST_LAUNCH_DRAM_BYTES if args.plan == "fast" else None,
-                     "traffic_note": "DRAM bytes per 65,536-denominator launch from ncu; the "
+                     "traffic": dram,
+                     "traffic_note": "DRAM bytes per 65,536-denominator launch from the dated ncu "
+                                     f"capture in {FAST_LAUNCH_PROFILE['source']} (cold L2); the "
                                      "algorithmic shared-memory bytes per launch are "
                                      f"{total_bytes / launches_per_step:.3g}",
-                     "hbm": None if args.plan != "fast" or not measured_hbm_gbs() else {
-                         "achieved": FAST_LAUNCH_DRAM_BYTES / (step_ms / launches_per_step / 1e3) / 1e9,
-                         "peak": measured_hbm_gbs(), "unit": "GB/s",
-                         "frac": FAST_LAUNCH_DRAM_BYTES / (step_ms / launches_per_step / 1e3) / 1e9
-                                 / measured_hbm_gbs(),
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (STREAM-style copy)"},
                      "algorithmic": f"{fast['bytes_per_word']} B of stage-1 shared-memory rows per "
                                     f"swept 64-site word x {fast['words']} words per step "
                                     f"/ {launches_per_step} launches",
-                     "peak_source": "152 SMs x 128 B/clk (LDS.64 lane-contiguous, measured on "
-                                    "GB300) x median SM clock sampled in the timed region"},
+                     "peak_source": "rpg_smem_read_probe in this run: lane-contiguous 64-bit shared "
+                                    f"loads from every resident warp, {probe['gbs']:.0f} GB/s = "
+                                    f"{probe['bytes_per_clock_per_sm']:.1f} B/clk/SM (nominal "
+                                    f"{NOMINAL_SMEM_BYTES_PER_CLK} B/clk/SM x {SMS} SMs at the sampled "
+                                    f"clock: {nominal:.0f} GB/s, frac {achieved / nominal:.3f})",
+                     "int_pipe": {"alu_pipe_frac": FAST_LAUNCH_PROFILE["alu_pipe_frac"],
+                                  "issue_active_frac": FAST_LAUNCH_PROFILE["issue_active_frac"],
+                                  "source": FAST_LAUNCH_PROFILE["source"]} if args.plan == "fast" else None,
+                     "hbm": None if dram is None or not measured_hbm_gbs() else {
+                         "achieved": dram / launch_s / 1e9, "peak": measured_hbm_gbs(), "unit": "GB/s",
+                         "frac": dram / launch_s / 1e9 / measured_hbm_gbs(),
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (STREAM-style copy)"}},
         "e2e": {"value": reduced / e2e_s / 1e9, "unit": UNIT,
                 "seconds": e2e_s, "points": len(points),
                 "h2d_bytes_per_step": int(e2e_stats.get("h2d_bytes", 0)) if e2e_stats else 0,
@@ -650,13 +762,17 @@ def main():
         "clocks": clock,
     }
     if args.reference_gpu_denominators > 0:
-        line["reference_gpu"] = reference_gpu(coeffs, args.reference_gpu_denominators, rpg)
+        line["reference_gpu"] = reference_gpu(coeffs, args.reference_gpu_denominators, rpg,
+                                              args.reference_gpu_steps)
     if ref is not None:
         line["reference_plan"] = {
             "value": reduced / (ref["ms"] / 1e3) / 1e9, "unit": UNIT,
             "ms_per_step": ref["ms"], "modular_survivors": ref["survivors"],
             "note": "same kernel family with the reference's 32-prime plan: survivor set "
                     "identical to the reference implementation's"}
+    if args.record_denominators > 0:
+        line["record_curve_kernels"] = record_curve_kernels(rpg, torch, flush,
+                                                            denominators=args.record_denominators)
     if args.batch_curves > 0:
         line["batch"] = batch_benchmark(rpg, args.batch_curves, args.batch_plain_curves,
                                         shape=args.batch_shape, smem_peak_gbs=peak)
@@ -668,6 +784,7 @@ def main():
         line["dense_curve"] = dense_curve_benchmark(rpg, args.dense_height)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(coeffs, seconds=args.cpu_seconds)
+    line["summary"] = summary(line)
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

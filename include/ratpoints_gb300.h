@@ -337,6 +337,18 @@ void rpg_server_destroy(rpg_server *server);
  * No reference counterpart: the reference's kernels have no waits. */
 rpg_status rpg_bounded_wait_selftest(int32_t device, int32_t polls, int32_t arrive);
 
+/*
+ * The shared-memory read rate of `device` (-1: the current one): every
+ * resident warp issues lane-contiguous 64-bit shared loads, the access the
+ * sieve kernels' first stage makes, for `iterations` x 16 loads per thread.
+ * Writes the rate in GB/s (CUDA events around the launch), in bytes per SM
+ * clock (clock64 around one CTA's loop, times the CTAs resident per SM) and
+ * the launch time.  The sieve's shared-memory roofline is measured against
+ * it.  No counterpart in the reference.
+ */
+rpg_status rpg_smem_read_probe(int32_t device, int32_t iterations, double *gbs,
+                               double *bytes_per_clock_per_sm, double *ms);
+
 /* A finished rpg_sieve_run or rpg_point_search leaves its streams, events,
  * survivor buffers (up to 262,144 survivors) and pinned staging for the next
  * search on the same device (at most four such sets per process, about 16 MB

@@ -29,9 +29,9 @@ BIN_DIR = PACKAGE / "bin"
 LIBRARY = LIB_DIR / "librpgpu.so"
 EXECUTABLE = BIN_DIR / "ratpoints_gpu"
 
-CUDA_SOURCES = ["sieve.cu", "noalloc.cu", "batch.cu", "preverify.cu", "selftest.cu"]
-CXX_SOURCES = ["bigint.cpp", "exact.cpp", "plan.cpp", "search.cpp", "cli.cpp", "capi.cpp", "serve.cpp",
-               "compat_sieve.cpp"]
+CUDA_SOURCES = ["sieve.cu", "noalloc.cu", "batch.cu", "preverify.cu", "selftest.cu", "probe.cu"]
+CXX_SOURCES = ["bigint.cpp", "exact.cpp", "plan.cpp", "search.cpp", "cli.cpp", "point_format.cpp", "capi.cpp",
+               "serve.cpp", "compat_sieve.cpp"]
 MAIN_SOURCE = "ratpoints_gpu_main.cpp"
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 

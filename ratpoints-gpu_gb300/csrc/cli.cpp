@@ -1,393 +1,410 @@
-// ratpoints-compatible command line, output formatter and program entry.
+// The ratpoints_gpu command line: argument grammar, output rendering and the
+// program's top-level flow.
 //
-// Restates the reference's CLI contract so its harnesses and callers can run
-// this binary unchanged:
-//   - parse_command_line / OptionParser (src/command_line.cpp:113-366);
-//   - OutputFormatter (src/output_formatter.cpp:7-105);
-//   - main, --help, --list-devices and the -v metrics line (src/main.cpp:14-85).
+// The observable contract is the reference's and is kept byte for byte: the
+// option names and their arguments, the defaults and clamps, every error
+// message and the order in which errors are detected (src/command_line.cpp:
+// 336-366), the stdout bytes of a search (src/output_formatter.cpp), the -v
+// metrics line and the --list-devices line (src/main.cpp:14-43), and the exit
+// codes (src/main.cpp:48-85).  The code is this project's own: options are
+// looked up in one table and applied by a single dispatcher, and the point
+// format is compiled once into a list of pieces that is rendered per point.
 // Two extensions: --sieve-plan reference|fast selects the sieve plan (default
 // fast; reference reproduces the reference's modular survivor set and counts),
 // and --host-verify-only sends every modular survivor to the host's exact check
 // (by default a device kernel first drops those that cannot be points).
 #include "cli.hpp"
 
+#include <algorithm>
+#include <cctype>
 #include <cerrno>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <limits>
-#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
 
+#include "point_format.hpp"
 #include "search.hpp"
 
 namespace rpg {
 
 namespace {
 
-constexpr int kMaximumDegree = 100;
-constexpr long long kMaximumHeight = (std::numeric_limits<long long>::max() - 32) / 2;
-constexpr char kUsage[] = "Usage: ratpoints_gpu 'c0 c1 ... cn' HEIGHT [OPTIONS]";
+constexpr std::size_t kMostCoefficients = 101;  // degree 100
+constexpr long long kHeightCeiling = (std::numeric_limits<long long>::max() - 32) / 2;
+constexpr int kSquareDenominatorCeiling = 46340;  // floor(sqrt(2^31 - 1))
+constexpr int kLargestBatch = 1 << 16;
 
-struct OutputOptions {
-    bool print_points = true;
-    bool print_y = true;
-    std::string format, before, between, after;
-};
+[[noreturn]] void usage_error(const std::string &message) { throw std::invalid_argument(message); }
 
-struct ProgramOptions {
+// ---------------------------------------------------------------------------
+// Settings the command line produces
+
+struct Invocation {
     SearchOptions search;
-    OutputOptions output;
-    bool quiet = false, verbose = false, stop_after_first = false;
+    RenderSettings render;
+    bool quiet = false;
+    bool verbose = false;
+    bool first_point_only = false;
 };
 
-long long parse_positive(const char *text, const char *name) {
+// ---------------------------------------------------------------------------
+// Scalar arguments
+
+// A positive decimal count as strtoll reads it (leading blanks and a sign are
+// allowed, nothing may follow); anything else is "<what> must be positive".
+long long positive_count(const char *text, const std::string &what) {
+    char *stop = nullptr;
     errno = 0;
-    char *end = nullptr;
-    long long value = std::strtoll(text, &end, 10);
-    if (errno == ERANGE || end == text || *end || value < 1)
-        throw std::invalid_argument(std::string(name) + " must be positive");
+    const long long value = std::strtoll(text, &stop, 10);
+    const bool whole = stop != text && *stop == '\0' && errno != ERANGE;
+    if (!whole || value <= 0) usage_error(what + " must be positive");
     return value;
 }
 
-int parse_positive_int(const char *text, const char *name) {
-    long long value = parse_positive(text, name);
-    if (value > std::numeric_limits<int>::max())
-        throw std::invalid_argument(std::string(name) + " exceeds GPU limit");
-    return int(value);
+int positive_int(const char *text, const std::string &what) {
+    const long long value = positive_count(text, what);
+    if (value > std::numeric_limits<int>::max()) usage_error(what + " exceeds GPU limit");
+    return static_cast<int>(value);
 }
 
-Rational real_or_throw(const char *text, const char *name) {
-    Rational r;
-    std::string error;
-    if (!parse_real(text, name, r, error)) throw std::invalid_argument(error);
-    return r;
+Rational real_bound(const char *text, const std::string &what) {
+    Rational value;
+    std::string problem;
+    if (!parse_real(text, what, value, problem)) usage_error(problem);
+    return value;
 }
 
-bool is_integer(const std::string &text) {
-    std::size_t i = !text.empty() && (text[0] == '-' || text[0] == '+');
-    if (i == text.size()) return false;
-    for (; i < text.size(); ++i)
-        if (text[i] < '0' || text[i] > '9') return false;
-    return true;
-}
-
-bool is_zero(const std::string &text) {
-    std::size_t i = !text.empty() && (text[0] == '-' || text[0] == '+');
-    for (; i < text.size(); ++i)
-        if (text[i] != '0') return false;
-    return true;
-}
-
-std::vector<std::string> split_coefficients(const char *text) {
-    std::istringstream stream(text);
-    std::vector<std::string> out;
-    for (std::string token; stream >> token;) {
-        if (!token.empty() && token.front() == '+') token.erase(0, 1);
-        out.push_back(token);
+// Whitespace-separated tokens of the coefficient argument, one leading '+' of
+// each token dropped.
+std::vector<std::string> coefficient_tokens(const char *text) {
+    std::vector<std::string> tokens;
+    const std::string s(text);
+    std::size_t i = 0;
+    while (i < s.size()) {
+        while (i < s.size() && std::isspace(static_cast<unsigned char>(s[i]))) ++i;
+        const std::size_t begin = i;
+        while (i < s.size() && !std::isspace(static_cast<unsigned char>(s[i]))) ++i;
+        if (i > begin) tokens.push_back(s.substr(begin, i - begin));
     }
-    return out;
+    for (auto &t : tokens)
+        if (t[0] == '+') t.erase(t.begin());
+    return tokens;
 }
 
-void validate_coefficients(const std::vector<std::string> &c) {
-    if (c.size() < 2 || c.size() > std::size_t(kMaximumDegree + 1))
-        throw std::invalid_argument("supported polynomial degrees are 1 through 100");
-    for (const auto &x : c)
-        if (!is_integer(x)) throw std::invalid_argument("coefficients must be decimal integers");
-    if (is_zero(c.back())) throw std::invalid_argument("leading coefficient must be nonzero");
+// Sign and digits of a decimal integer token: whether it is one, and whether
+// its digits are all zero.
+struct IntegerShape {
+    bool integer;
+    bool zero;
+};
+
+IntegerShape shape_of(const std::string &token) {
+    const bool signed_token = !token.empty() && (token[0] == '+' || token[0] == '-');
+    const auto digits = token.begin() + (signed_token ? 1 : 0);
+    const bool any = digits != token.end();
+    const bool all_digits = std::all_of(digits, token.end(), [](char c) { return c >= '0' && c <= '9'; });
+    const bool all_zero = std::all_of(digits, token.end(), [](char c) { return c == '0'; });
+    return {any && all_digits, all_zero};
 }
 
-class OptionParser {
+void check_coefficients(const std::vector<std::string> &tokens) {
+    if (tokens.size() < 2 || tokens.size() > kMostCoefficients)
+        usage_error("supported polynomial degrees are 1 through 100");
+    if (!std::all_of(tokens.begin(), tokens.end(),
+                     [](const std::string &t) { return shape_of(t).integer; }))
+        usage_error("coefficients must be decimal integers");
+    if (shape_of(tokens.back()).zero) usage_error("leading coefficient must be nonzero");
+}
+
+// ---------------------------------------------------------------------------
+// Option table and dispatcher
+
+enum class Action {
+    LowerDenominator, UpperDenominator, OpenInterval, CloseInterval, HideInfinity, ShowInfinity,
+    HideOrdinates, ShowOrdinates, HidePoints, ShowPoints, Format, Prefix, Separator, Suffix,
+    Devices, BatchSize, SquareDenominators, SievePlan, HostVerifyOnly, Quiet, Verbose,
+    FirstPointOnly, NoEffect
+};
+
+struct OptionEntry {
+    const char *flag;
+    Action action;
+};
+
+constexpr OptionEntry kOptionTable[] = {
+    {"-dl", Action::LowerDenominator}, {"-du", Action::UpperDenominator},
+    {"-l", Action::OpenInterval},      {"-u", Action::CloseInterval},
+    {"-i", Action::HideInfinity},      {"-I", Action::ShowInfinity},
+    {"-y", Action::HideOrdinates},     {"-Y", Action::ShowOrdinates},
+    {"-z", Action::HidePoints},        {"-Z", Action::ShowPoints},
+    {"-f", Action::Format},            {"-fs", Action::Prefix},
+    {"-fm", Action::Separator},        {"-fe", Action::Suffix},
+    {"--devices", Action::Devices},    {"--batch-size", Action::BatchSize},
+    {"--square-denominators", Action::SquareDenominators},
+    {"--sieve-plan", Action::SievePlan},
+    {"--host-verify-only", Action::HostVerifyOnly},
+    {"-q", Action::Quiet},             {"-v", Action::Verbose},
+    {"-1", Action::FirstPointOnly},
+    // CPU-side switches of ratpoints; they do not change the searched set.
+    {"-s", Action::NoEffect}, {"-k", Action::NoEffect}, {"-K", Action::NoEffect},
+    {"-j", Action::NoEffect}, {"-J", Action::NoEffect},
+};
+
+class ArgumentReader {
 public:
-    OptionParser(int argc, char **argv, ProgramOptions &result)
-        : argc_(argc), argv_(argv), result_(result) {}
-
-    void parse() {
-        while (index_ < argc_) {
-            std::string option(argv_[index_++]);
-            if (search_option(option) || output_option(option) || runtime_option(option)) continue;
-            throw std::invalid_argument("unsupported ratpoints option: " + option);
-        }
-        if (has_pending_) {
-            SearchInterval iv;
-            iv.lower = pending_;
-            iv.upper_infinite = true;
-            result_.search.intervals.push_back(iv);
-        }
+    ArgumentReader(int argc, char **argv, int start) : argc_(argc), argv_(argv), at_(start) {}
+    bool done() const { return at_ >= argc_; }
+    std::string take_flag() { return argv_[at_++]; }
+    const char *take_value(const std::string &flag) {
+        if (done()) usage_error(flag + " requires an argument");
+        return argv_[at_++];
     }
 
 private:
-    const char *argument(const std::string &option) {
-        if (index_ >= argc_) throw std::invalid_argument(option + " requires an argument");
-        return argv_[index_++];
-    }
-
-    bool search_option(const std::string &o) {
-        if (o == "-dl") {
-            result_.search.first = parse_positive_int(argument(o), "lower denominator");
-        } else if (o == "-du") {
-            result_.search.last = parse_positive_int(argument(o), "upper denominator");
-        } else if (o == "-l") {
-            if (has_pending_) throw std::invalid_argument("interval lower bound without upper bound");
-            pending_ = real_or_throw(argument(o), "interval lower bound");
-            has_pending_ = true;
-        } else if (o == "-u") {
-            Rational upper = real_or_throw(argument(o), "interval upper bound");
-            if (has_pending_ && Rational::compare(pending_, upper) > 0)
-                throw std::invalid_argument("interval lower bound exceeds upper bound");
-            auto &ivs = result_.search.intervals;
-            if (!ivs.empty() && (!has_pending_ || ivs.back().upper_infinite ||
-                                 Rational::compare(pending_, ivs.back().upper) < 0))
-                throw std::invalid_argument("search intervals must be ordered");
-            SearchInterval iv;
-            iv.lower = pending_;
-            iv.upper = upper;
-            iv.lower_infinite = !has_pending_;
-            ivs.push_back(iv);
-            has_pending_ = false;
-        } else if (o == "-i") {
-            result_.search.include_infinity = false;
-        } else if (o == "-I") {
-            result_.search.include_infinity = true;
-        } else {
-            return false;
-        }
-        return true;
-    }
-
-    bool output_option(const std::string &o) {
-        auto &out = result_.output;
-        if (o == "-y") out.print_y = false;
-        else if (o == "-Y") out.print_y = true;
-        else if (o == "-z") out.print_points = false;
-        else if (o == "-Z") out.print_points = true;
-        else if (o == "-f") out.format = argument(o);
-        else if (o == "-fs") out.before = argument(o);
-        else if (o == "-fm") out.between = argument(o);
-        else if (o == "-fe") out.after = argument(o);
-        else return false;
-        return true;
-    }
-
-    bool runtime_option(const std::string &o) {
-        auto &s = result_.search;
-        if (o == "--devices") {
-            s.devices = parse_device_selection(argument(o));
-        } else if (o == "--batch-size") {
-            s.batch_size = parse_positive_int(argument(o), "denominator batch size");
-            if (s.batch_size > (1 << 16))
-                throw std::invalid_argument("--batch-size must not exceed 65536");
-        } else if (o == "--square-denominators") {
-            s.square = true;
-        } else if (o == "--sieve-plan") {
-            std::string v = argument(o);
-            if (v == "reference") s.plan = PlanKind::reference;
-            else if (v == "fast") s.plan = PlanKind::fast;
-            else throw std::invalid_argument("--sieve-plan must be reference or fast");
-        } else if (o == "--host-verify-only") {
-            s.device_preverify = false;
-        } else if (o == "-q") {
-            result_.quiet = true;
-        } else if (o == "-v") {
-            result_.verbose = true;
-        } else if (o == "-1") {
-            result_.stop_after_first = true;
-        } else if (o == "-s" || o == "-k" || o == "-K" || o == "-j" || o == "-J") {
-            // Accepted with no effect, as in the reference (command_line.cpp:252-254).
-        } else {
-            return false;
-        }
-        return true;
-    }
-
     int argc_;
     char **argv_;
-    ProgramOptions &result_;
-    int index_ = 3;
-    Rational pending_;
-    bool has_pending_ = false;
+    int at_;
 };
 
-ProgramOptions parse_command_line(int argc, char **argv) {
-    if (argc < 3) throw std::invalid_argument(kUsage);
-    ProgramOptions r;
-    r.search.coefficients = split_coefficients(argv[1]);
-    r.search.numerator_bound = parse_positive(argv[2], "maximum height");
-    if (r.search.numerator_bound > kMaximumHeight)
-        throw std::invalid_argument("maximum height exceeds safe GPU limit");
-    r.search.last = r.search.numerator_bound > std::numeric_limits<int>::max()
-                        ? std::numeric_limits<int>::max()
-                        : r.search.numerator_bound;
-    OptionParser(argc, argv, r).parse();
-    if (r.search.last > r.search.numerator_bound) r.search.last = r.search.numerator_bound;
-    if (r.search.square && r.search.last > 46340) r.search.last = 46340;
-    if (r.search.first > r.search.last) throw std::invalid_argument("empty denominator range");
-    validate_coefficients(r.search.coefficients);
-    return r;
-}
+// Interval state across -l / -u: an -l waits for its -u; an -l left open at
+// the end becomes [lower, +infinity).
+struct IntervalBuilder {
+    bool open = false;
+    Rational lower;
 
-class OutputFormatter {
-public:
-    explicit OutputFormatter(const OutputOptions &o)
-        : print_points_(o.print_points), print_y_(o.print_y),
-          format_(decode(o.format.empty() ? (o.print_y ? "(%x : %y : %z)\\n" : "(%x : %z)\\n")
-                                          : o.format)),
-          before_(decode(o.before)), between_(decode(o.between)), after_(decode(o.after)) {
-        if (print_points_) write(before_);
+    void begin(const Rational &bound) {
+        open = true;
+        lower = bound;
     }
-
-    void point_pair(const PointPair &p, bool include_conjugate) {
-        write_point(p.numerator, p.ordinate, p.denominator);
-        if (include_conjugate && print_y_ && p.ordinate != "0")
-            write_point(p.numerator, "-" + p.ordinate, p.denominator);
-    }
-
-    void finish() {
-        if (finished_) return;
-        write(after_);
-        if (std::fflush(stdout) == EOF) throw std::runtime_error("failed to flush standard output");
-        finished_ = true;
-    }
-
-private:
-    static constexpr char kEscapedPercent = '\x01';
-
-    static std::string decode(const std::string &in) {
-        std::string out;
-        for (std::size_t i = 0; i < in.size(); ++i) {
-            if (in[i] != '\\' || i + 1 == in.size()) {
-                out.push_back(in[i]);
-                continue;
-            }
-            char e = in[++i];
-            if (e == 'n') out.push_back('\n');
-            else if (e == 't') out.push_back('\t');
-            else if (e == '%') out.push_back(kEscapedPercent);
-            else {
-                out.push_back('\\');
-                out.push_back(e);
-            }
+    void close(const Rational &upper, std::vector<SearchInterval> &out) {
+        if (open && Rational::compare(lower, upper) > 0)
+            usage_error("interval lower bound exceeds upper bound");
+        if (!out.empty()) {
+            const SearchInterval &prev = out.back();
+            const bool ordered = open && !prev.upper_infinite && Rational::compare(lower, prev.upper) >= 0;
+            if (!ordered) usage_error("search intervals must be ordered");
         }
-        return out;
+        SearchInterval iv;
+        iv.lower_infinite = !open;
+        if (open) iv.lower = lower;
+        iv.upper = upper;
+        out.push_back(iv);
+        open = false;
     }
-
-    static void write(const std::string &text) {
-        if (std::fputs(text.c_str(), stdout) == EOF)
-            throw std::runtime_error("failed to write standard output");
+    void finish(std::vector<SearchInterval> &out) {
+        if (!open) return;
+        SearchInterval iv;
+        iv.lower = lower;
+        iv.upper_infinite = true;
+        out.push_back(iv);
+        open = false;
     }
-
-    void write_point(long long numerator, const std::string &ordinate, long long denominator) {
-        if (!print_points_) return;
-        if (emitted_) write(between_);
-        std::string s;
-        for (std::size_t i = 0; i < format_.size(); ++i) {
-            if (format_[i] != '%' || i + 1 == format_.size()) {
-                s.push_back(format_[i]);
-                continue;
-            }
-            char m = format_[i + 1];
-            if (m == 'x') s += std::to_string(numerator);
-            else if (m == 'y' && print_y_) s += ordinate;
-            else if (m == 'z') s += std::to_string(denominator);
-            else {
-                s.push_back('%');
-                s.push_back(m);
-            }
-            ++i;
-        }
-        for (char &c : s)
-            if (c == kEscapedPercent) c = '%';
-        write(s);
-        emitted_ = true;
-    }
-
-    bool print_points_, print_y_;
-    std::string format_, before_, between_, after_;
-    bool emitted_ = false, finished_ = false;
 };
 
-void print_help(std::FILE *stream) {
-    static const char text[] =
-        "Usage: ratpoints_gpu 'c0 c1 ... cn' HEIGHT [OPTIONS]\n"
-        "\n"
-        "Search y^2 = c0 + c1 x + ... + cn x^n for x = a/b with |a| <= HEIGHT.\n"
-        "\n"
-        "Device options:\n"
-        "  --devices all|0,1,...  choose CUDA-visible GPUs; the first one runs the search\n"
-        "  --batch-size N         denominators per batch, 1..65536 (default 65536)\n"
-        "  --square-denominators  treat -dl/-du as bounds on k and search d = k^2\n"
-        "  --sieve-plan P         reference or fast (default fast); same points either way\n"
-        "  --host-verify-only     check every modular survivor on the host (no device pre-verification)\n"
-        "  --list-devices         print the visible GPUs and exit\n"
-        "\n"
-        "Search and output options:\n"
-        "  -dl B, -du B   lower and upper denominator bounds\n"
-        "  -l L, -u U     start and end a closed interval for x (repeatable)\n"
-        "  -1             stop after the first point\n"
-        "  -i, -I         leave out or include points at infinity\n"
-        "  -y, -Y         leave out or include ordinates\n"
-        "  -z, -Z         leave out or include point lines\n"
-        "  -q             no timing output\n"
-        "  -v             timing and survivor metrics on standard error\n"
-        "  -f FORMAT      point format with %x, %y, %z\n"
-        "  -fs, -fm, -fe  text before, between and after the points\n"
-        "  -s, -k, -K, -j, -J  accepted, no effect\n"
-        "  --help         this text\n";
-    if (std::fputs(text, stream) == EOF) throw std::runtime_error("failed to write help output");
+void apply(Action action, const std::string &flag, ArgumentReader &args, IntervalBuilder &intervals,
+           Invocation &inv) {
+    SearchOptions &s = inv.search;
+    RenderSettings &r = inv.render;
+    switch (action) {
+    case Action::LowerDenominator: s.first = positive_int(args.take_value(flag), "lower denominator"); break;
+    case Action::UpperDenominator: s.last = positive_int(args.take_value(flag), "upper denominator"); break;
+    case Action::OpenInterval:
+        // an unmatched -l is reported before this one's argument is read
+        if (intervals.open) usage_error("interval lower bound without upper bound");
+        intervals.begin(real_bound(args.take_value(flag), "interval lower bound"));
+        break;
+    case Action::CloseInterval:
+        intervals.close(real_bound(args.take_value(flag), "interval upper bound"), s.intervals);
+        break;
+    case Action::HideInfinity: s.include_infinity = false; break;
+    case Action::ShowInfinity: s.include_infinity = true; break;
+    case Action::HideOrdinates: r.ordinates = false; break;
+    case Action::ShowOrdinates: r.ordinates = true; break;
+    case Action::HidePoints: r.points = false; break;
+    case Action::ShowPoints: r.points = true; break;
+    case Action::Format: r.format = args.take_value(flag); break;
+    case Action::Prefix: r.before = args.take_value(flag); break;
+    case Action::Separator: r.between = args.take_value(flag); break;
+    case Action::Suffix: r.after = args.take_value(flag); break;
+    case Action::Devices: s.devices = parse_device_selection(args.take_value(flag)); break;
+    case Action::BatchSize:
+        s.batch_size = positive_int(args.take_value(flag), "denominator batch size");
+        if (s.batch_size > kLargestBatch) usage_error("--batch-size must not exceed 65536");
+        break;
+    case Action::SquareDenominators: s.square = true; break;
+    case Action::SievePlan: {
+        const std::string plan = args.take_value(flag);
+        if (plan == "fast") s.plan = PlanKind::fast;
+        else if (plan == "reference") s.plan = PlanKind::reference;
+        else usage_error("--sieve-plan must be reference or fast");
+        break;
+    }
+    case Action::HostVerifyOnly: s.device_preverify = false; break;
+    case Action::Quiet: inv.quiet = true; break;
+    case Action::Verbose: inv.verbose = true; break;
+    case Action::FirstPointOnly: inv.first_point_only = true; break;
+    case Action::NoEffect: break;
+    }
 }
 
-void print_device(std::FILE *stream, const GpuDevice &d) {
-    std::fprintf(stream, "device=%d name=\"%s\" compute=%d.%d sm=%d memory_mib=%llu pci=%s\n", d.id,
-                 d.name.c_str(), d.major, d.minor, d.multiprocessors,
-                 d.memory_bytes / (1024ULL * 1024ULL), d.pci_bus_id.c_str());
+Invocation read_invocation(int argc, char **argv) {
+    if (argc < 3) usage_error("Usage: ratpoints_gpu 'c0 c1 ... cn' HEIGHT [OPTIONS]");
+    Invocation inv;
+    SearchOptions &s = inv.search;
+    s.coefficients = coefficient_tokens(argv[1]);
+    s.numerator_bound = positive_count(argv[2], "maximum height");
+    if (s.numerator_bound > kHeightCeiling) usage_error("maximum height exceeds safe GPU limit");
+    s.last = std::min<long long>(s.numerator_bound, std::numeric_limits<int>::max());
+
+    ArgumentReader args(argc, argv, 3);
+    IntervalBuilder intervals;
+    while (!args.done()) {
+        const std::string flag = args.take_flag();
+        const auto *entry = std::find_if(std::begin(kOptionTable), std::end(kOptionTable),
+                                         [&](const OptionEntry &e) { return flag == e.flag; });
+        if (entry == std::end(kOptionTable)) usage_error("unsupported ratpoints option: " + flag);
+        apply(entry->action, flag, args, intervals, inv);
+    }
+    intervals.finish(s.intervals);
+
+    s.last = std::min(s.last, s.numerator_bound);
+    if (s.square) s.last = std::min<long long>(s.last, kSquareDenominatorCeiling);
+    if (s.first > s.last) usage_error("empty denominator range");
+    check_coefficients(s.coefficients);
+    return inv;
 }
 
-void print_metrics(const SearchMetrics &m) {
-    std::fprintf(stderr,
-                 "wall_ms=%.3f devices=%zu denominators=%llu basis_ms=%.3f sieve_ms=%.3f words=%llu "
-                 "initial_mask_gbs=%.3f survivors=%llu exact_survivors=%llu plan_ms=%.3f "
-                 "workspace_ms=%.3f basis_wall_ms=%.3f survivor_setup_ms=%.3f "
-                 "verification_ms=%.3f sieve_wall_ms=%.3f\n",
-                 m.wall_ms, m.devices.size(), m.denominator_count, m.basis_ms, m.sieve_ms,
-                 m.word_count, m.initial_mask_gbs(), m.modular_survivors, m.exact_survivors,
-                 m.plan_ms, m.workspace_ms, m.basis_wall_ms, m.survivor_setup_ms,
-                 m.verification_ms, m.sieve_wall_ms);
-    for (const auto &e : m.devices) {
-        print_device(stderr, e.device);
+// ---------------------------------------------------------------------------
+// Help, device listing and metrics
+
+constexpr char kHelpText[] =
+    "Usage: ratpoints_gpu 'c0 c1 ... cn' HEIGHT [OPTIONS]\n"
+    "\n"
+    "Search y^2 = c0 + c1 x + ... + cn x^n for x = a/b with |a| <= HEIGHT.\n"
+    "\n"
+    "Device options:\n"
+    "  --devices all|0,1,...  choose CUDA-visible GPUs; the first one runs the search\n"
+    "  --batch-size N         denominators per batch, 1..65536 (default 65536)\n"
+    "  --square-denominators  treat -dl/-du as bounds on k and search d = k^2\n"
+    "  --sieve-plan P         reference or fast (default fast); same points either way\n"
+    "  --host-verify-only     check every modular survivor on the host (no device pre-verification)\n"
+    "  --list-devices         print the visible GPUs and exit\n"
+    "\n"
+    "Search and output options:\n"
+    "  -dl B, -du B   lower and upper denominator bounds\n"
+    "  -l L, -u U     start and end a closed interval for x (repeatable)\n"
+    "  -1             stop after the first point\n"
+    "  -i, -I         leave out or include points at infinity\n"
+    "  -y, -Y         leave out or include ordinates\n"
+    "  -z, -Z         leave out or include point lines\n"
+    "  -q             no timing output\n"
+    "  -v             timing and survivor metrics on standard error\n"
+    "  -f FORMAT      point format with %x, %y, %z\n"
+    "  -fs, -fm, -fe  text before, between and after the points\n"
+    "  -s, -k, -K, -j, -J  accepted, no effect\n"
+    "  --help         this text\n";
+
+void show_help(std::FILE *to) {
+    if (std::fputs(kHelpText, to) == EOF) throw std::runtime_error("failed to write help output");
+}
+
+void describe_device(std::FILE *to, const GpuDevice &g) {
+    std::fprintf(to, "device=%d name=\"%s\" compute=%d.%d sm=%d memory_mib=%llu pci=%s\n", g.id,
+                 g.name.c_str(), g.major, g.minor, g.multiprocessors, g.memory_bytes >> 20,
+                 g.pci_bus_id.c_str());
+}
+
+// The -v line: key=value fields in the reference's order and formats (the
+// reference's benchmark harness parses them), then one pair of lines per GPU.
+void report_metrics(const SearchMetrics &m) {
+    struct Field {
+        const char *key;
+        bool real;
+        double x;
+        unsigned long long n;
+    };
+    const Field fields[] = {
+        {"wall_ms", true, m.wall_ms, 0},
+        {"devices", false, 0, m.devices.size()},
+        {"denominators", false, 0, m.denominator_count},
+        {"basis_ms", true, m.basis_ms, 0},
+        {"sieve_ms", true, m.sieve_ms, 0},
+        {"words", false, 0, m.word_count},
+        {"initial_mask_gbs", true, m.initial_mask_gbs(), 0},
+        {"survivors", false, 0, m.modular_survivors},
+        {"exact_survivors", false, 0, m.exact_survivors},
+        {"plan_ms", true, m.plan_ms, 0},
+        {"workspace_ms", true, m.workspace_ms, 0},
+        {"basis_wall_ms", true, m.basis_wall_ms, 0},
+        {"survivor_setup_ms", true, m.survivor_setup_ms, 0},
+        {"verification_ms", true, m.verification_ms, 0},
+        {"sieve_wall_ms", true, m.sieve_wall_ms, 0},
+    };
+    std::string line;
+    char buf[64];
+    for (const Field &f : fields) {
+        if (f.real) std::snprintf(buf, sizeof buf, "%s=%.3f", f.key, f.x);
+        else std::snprintf(buf, sizeof buf, "%s=%llu", f.key, f.n);
+        if (!line.empty()) line.push_back(' ');
+        line += buf;
+    }
+    std::fprintf(stderr, "%s\n", line.c_str());
+    for (const DeviceMetrics &d : m.devices) {
+        describe_device(stderr, d.device);
         std::fprintf(stderr, "gpu=%d denominators=%llu batches=%llu basis_ms=%.3f sieve_ms=%.3f\n",
-                     e.device.id, e.denominator_count, e.batches, e.basis_ms, e.sieve_ms);
+                     d.device.id, d.denominator_count, d.batches, d.basis_ms, d.sieve_ms);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Program flow
+
+enum class Request { HelpOnStderr, Help, ListDevices, Search };
+
+Request classify(int argc, char **argv) {
+    if (argc <= 1) return Request::HelpOnStderr;
+    if (argc == 2 && std::strcmp(argv[1], "--help") == 0) return Request::Help;
+    if (argc == 2 && std::strcmp(argv[1], "--list-devices") == 0) return Request::ListDevices;
+    return Request::Search;
+}
+
+int search_and_print(int argc, char **argv) {
+    const Invocation inv = read_invocation(argc, argv);
+    PointSearch search(inv.search);  // validates before anything is written
+    PointPrinter printer(inv.render, stdout);
+    const bool keep_going = !inv.first_point_only;
+    const SearchMetrics metrics = search.run([&](const PointPair &p) {
+        printer.point(p.numerator, p.ordinate, p.denominator, keep_going);
+        return keep_going;
+    });
+    printer.close();
+    const bool benchmark_env = std::getenv("RATPOINTS_GPU_BENCHMARK") != nullptr;
+    if (benchmark_env || (inv.verbose && !inv.quiet)) report_metrics(metrics);
+    return 0;
 }
 
 }  // namespace
 
 int run_cli(int argc, char **argv) {
     try {
-        if (argc == 1) {
-            print_help(stderr);
+        switch (classify(argc, argv)) {
+        case Request::HelpOnStderr:
+            show_help(stderr);
             return 1;
-        }
-        if (argc == 2 && std::string(argv[1]) == "--help") {
-            print_help(stdout);
+        case Request::Help:
+            show_help(stdout);
             return 0;
-        }
-        if (argc == 2 && std::string(argv[1]) == "--list-devices") {
-            for (const auto &d : available_gpu_devices()) print_device(stdout, d);
+        case Request::ListDevices:
+            for (const GpuDevice &g : available_gpu_devices()) describe_device(stdout, g);
             return std::fflush(stdout) == EOF ? 1 : 0;
+        case Request::Search:
+            return search_and_print(argc, argv);
         }
-        ProgramOptions options = parse_command_line(argc, argv);
-        PointSearch search(options.search);
-        OutputFormatter output(options.output);
-        const bool stop = options.stop_after_first;
-        SearchMetrics metrics = search.run([&](const PointPair &p) {
-            output.point_pair(p, !stop);
-            return !stop;
-        });
-        output.finish();
-        if (std::getenv("RATPOINTS_GPU_BENCHMARK") != nullptr || (options.verbose && !options.quiet))
-            print_metrics(metrics);
-        return 0;
+        return 1;
     } catch (const std::exception &error) {
         std::fflush(stdout);
         std::fprintf(stderr, "%s\n", error.what());

@@ -231,67 +231,66 @@ int Rational::compare_fraction(long long a, long long d) const {
     return BigInt::compare(left, right);
 }
 
+namespace {
+
+// A run of decimal digits starting at `at`; advances `at` past it.
+std::string digit_run(const std::string &text, std::size_t &at) {
+    const std::size_t begin = at;
+    while (at < text.size() && text[at] >= '0' && text[at] <= '9') ++at;
+    return text.substr(begin, at - begin);
+}
+
+}  // namespace
+
+// Grammar: [sign] int-digits [ '.' frac-digits ] [ ('e'|'E') [sign] exp-digits ]
+// with at least one int or frac digit and at least one exp digit after an 'e'.
+// The exponent's magnitude is checked digit by digit as it is read (a value
+// above 10000 is "exponent is too large", reported before anything after the
+// exponent is looked at); every other malformed input is "must be real".
+// The value is (int-digits frac-digits) x 10^(exp - #frac-digits).
 bool parse_real(const std::string &input, const std::string &name, Rational &out,
                 std::string &error) {
-    std::size_t index = 0;
-    bool negative = false;
-    if (index < input.size() && (input[index] == '+' || input[index] == '-'))
-        negative = input[index++] == '-';
-    std::string digits;
-    std::size_t fractional = 0;
-    bool saw_digit = false;
-    while (index < input.size() && input[index] >= '0' && input[index] <= '9') {
-        digits.push_back(input[index++]);
-        saw_digit = true;
-    }
-    if (index < input.size() && input[index] == '.') {
-        ++index;
-        std::size_t start = digits.size();
-        while (index < input.size() && input[index] >= '0' && input[index] <= '9') {
-            digits.push_back(input[index++]);
-            saw_digit = true;
-        }
-        fractional = digits.size() - start;
-    }
-    long long exponent = 0;
-    bool exponent_negative = false;
-    if (index < input.size() && (input[index] == 'e' || input[index] == 'E')) {
-        ++index;
-        if (index < input.size() && (input[index] == '+' || input[index] == '-'))
-            exponent_negative = input[index++] == '-';
-        std::size_t start = index;
-        while (index < input.size() && input[index] >= '0' && input[index] <= '9') {
-            int digit = input[index++] - '0';
-            if (exponent > (10000 - digit) / 10) {
-                error = name + " exponent is too large";
-                return false;
-            }
-            exponent = exponent * 10 + digit;
-        }
-        if (index == start) {
-            error = name + " must be real";
-            return false;
-        }
-    }
-    if (!saw_digit || index != input.size()) {
-        error = name + " must be real";
+    auto reject = [&](const char *why) {
+        error = name + why;
         return false;
+    };
+    std::size_t at = 0;
+    const bool minus = at < input.size() && input[at] == '-';
+    if (at < input.size() && (input[at] == '-' || input[at] == '+')) ++at;
+    std::string mantissa = digit_run(input, at);
+    std::size_t fraction_digits = 0;
+    if (at < input.size() && input[at] == '.') {
+        ++at;
+        const std::string fraction = digit_run(input, at);
+        fraction_digits = fraction.size();
+        mantissa += fraction;
     }
-    if (exponent_negative) exponent = -exponent;
-    BigInt numerator;
-    if (!BigInt::parse(digits.empty() ? std::string("0") : digits, numerator)) {
-        error = name + " must be real";
-        return false;
+    long long power_of_ten = 0;
+    if (at < input.size() && (input[at] == 'e' || input[at] == 'E')) {
+        ++at;
+        const bool exponent_minus = at < input.size() && input[at] == '-';
+        if (at < input.size() && (input[at] == '-' || input[at] == '+')) ++at;
+        const std::string exponent = digit_run(input, at);
+        if (exponent.empty()) return reject(" must be real");
+        long long magnitude = 0;
+        for (char c : exponent) {
+            magnitude = magnitude * 10 + (c - '0');
+            if (magnitude > 10000) return reject(" exponent is too large");
+        }
+        power_of_ten = exponent_minus ? -magnitude : magnitude;
     }
-    if (negative) numerator.negate();
-    long long scale = (long long)fractional - exponent;
-    BigInt power(1);
-    for (long long i = 0; i < (scale < 0 ? -scale : scale); ++i) power.mul_small(10);
-    if (scale >= 0) {
-        out.num = numerator;
-        out.den = power;
+    if (mantissa.empty() || at != input.size()) return reject(" must be real");
+    BigInt value;
+    if (!BigInt::parse(mantissa, value)) return reject(" must be real");
+    if (minus) value.negate();
+    const long long shift = power_of_ten - (long long)fraction_digits;
+    BigInt scale(1);
+    for (long long k = shift < 0 ? -shift : shift; k > 0; --k) scale.mul_small(10);
+    if (shift < 0) {
+        out.num = value;
+        out.den = scale;
     } else {
-        out.num = BigInt::mul(numerator, power);
+        out.num = BigInt::mul(value, scale);
         out.den = BigInt(1);
     }
     return true;

@@ -52,9 +52,10 @@ struct Rational {
     int compare_fraction(long long a, long long d) const;
 };
 
-// parse_real of the reference (src/command_line.cpp:39-108): [+-]digits[.digits][e[+-]digits],
-// at least one digit, exponent magnitude at most 10000.  On failure returns false and
-// sets error to "<name> must be real" or "<name> exponent is too large".
+// A real bound of -l / -u in the reference's accepted syntax (src/command_line.cpp:39-108):
+// [+-]digits[.digits][e[+-]digits] with at least one digit and an exponent of magnitude at
+// most 10000.  On failure returns false and sets error to "<name> must be real" or
+// "<name> exponent is too large".
 bool parse_real(const std::string &text, const std::string &name, Rational &out,
                 std::string &error);
 

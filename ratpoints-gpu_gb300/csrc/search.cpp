@@ -80,88 +80,110 @@ void require_cuda(cudaError_t status, const char *operation) {
 
 }  // namespace
 
-bool SearchOptions::accepts(long long numerator, long long denominator) const {
-    if (intervals.empty()) return true;
-    for (const auto &iv : intervals) {
-        // compare_fraction gives sign(numerator/denominator - bound)
-        bool above = iv.lower_infinite || iv.lower.compare_fraction(numerator, denominator) >= 0;
-        bool below = iv.upper_infinite || iv.upper.compare_fraction(numerator, denominator) <= 0;
-        if (above && below) return true;
+namespace {
+
+// numerator/denominator inside the closed interval (an infinite end always holds).
+bool inside(const SearchInterval &iv, long long numerator, long long denominator) {
+    // compare_fraction gives sign(numerator/denominator - bound)
+    if (!iv.lower_infinite && iv.lower.compare_fraction(numerator, denominator) < 0) return false;
+    return iv.upper_infinite || iv.upper.compare_fraction(numerator, denominator) <= 0;
+}
+
+[[noreturn]] void bad_devices(const char *why) { throw std::invalid_argument(why); }
+
+// One GPU ordinal of a --devices list: decimal digits only, at most INT_MAX.
+int device_ordinal(const std::string &token) {
+    long long value = 0;
+    for (char c : token) {
+        if (c < '0' || c > '9') bad_devices("--devices requires all or comma-separated nonnegative GPU IDs");
+        value = value * 10 + (c - '0');
+        if (value > std::numeric_limits<int>::max())
+            bad_devices("--devices requires all or comma-separated nonnegative GPU IDs");
     }
-    return false;
+    return int(value);
+}
+
+GpuDevice query_device(int ordinal) {
+    cudaDeviceProp prop{};
+    require_cuda(cudaGetDeviceProperties(&prop, ordinal), "cudaGetDeviceProperties");
+    char bus[32] = {};
+    require_cuda(cudaDeviceGetPCIBusId(bus, int(sizeof bus), ordinal), "cudaDeviceGetPCIBusId");
+    GpuDevice g;
+    g.id = ordinal;
+    g.name = prop.name;
+    g.major = prop.major;
+    g.minor = prop.minor;
+    g.multiprocessors = prop.multiProcessorCount;
+    g.memory_bytes = (unsigned long long)prop.totalGlobalMem;
+    g.pci_bus_id = bus;
+    return g;
+}
+
+}  // namespace
+
+bool SearchOptions::accepts(long long numerator, long long denominator) const {
+    return intervals.empty() ||
+           std::any_of(intervals.begin(), intervals.end(),
+                       [&](const SearchInterval &iv) { return inside(iv, numerator, denominator); });
 }
 
 double SearchMetrics::initial_mask_gbs() const {
-    if (sieve_ms == 0.0) return 0.0;
-    return double(initial_mask_bytes / ((long double)sieve_ms * 1.0e6L));
+    // bytes of the reference's 14 first-stage masks per word, per millisecond of sieve time
+    return sieve_ms > 0.0 ? double(initial_mask_bytes / ((long double)sieve_ms * 1.0e6L)) : 0.0;
 }
 
+// --devices: "all" (every visible GPU, returned as an empty list) or ordinals
+// separated by commas.  Tokens are checked left to right: an empty token in
+// the middle, a malformed or too large ordinal, or a repeated one fails where
+// it is met; a list ending in a comma (or an empty text) fails after that.
 std::vector<int> parse_device_selection(const std::string &text) {
     if (text == "all") return {};
-    std::vector<int> ids;
-    std::size_t start = 0;
-    while (start < text.size()) {
-        std::size_t end = text.find(',', start);
-        if (end == std::string::npos) end = text.size();
-        if (end == start) throw std::invalid_argument("empty GPU ID in --devices");
-        int id = 0;
-        for (std::size_t i = start; i < end; ++i) {
-            if (text[i] < '0' || text[i] > '9' ||
-                id > (std::numeric_limits<int>::max() - (text[i] - '0')) / 10)
-                throw std::invalid_argument(
-                    "--devices requires all or comma-separated nonnegative GPU IDs");
-            id = id * 10 + (text[i] - '0');
-        }
-        if (std::find(ids.begin(), ids.end(), id) != ids.end())
-            throw std::invalid_argument("duplicate GPU ID in --devices");
-        ids.push_back(id);
-        start = end + 1;
+    std::vector<int> ordinals;
+    std::size_t begin = 0;
+    for (;;) {
+        const std::size_t comma = text.find(',', begin);
+        const std::size_t end = comma == std::string::npos ? text.size() : comma;
+        if (end == text.size() && begin == end) break;  // nothing after the last comma
+        if (begin == end) bad_devices("empty GPU ID in --devices");
+        const int ordinal = device_ordinal(text.substr(begin, end - begin));
+        if (std::count(ordinals.begin(), ordinals.end(), ordinal))
+            bad_devices("duplicate GPU ID in --devices");
+        ordinals.push_back(ordinal);
+        if (comma == std::string::npos) break;
+        begin = comma + 1;
     }
-    if (ids.empty() || text.back() == ',')
-        throw std::invalid_argument("--devices requires all or a nonempty GPU list");
-    return ids;
+    if (ordinals.empty() || text.back() == ',') bad_devices("--devices requires all or a nonempty GPU list");
+    return ordinals;
 }
 
 std::vector<GpuDevice> available_gpu_devices() {
     int count = 0;
-    cudaError_t status = cudaGetDeviceCount(&count);
+    const cudaError_t status = cudaGetDeviceCount(&count);
     if (status == cudaErrorNoDevice || (status == cudaSuccess && count == 0))
-        throw std::runtime_error(
-            "no visible CUDA devices; check the driver and CUDA_VISIBLE_DEVICES");
+        throw std::runtime_error("no visible CUDA devices; check the driver and CUDA_VISIBLE_DEVICES");
     require_cuda(status, "cudaGetDeviceCount");
     std::vector<GpuDevice> devices;
-    for (int id = 0; id < count; ++id) {
-        cudaDeviceProp prop{};
-        require_cuda(cudaGetDeviceProperties(&prop, id), "cudaGetDeviceProperties");
-        char pci[32] = {};
-        require_cuda(cudaDeviceGetPCIBusId(pci, sizeof pci, id), "cudaDeviceGetPCIBusId");
-        GpuDevice dev;
-        dev.id = id;
-        dev.name = prop.name;
-        dev.major = prop.major;
-        dev.minor = prop.minor;
-        dev.multiprocessors = prop.multiProcessorCount;
-        dev.memory_bytes = (unsigned long long)prop.totalGlobalMem;
-        dev.pci_bus_id = pci;
-        devices.push_back(dev);
-    }
+    devices.reserve(std::size_t(count));
+    for (int ordinal = 0; ordinal < count; ++ordinal) devices.push_back(query_device(ordinal));
     return devices;
 }
 
+// The GPUs a --devices list names, in its order (all visible ones for "all").
 std::vector<GpuDevice> select_gpu_devices(const std::vector<int> &ids) {
-    std::vector<GpuDevice> available = available_gpu_devices();
-    if (ids.empty()) return available;
-    std::vector<GpuDevice> selected;
-    for (int id : ids) {
-        if (id < 0 || std::size_t(id) >= available.size())
+    const std::vector<GpuDevice> visible = available_gpu_devices();
+    if (ids.empty()) return visible;
+    std::vector<GpuDevice> chosen;
+    for (std::size_t k = 0; k < ids.size(); ++k) {
+        const int id = ids[k];
+        if (id < 0 || std::size_t(id) >= visible.size())
             throw std::invalid_argument("GPU ID " + std::to_string(id) +
                                         " is not visible; run --list-devices (IDs are "
                                         "CUDA-visible ordinals)");
-        for (const auto &d : selected)
-            if (d.id == id) throw std::invalid_argument("duplicate GPU ID in selection");
-        selected.push_back(available[std::size_t(id)]);
+        if (std::find(ids.begin(), ids.begin() + std::ptrdiff_t(k), id) != ids.begin() + std::ptrdiff_t(k))
+            throw std::invalid_argument("duplicate GPU ID in selection");
+        chosen.push_back(visible[std::size_t(id)]);
     }
-    return selected;
+    return chosen;
 }
 
 PointSearch::PointSearch(SearchOptions options)

@@ -170,6 +170,9 @@ def load():
     lib.rpg_release_cached_resources.argtypes = [ctypes.c_int32]
     lib.rpg_bounded_wait_selftest.restype = S
     lib.rpg_bounded_wait_selftest.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
+    lib.rpg_smem_read_probe.restype = S
+    lib.rpg_smem_read_probe.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     lib.rpg_cli_main.restype = ctypes.c_int32
     lib.rpg_cli_main.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_char_p)]
     lib.rpg_session_create.restype = S
@@ -422,6 +425,15 @@ def bounded_wait_selftest(polls, arrive, device=0):
     """Runs the bounded mbarrier wait self-test; raises RpgError with status
     RPG_E_TIMEOUT (4) when the wait gave up."""
     _check(load().rpg_bounded_wait_selftest(int(device), int(polls), int(bool(arrive))))
+
+
+def smem_read_probe(iterations=4096, device=0):
+    """Shared-memory read rate of the device: dict with gbs (GB/s),
+    bytes_per_clock_per_sm and ms of the timed launch."""
+    gbs, per_clk, ms = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
+    _check(load().rpg_smem_read_probe(int(device), int(iterations), ctypes.byref(gbs),
+                                      ctypes.byref(per_clk), ctypes.byref(ms)))
+    return {"gbs": gbs.value, "bytes_per_clock_per_sm": per_clk.value, "ms": ms.value}
 
 
 def square_root(coefficients, a, b):

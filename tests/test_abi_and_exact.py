@@ -113,6 +113,16 @@ BAD_ARGS = [
     ["1 0 1", "5", "--devices", "-1"], ["1 0 1", "5", "--devices", "+0"],
     ["1 0 1", "5", "--devices", "99999999999999999999999"], ["1 0 1", "5", "--devices"],
     ["1", "5"], ["1 x 1", "5"], ["1 0 0", "5"], ["1 " + "0 " * 100 + "1", "5"], ["1 -2 1", "5"],
+    ["1 0 1", "5", "--devices", ",0"], ["1 0 1", "5", "--devices", "0,,1"],
+    ["1 0 1", "5", "--devices", "1,1,x"], ["1 0 1", "5", "--devices", "0a"],
+    ["1 0 1", "5", "--devices", "2147483648"], ["1 0 1", "5", "--devices", "0,x,"],
+    ["1 0 1", "5", "-l", ".e99999"], ["1 0 1", "5", "-l", "1e"], ["1 0 1", "5", "-l", "1e+"],
+    ["1 0 1", "5", "-l", "--"], ["1 0 1", "5", "-u", "."], ["1 0 1", "5", "-l", "e5"],
+    ["1 0 1", "5", "-l", "1.5.3"], ["1 0 1", "5", "-l", "1", "-u", "0.5e0"],
+    ["1 0 1", "5", "-l", "1e99999x"], ["1 0 1", "5", "-l", "1", "-l"], ["1 0 1", "5", "-l"],
+    ["1 0 1", "5", "-f"], ["1 0 1", "5 "], ["+ 1", "5"], ["1 0 -0", "5"], ["1 0 +00", "5"],
+    ["1 0 1", "5", "-dl", "3", "-du", "2"], ["1 0 1", "5", "--square-denominators", "-dl", "46341"],
+    ["1 0 1", "5", "-l", "-1", "-u", "1e4", "-u", "2e4"],
 ]
 
 

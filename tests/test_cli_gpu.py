@@ -28,7 +28,8 @@ OPTIONS = [[], ["-i"], ["-y"], ["-z"], ["-1"], ["-i", "-1"],
            ["-f", "%x,%y,%z", "-fs", "[", "-fm", ";", "-fe", "]"], ["-f", "--devices"],
            ["-i", "-I", "-y", "-Y"], ["-z", "-fs", "S", "-fe", "E\\n"], ["-y", "-f", "%x %y %q %%\\%\\t|"],
            ["-l", "-3/2"][:0] + ["-u", "-0.5"], ["-l", "0.25"], ["-s", "-k", "-K", "-j", "-J", "-q"],
-           ["-Z", "-z", "-1"], ["-fm", "\\n--\\n", "-i"]]
+           ["-Z", "-z", "-1"], ["-fm", "\\n--\\n", "-i"],
+           ["-f", "%\\%x%", "-fs", "\\%a\\q\\", "-fe", "%"], ["-y", "-f", "%y%x\\\\%z\\"]]
 
 
 @pytest.mark.parametrize("option", OPTIONS, ids=[" ".join(o) or "default" for o in OPTIONS])
