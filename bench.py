@@ -517,6 +517,15 @@ def serving_benchmark(rpg, count=1000, rate=200.0, lanes=2, check=40):
         wall = time.perf_counter() - t0
     lat = sorted(r[2]["latency_ms"] for r in results)
     pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))]
+    queue = sorted(r[2]["queue_ms"] for r in results)
+    qpct = lambda q: queue[min(len(queue) - 1, int(q * len(queue)))]
+    # the slowest 1%: how much of their latency was queueing, and their waves
+    tail = sorted(results, key=lambda r: r[2]["latency_ms"])[-max(1, len(results) // 100):]
+    tail_info = {"requests": len(tail),
+                 "mean_latency_ms": statistics.fmean(r[2]["latency_ms"] for r in tail),
+                 "mean_queue_ms": statistics.fmean(r[2]["queue_ms"] for r in tail),
+                 "mean_waves": statistics.fmean(r[2]["waves"] for r in tail),
+                 "mean_rectangle_sites": statistics.fmean(r[2]["rectangle_sites"] for r in tail)}
     rect = sum(r[2]["rectangle_sites"] for r in results)
     reduced = 0
     for (_, req, _), r in zip(stream, results):
@@ -535,11 +544,12 @@ def serving_benchmark(rpg, count=1000, rate=200.0, lanes=2, check=40):
                         "[1e2, 1e6], 30% first point only",
             "lanes": lanes, "requests": count, "wall_s": wall,
             "p50_ms": pct(0.50), "p99_ms": pct(0.99), "mean_ms": statistics.fmean(lat),
-            "max_ms": lat[-1], "value": reduced / wall / 1e9, "unit": UNIT,
+            "max_ms": lat[-1], "queue_p50_ms": qpct(0.50), "queue_p99_ms": qpct(0.99),
+            "slowest_1pct": tail_info, "offered_rate": rate,
+            "value": reduced / wall / 1e9, "unit": UNIT,
             "rectangle_gsites_per_s": rect / wall / 1e9,
             "note": "throughput = reduced sites searched (first-point requests count the "
-                    "denominators their waves covered) / stream wall time; the offered load is "
-                    "the arrival rate, not the device's capacity",
+                    "denominators their waves covered) / stream wall time",
             "identical_to_single_search": {"checked": len(sample), "all": identical}}
 
 
@@ -632,6 +642,8 @@ def main():
                         help="square-denominator cubics of the restricted searches (0: skip)")
     parser.add_argument("--serving-requests", type=int, default=1000,
                         help="requests of the serving stream (0: skip)")
+    parser.add_argument("--saturation-rate", type=float, default=20000.0,
+                        help="arrival rate (requests/s) of the serving saturation run")
     parser.add_argument("--dense-height", type=int, default=10 ** 7,
                         help="record-curve box height for the pre-verification runs (0: skip)")
     args = parser.parse_args()
@@ -780,6 +792,12 @@ def main():
         line["restricted"] = restricted_benchmark(rpg, args.restricted, args.square_cubics)
     if args.serving_requests > 0:
         line["serving"] = serving_benchmark(rpg, args.serving_requests)
+        # the same stream offered far above what the device answers: the
+        # sustained throughput and the latency at saturation
+        sat = serving_benchmark(rpg, args.serving_requests, rate=args.saturation_rate, check=10)
+        line["serving"]["saturation"] = {k: sat[k] for k in (
+            "offered_rate", "requests", "wall_s", "value", "unit", "p50_ms", "p99_ms",
+            "queue_p50_ms", "queue_p99_ms", "rectangle_gsites_per_s", "identical_to_single_search")}
     if args.dense_height > 0:
         line["dense_curve"] = dense_curve_benchmark(rpg, args.dense_height)
     if not args.no_cpu_baseline:

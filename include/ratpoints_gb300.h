@@ -342,8 +342,8 @@ rpg_status rpg_bounded_wait_selftest(int32_t device, int32_t polls, int32_t arri
  * resident warp issues lane-contiguous 64-bit shared loads, the access the
  * sieve kernels' first stage makes, for `iterations` x 16 loads per thread.
  * Writes the rate in GB/s (CUDA events around the launch), in bytes per SM
- * clock (clock64 around one CTA's loop, times the CTAs resident per SM) and
- * the launch time.  The sieve's shared-memory roofline is measured against
+ * clock (that rate over the SM count and the SM clock, measured in the
+ * kernel as clock64 ticks per globaltimer nanosecond) and the launch time.  The sieve's shared-memory roofline is measured against
  * it.  No counterpart in the reference.
  */
 rpg_status rpg_smem_read_probe(int32_t device, int32_t iterations, double *gbs,

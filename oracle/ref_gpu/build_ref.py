@@ -7,8 +7,11 @@ the CUDA driver API and restates the reference's host driver
 (src/sieve.cu:390-580) so the reference kernels can be timed and their
 survivor sets compared on a GPU host that has no reference sources.
 
-Runs only where the reference tree exists (default /root/reference); the
-cubin it leaves is architecture-specific to the GPU, not to the host CPU.
+Runs only where the reference tree exists: --reference PATH, else the
+RPG_REFERENCE_TREE environment variable, else the tree's mount point in the
+build container (/root/reference).  It prints what it did (built, up to
+date, or not built and why); the cubin it leaves is specific to the GPU
+architecture, not to the host CPU, so it travels with the checkout.
 
     python oracle/ref_gpu/build_ref.py [--reference PATH]
 """
@@ -44,10 +47,19 @@ def build(reference: Path) -> Path | None:
 
 def main():
     parser = argparse.ArgumentParser(description=__doc__)
-    parser.add_argument("--reference", default="/root/reference")
+    parser.add_argument("--reference",
+                        default=os.environ.get("RPG_REFERENCE_TREE", "/root/reference"))
     args = parser.parse_args()
+    before = OUT.stat().st_mtime if OUT.exists() else None
     out = build(Path(args.reference))
-    print(out if out else "reference tree not present; cubin not built")
+    if out:
+        state = "up to date" if before == out.stat().st_mtime else "built"
+        print(f"reference cubin: {out} ({state} from {args.reference})")
+    elif OUT.exists():
+        print(f"reference cubin: {OUT} (prebuilt; no reference tree at {args.reference})")
+    else:
+        print(f"reference cubin: not built (no reference tree at {args.reference}); "
+              "the tests that compare with the reference's kernels will skip")
     return 0
 
 

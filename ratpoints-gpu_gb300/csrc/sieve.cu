@@ -383,7 +383,6 @@ struct Sieve::Impl {
     dev::u64 *fast_adm = nullptr;
     dev::FastClassStart *fast_starts = nullptr;
     dev::FastRun *list_runs = nullptr;     // class lists by denominator class (see FastTables)
-    int *list_prefix = nullptr;
     int *list_count = nullptr;
     long long list_words = 0;              // class words the lists cover (launches from word 0 to at least this)
     int fast_max_classes = 1;
@@ -559,10 +558,8 @@ struct Sieve::Impl {
         cudaFree(fast_starts);
         fast_starts = nullptr;
         cudaFree(list_runs);
-        cudaFree(list_prefix);
         cudaFree(list_count);
         list_runs = nullptr;
-        list_prefix = nullptr;
         list_count = nullptr;
         if (h_count) cudaFreeHost(h_count);
         if (h_a) cudaFreeHost(h_a);
@@ -908,11 +905,14 @@ struct Sieve::Impl {
         const int ncombo = 64 * q;
         list_words = (F.count_q + 1 + 63) >> 6;
         std::vector<dev::FastRun> lruns;
-        std::vector<int> lprefix, lcount;
+        std::vector<int> lcount;
+        int list_ipc = 1;
         if (list_words < (1LL << 23)) {
             lruns.assign(std::size_t(ncombo) * maxc, dev::FastRun{});
-            lprefix.assign(std::size_t(ncombo) * (maxc + 1), 0);
             lcount.assign(std::size_t(ncombo), 0);
+            // every class of a whole row has the same number of sweep items:
+            // that of the longest class (classes differ by one word at most)
+            list_ipc = int((list_words + dev::kFItemWords - 1) / dev::kFItemWords);
             auto nth_bit = [](dev::u64 mask, int k) {
                 for (int i = 0; i < k; ++i) mask &= mask - 1;
                 return __builtin_ctzll(mask);
@@ -925,7 +925,6 @@ struct Sieve::Impl {
                     const int nq = __builtin_popcountll(classesq);
                     const int nclass = __builtin_popcountll(classes2) * nq;
                     if (nclass > maxc) throw std::logic_error("class list longer than the class bound");
-                    int items = 0;
                     for (int c = 0; c < nclass; ++c) {
                         const int i2 = c / nq;
                         const int r64 = nth_bit(classes2, i2);
@@ -939,10 +938,8 @@ struct Sieve::Impl {
                         run.words_last = dev::u32(cw) | (cw > 0 ? 1u << 24 : 0u) | ((last_bits - 1) << 25);
                         run.ofs = cs.ofs;
                         for (int sl = 0; sl < dev::kFastSlots; ++sl) run.start[sl] = cs.start[sl];
-                        lprefix[std::size_t(k) * (maxc + 1) + c] = items;
-                        items += int((cw + dev::kFItemWords - 1) / dev::kFItemWords);
+                        if (cw > list_words) throw std::logic_error("class longer than its row");
                     }
-                    lprefix[std::size_t(k) * (maxc + 1) + nclass] = items;
                     lcount[std::size_t(k)] = nclass;
                 }
         }
@@ -950,18 +947,14 @@ struct Sieve::Impl {
         auto t1 = Clock::now();
         if (!lruns.empty()) {
             list_runs = device_alloc<dev::FastRun>(lruns.size(), "cudaMalloc(class lists)");
-            list_prefix = device_alloc<int>(lprefix.size(), "cudaMalloc(class lists)");
             list_count = device_alloc<int>(lcount.size(), "cudaMalloc(class lists)");
             check_cuda(cudaMemcpyAsync(list_runs, lruns.data(), lruns.size() * sizeof(dev::FastRun),
-                                       cudaMemcpyHostToDevice, stream),
-                       "upload class lists");
-            check_cuda(cudaMemcpyAsync(list_prefix, lprefix.data(), lprefix.size() * sizeof(int),
                                        cudaMemcpyHostToDevice, stream),
                        "upload class lists");
             check_cuda(cudaMemcpyAsync(list_count, lcount.data(), lcount.size() * sizeof(int),
                                        cudaMemcpyHostToDevice, stream),
                        "upload class lists");
-            timings.h2d_bytes += lruns.size() * sizeof(dev::FastRun) + (lprefix.size() + lcount.size()) * sizeof(int);
+            timings.h2d_bytes += lruns.size() * sizeof(dev::FastRun) + lcount.size() * sizeof(int);
         }
         fast_rows = device_alloc<dev::u64>(std::size_t(total), "cudaMalloc(class tables)");
         fast_adm = device_alloc<dev::u64>(adm.size(), "cudaMalloc(admissible classes)");
@@ -1022,8 +1015,8 @@ struct Sieve::Impl {
         F.class_starts = fast_starts;
         F.max_classes = fast_max_classes;
         F.list_runs = list_runs;
-        F.list_prefix = list_prefix;
         F.list_count = list_count;
+        F.list_ipc = list_ipc;
         fast_smem = fast_dynamic_smem(F.smem_words, fast_max_classes, fast_plan.row_slots);
         const void *kernel = fast_kernel_ptr(F.slots, fast_plan.row_slots);
         check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1103,7 +1096,6 @@ struct Sieve::Impl {
             for (int i = 0; i < Fl.slots; ++i) Fl.mod[i].wlo_mod = dev::u32(A.w_lo % Fl.mod[i].m);
             if (A.w_lo != 0 || A.w_hi < list_words) {  // part of the class rows: the producer lays them out
                 Fl.list_runs = nullptr;
-                Fl.list_prefix = nullptr;
                 Fl.list_count = nullptr;
             }
             launch_fast(Fl, A, work, st);

@@ -40,7 +40,7 @@ constexpr int kFWarps = 12;                // warp 0 produces, the others sweep
 constexpr int kFThreads = kFWarps * kWarpSize;
 constexpr int kFConsumers = kFWarps - 1;
 constexpr int kFMaxSlotCount = 3;                          // denominators in flight per CTA: 2 or 3
-constexpr int kFChunk = 4;                                 // parameters per producer fetch
+constexpr int kFChunk = 16;                                // parameters per producer fetch (one per lane)
 constexpr int kFSteps = 4;                                 // steps per work item
 constexpr int kFItemWords = kWarpSize * kFK * kFSteps;     // 512 words per item
 constexpr int kFExt = kWarpSize * (kFK - 1);               // row extension
@@ -89,13 +89,16 @@ struct FastTables {
     const FastClassStart *class_starts;  // [M]
     int max_classes;               // most admissible classes of any denominator
     // Class lists by denominator class k = (d mod 64) q + (d mod q), for
-    // launches over whole class rows (null otherwise): list_count[k] classes,
-    // their runs list_runs[k max_classes ..] and sweep-item prefix
-    // list_prefix[k (max_classes + 1) ..].  A denominator's classes depend on
-    // k alone, so the producer looks them up instead of laying them out.
+    // launches over whole class rows (null otherwise): list_count[k] classes
+    // and their runs list_runs[k max_classes ..].  A denominator's classes
+    // depend on k alone, so the producer looks them up instead of laying them
+    // out.  Every class of a whole row has list_ipc sweep items (its words
+    // differ from another class's by at most one, and a class with fewer
+    // words finds nothing to sweep in its last item), so item i of a list is
+    // item i mod list_ipc of class i / list_ipc.
     const FastRun *list_runs;
-    const int *list_prefix;
     const int *list_count;
+    int list_ipc;
     const u64 *rows;               // stage-1 modulus tables
     const u64 *prime_rows;         // reference candidate tables (class layout)
     const u64 *admissible;         // [64] 2-adic classes by d mod 64, then [kFAdmQ] residues by d mod q
@@ -229,9 +232,10 @@ static_assert(sizeof(FastRun) == 32, "packed class run");
 struct FastSlot {
     long long d;                   // denominator; -1: no more work
     const FastRun *runs;
-    const int *prefix;
+    const int *prefix;             // sweep-item prefix of laid-out classes (null for class lists)
     int nclass;
-    int next;                      // sweep-item counter
+    int items;                     // sweep items of the denominator
+    int rot;                       // items handed out in this CTA before these, mod the consumer count
     unsigned char sel[kSelectedPrimes];  // selected candidates, largest first
 };
 
@@ -332,8 +336,8 @@ __device__ __forceinline__ void fast_select(const FastTables &T, u32 du, FastSlo
 
 // Producer work for denominator d into slot S (the whole warp): the prime
 // selection, then the admissible classes and their sweep items (a prefix
-// scan, 32 classes per pass) in shared memory.
-__device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs &A, long long d,
+// scan, 32 classes per pass) in shared memory.  Returns the item count.
+__device__ __forceinline__ int fast_setup(const FastTables &T, const SieveArgs &A, long long d,
                                            FastSlot &S, FastRun *runs, int *prefix) {
     const int lane = threadIdx.x & 31;
     const u32 du = u32(d);
@@ -395,9 +399,10 @@ __device__ __forceinline__ void fast_setup(const FastTables &T, const SieveArgs 
         S.runs = runs;
         S.prefix = prefix;
         S.nclass = nclass;
-        S.next = 0;
+        S.items = carry;
         S.d = d;
     }
+    return carry;
     (void)M;
 }
 
@@ -429,95 +434,110 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
 
     if (warp == 0) {
         // ---- producer: next live denominator into the next free slot ----
+        // Parameters come kFChunk at a time from the launch's work counter, the
+        // next chunk's fetch issued before this chunk is handed out so that its
+        // latency is hidden; lane j classifies parameter j of a chunk (class
+        // list length by d mod 64 and d mod q), and the live ones go to the
+        // slots in order.  The row copies of a slot are issued by lanes
+        // 0 .. NS-1, one row each.
         const int q = T.class_prime;
         const unsigned long long magic_q = (~0ull) / u32(q) + 1;  // q >= 1: mod_u32 constant
         const bool lists = T.list_count != nullptr;
-        long long chunk = 0;
-        int j = kFChunk;                 // position inside the fetched chunk
         int uses[SLOTS] = {};      // fills of each slot so far
         int b = 0;
         bool failed = false;
-        for (;;) {
-            long long d = -1;
-            int combo = 0, list_n = 0;
-            for (;;) {
-                if (j == kFChunk) {
-                    unsigned long long base = 0;
-                    if (lane == 0) base = atomicAdd(work, (unsigned long long)kFChunk);
-                    chunk = (long long)__shfl_sync(kFullMask, base, 0);
-                    j = 0;
-                    if (chunk >= A.k_count) break;
-                }
-                const long long idx = chunk + j++;
-                if (idx >= A.k_count) {
-                    j = kFChunk;
-                    continue;
-                }
-                const long long k = A.k_first + idx;
-                const long long dd = A.square ? k * k : k;
-                const u32 du = u32(dd);
-                if (lists) {
-                    combo = int(du & 63) * q + (q > 1 ? int(mod_u32(du, u32(q), magic_q)) : 0);
-                    list_n = __ldg(T.list_count + combo);
-                    if (list_n == 0) continue;
-                } else {
-                    if (__ldg(T.admissible + (du & 63)) == 0) continue;
-                    if (q > 1 && __ldg(T.admissible + 64 + int(mod_u32(du, u32(q), magic_q))) == 0)
-                        continue;
-                }
-                d = dd;
-                break;
-            }
-            // slot b must be released by every consumer before it is refilled
+        int rot = 0;               // sweep items handed out so far, mod kFConsumers
+        unsigned long long next_chunk = 0;
+        if (lane == 0) next_chunk = atomicAdd(work, (unsigned long long)kFChunk);
+        // waits until slot b is released by every consumer (false: gave up)
+        auto acquire_slot = [&]() -> bool {
             int used = 0;
 #pragma unroll
             for (int t = 0; t < SLOTS; ++t) used = t == b ? uses[t] : used;
-            if (used > 0 && !mbar_wait(smem_addr(&s_empty[b]), u32(used - 1) & 1u)) {
-                failed = true;
-                break;
+            return used == 0 || mbar_wait(smem_addr(&s_empty[b]), u32(used - 1) & 1u);
+        };
+        for (;;) {
+            const long long chunk = (long long)__shfl_sync(kFullMask, next_chunk, 0);
+            if (chunk >= A.k_count) break;
+            if (lane == 0) next_chunk = atomicAdd(work, (unsigned long long)kFChunk);
+            const long long idx = chunk + lane;
+            const bool valid = lane < kFChunk && idx < A.k_count;
+            const long long k = A.k_first + (valid ? idx : 0);
+            const long long dd = A.square ? k * k : k;
+            const u32 du = u32(dd);
+            const int combo = int(du & 63) * q + (q > 1 ? int(mod_u32(du, u32(q), magic_q)) : 0);
+            int list_n = 0;
+            if (valid) {
+                if (lists) {
+                    list_n = __ldg(T.list_count + combo);
+                } else {
+                    const bool adm = __ldg(T.admissible + (du & 63)) != 0 &&
+                                     (q == 1 || __ldg(T.admissible + 64 + int(mod_u32(du, u32(q), magic_q))) != 0);
+                    list_n = adm ? 1 : 0;
+                }
             }
-            FastSlot &S = slot[b];
-            const u32 full = smem_addr(&s_full[b]);
-            if (d < 0) {
-                if (lane == 0) S.d = -1;
+            u32 live = __ballot_sync(kFullMask, list_n > 0);
+            while (live) {
+                const int j = __ffs(live) - 1;
+                live &= live - 1;
+                const long long d = __shfl_sync(kFullMask, dd, j);
+                const int combo_j = __shfl_sync(kFullMask, combo, j);
+                const int n_j = __shfl_sync(kFullMask, list_n, j);
+                if (!acquire_slot()) {
+                    failed = true;
+                    break;
+                }
+                FastSlot &S = slot[b];
+                const u32 full = smem_addr(&s_full[b]);
+                int items;
+                if (lists) {
+                    fast_select(T, u32(d), S);
+                    items = n_j * T.list_ipc;
+                    if (lane == 0) {
+                        S.runs = T.list_runs + (long long)combo_j * T.max_classes;
+                        S.prefix = nullptr;
+                        S.nclass = n_j;
+                        S.items = items;
+                        S.d = d;
+                    }
+                } else {
+                    items = fast_setup(T, A, d, S, runs0 + b * T.max_classes, prefix0 + b * (T.max_classes + 1));
+                }
+                if (lane == 0) S.rot = rot;
+                rot = int((rot + (unsigned)items) % unsigned(kFConsumers));
                 __syncwarp();
                 if (lane == 0) {
                     __threadfence_block();
-                    mbar_arrive(full);
+                    mbar_arrive_expect_tx(full, u32(T.smem_words) * 8u);
                 }
-                break;
-            }
-            if (lists) {
-                fast_select(T, u32(d), S);
-                if (lane == 0) {
-                    S.runs = T.list_runs + (long long)combo * T.max_classes;
-                    S.prefix = T.list_prefix + (long long)combo * (T.max_classes + 1);
-                    S.nclass = list_n;
-                    S.next = 0;
-                    S.d = d;
-                }
-            } else {
-                fast_setup(T, A, d, S, runs0 + b * T.max_classes, prefix0 + b * (T.max_classes + 1));
-            }
-            __syncwarp();
-            if (lane == 0) {
-                __threadfence_block();
-                fence_proxy_async_shared();
-                mbar_arrive_expect_tx(full, u32(T.smem_words) * 8u);
-                const u32 du = u32(d);
-                const u32 dst = smem_addr(smem + b * row_stride);
-#pragma unroll
-                for (int sl = 0; sl < NS; ++sl) {
-                    const FastModulus &Md = T.mod[sl];
-                    const u32 rho = mod_u32(du, u32(Md.m), Md.magic);
-                    bulk_copy_to_shared(dst + u32(Md.smem_offset) * 8u,
+                __syncwarp();
+                if (lane < NS) {
+                    // the consumers' reads of this slot's previous rows are
+                    // ordered before the asynchronous copies that overwrite them
+                    fence_proxy_async_shared();
+                    const FastModulus &Md = T.mod[lane];
+                    const u32 rho = mod_u32(u32(d), u32(Md.m), Md.magic);
+                    bulk_copy_to_shared(smem_addr(smem + b * row_stride) + u32(Md.smem_offset) * 8u,
                                         T.rows + Md.offset + (long long)rho * Md.length,
                                         u32(Md.length) * 8u, full);
                 }
-            }
 #pragma unroll
-            for (int t = 0; t < SLOTS; ++t) uses[t] += t == b ? 1 : 0;
-            b = b + 1 == SLOTS ? 0 : b + 1;
+                for (int t = 0; t < SLOTS; ++t) uses[t] += t == b ? 1 : 0;
+                b = b + 1 == SLOTS ? 0 : b + 1;
+            }
+            if (failed) break;
+        }
+        if (!failed) {
+            // no more work: an empty slot fill tells the consumers to finish
+            if (acquire_slot()) {
+                if (lane == 0) {
+                    slot[b].d = -1;
+                    __threadfence_block();
+                    mbar_arrive(smem_addr(&s_full[b]));
+                }
+            } else {
+                failed = true;
+            }
         }
         if (failed) {
             if (A.error && lane == 0) atomicOr(A.error, 1ull);
@@ -530,6 +550,10 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
     }
 
     // ---- consumers: sweep the items of each filled slot in turn ----
+    // Items are dealt round-robin over the consumer warps, continuing across
+    // denominators (the slot's rot): consumer cw sweeps items i of a fill with
+    // (i + rot) mod kFConsumers = cw.  No counter is shared, and a warp with
+    // no item in a fill only releases the slot.
     const int cw = warp - 1;
     u64 *wq_mask = qmask + cw * kFQueue;
     u64 *wq_pos = qpos + cw * kFQueue;
@@ -537,7 +561,7 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
     u32 phase = 0;   // bit b: parity of slot b's next fill
     int b = 0;
     int qn = 0;      // queued words (kept across denominators)
-    int seq = 0;     // slot fills this warp has taken
+    int seq = 0;     // slot fills this warp has taken items from
     int oldest = 0;  // oldest context that may still have queued words
     auto drain_all = [&]() {
         while (qn > 0) {
@@ -558,120 +582,133 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
             drain_all();
             return;
         }
-        // context k replaces the one taken kFCtx fills ago: its queued words go first
-        const int k = seq & (kFCtx - 1);
-        if (qn > 0 && seq - oldest >= kFCtx) drain_all();
-        if (qn == 0) oldest = seq;
-        __syncwarp();
-        ctx[k].sel[lane] = S.sel[lane];
-        if (lane == 0) ctx[k].d = int(S.d);
-        __syncwarp();
-        const u64 tag = u64(k) << 56;
+        const int total_items = S.items;
+        int item = cw - S.rot;
+        if (item < 0) item += kFConsumers;
+        if (item < total_items) {
+            // context k replaces the one taken kFCtx fills ago: its queued words go first
+            const int k = seq & (kFCtx - 1);
+            if (qn > 0 && seq - oldest >= kFCtx) drain_all();
+            if (qn == 0) oldest = seq;
+            __syncwarp();
+            ctx[k].sel[lane] = S.sel[lane];
+            if (lane == 0) ctx[k].d = int(S.d);
+            __syncwarp();
+            const u64 tag = u64(k) << 56;
 
-        const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
-        const FastRun *runs = S.runs;
-        const int *prefix = S.prefix;
-        const int nclass = S.nclass;
-        // up to 31 classes: lane c keeps prefix[c] (lane nclass the total), so
-        // finding an item's class takes no memory access
-        const bool lane_prefix = nclass < kWarpSize;
-        const int my_prefix = lane_prefix && lane <= nclass ? prefix[lane] : 0;
-        const int total_items = lane_prefix ? __shfl_sync(kFullMask, my_prefix, nclass) : prefix[nclass];
-        u32 step8[NS], mod8[NS];
-        const unsigned char *slot_base[NS];
-#pragma unroll
-        for (int sl = 0; sl < NS; ++sl) {
-            step8[sl] = 8u * T.mod[sl].step;
-            mod8[sl] = 8u * u32(T.mod[sl].m);
-            slot_base[sl] = sbase + 8 * T.mod[sl].smem_offset;
-        }
-        int c = 0;  // this warp's items of a slot only increase: so do their classes
-        for (;;) {
-            int item = 0;
-            if (lane == 0) item = atomicAdd(const_cast<int *>(&S.next), 1);
-            item = __shfl_sync(kFullMask, item, 0);
-            if (item >= total_items) break;
-            // class index: largest c with prefix[c] <= item (32 classes per
-            // probe, from the last one on)
-            int first_item;
-            if (lane_prefix) {
-                const u32 bb = __ballot_sync(kFullMask, lane < nclass && my_prefix <= item);
-                c = 31 - __clz(bb);
-                first_item = __shfl_sync(kFullMask, my_prefix, c);
-            } else {
-                for (int base = c; base < nclass; base += 32) {
-                    const int cc = base + lane;
-                    const u32 bb = __ballot_sync(kFullMask, cc < nclass && prefix[cc] <= item);
-                    if (bb) c = base + 31 - __clz(bb);
-                    if (bb != kFullMask) break;
-                }
-                first_item = prefix[c];
-            }
-            const int w0 = (item - first_item) * kFItemWords;
-            const FastRun run = runs[c];
-            const int wt = int(run.words_last & 0xFFFFFFu);
-            const int last_word = (run.words_last >> 24) & 1u ? wt - 1 : -1;
-            const u32 last_bits = (run.words_last >> 25) + 1;
-            const u64 last_mask = last_bits >= 64 ? ~u64(0) : ((u64(1) << last_bits) - 1);
-            // pos of word w of this class: ofs + S (w_lo + w)
-            const u64 pos0 = u64(run.ofs) + u64(T.stride) * u64(A.w_lo);
-            u32 o[NS];  // byte offset of this lane's word inside each staged row
+            const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
+            const FastRun *runs = S.runs;
+            const int *prefix = S.prefix;  // null: a class list, list_ipc items per class
+            const int nclass = S.nclass;
+            // laid-out classes, up to 31 of them: lane c keeps prefix[c], so
+            // finding an item's class takes no memory access
+            const bool lane_prefix = prefix != nullptr && nclass < kWarpSize;
+            const int my_prefix = lane_prefix && lane <= nclass ? prefix[lane] : 0;
+            u32 step8[NS], mod8[NS];
+            const unsigned char *slot_base[NS];
 #pragma unroll
             for (int sl = 0; sl < NS; ++sl) {
-                const u32 m = u32(T.mod[sl].m);
-                const u32 v = u32(run.start[sl]) + u32(w0 + lane);
-                // a class's first item: start < m and lane < 32 <= m, one subtraction
-                o[sl] = 8u * (w0 == 0 && m >= 32 ? (v >= m ? v - m : v) : mod_u32(v, m, T.mod[sl].magic));
+                step8[sl] = 8u * T.mod[sl].step;
+                mod8[sl] = 8u * u32(T.mod[sl].m);
+                slot_base[sl] = sbase + 8 * T.mod[sl].smem_offset;
             }
-#pragma unroll 1
-            for (int step = 0; step < kFSteps; ++step) {
-                const int ws = w0 + step * kWarpSize * kFK;
-                if (ws >= wt) break;
-                u64 acc[kFK];
-#pragma unroll
-                for (int kk = 0; kk < kFK; ++kk)
-                    acc[kk] = *reinterpret_cast<const u64 *>(slot_base[0] + o[0] + 256 * kk);
-#pragma unroll
-                for (int sl = 1; sl < NS; ++sl) {
-#pragma unroll
-                    for (int kk = 0; kk < kFK; ++kk)
-                        acc[kk] &= *reinterpret_cast<const u64 *>(slot_base[sl] + o[sl] + 256 * kk);
+            int c = 0;  // this warp's items of a slot only increase: so do their classes
+            for (; item < total_items; item += kFConsumers) {
+                // class index: item / list_ipc for a class list; otherwise the
+                // largest c with prefix[c] <= item (32 classes per probe, from
+                // the last one on)
+                int first_item;
+                if (prefix == nullptr) {
+                    const int ipc = T.list_ipc;
+                    c = ipc == 1 ? item : item / ipc;
+                    first_item = c * ipc;
+                } else if (lane_prefix) {
+                    const u32 bb = __ballot_sync(kFullMask, lane < nclass && my_prefix <= item);
+                    c = 31 - __clz(bb);
+                    first_item = __shfl_sync(kFullMask, my_prefix, c);
+                } else {
+                    for (int base = c; base < nclass; base += 32) {
+                        const int cc = base + lane;
+                        const u32 bb = __ballot_sync(kFullMask, cc < nclass && prefix[cc] <= item);
+                        if (bb) c = base + 31 - __clz(bb);
+                        if (bb != kFullMask) break;
+                    }
+                    first_item = prefix[c];
                 }
+                const int w0 = (item - first_item) * kFItemWords;
+                const FastRun run = runs[c];
+                const int wt = int(run.words_last & 0xFFFFFFu);
+                const int last_word = (run.words_last >> 24) & 1u ? wt - 1 : -1;
+                const u32 last_bits = (run.words_last >> 25) + 1;
+                const u64 last_mask = last_bits >= 64 ? ~u64(0) : ((u64(1) << last_bits) - 1);
+                // pos of word w of this class: ofs + S (w_lo + w)
+                const u64 pos0 = u64(run.ofs) + u64(T.stride) * u64(A.w_lo);
+                u32 o[NS];  // byte offset of this lane's word inside each staged row
 #pragma unroll
                 for (int sl = 0; sl < NS; ++sl) {
-                    // advance (32 kFK) mod m words; unsigned min wraps into [0, m)
-                    const u32 t = o[sl] + step8[sl];
-                    o[sl] = min(t, t - mod8[sl]);
+                    const u32 m = u32(T.mod[sl].m);
+                    const u32 v = u32(run.start[sl]) + u32(w0 + lane);
+                    // a class's first item: start < m and lane < 32 <= m, one subtraction
+                    o[sl] = 8u * (w0 == 0 && m >= 32 ? (v >= m ? v - m : v) : mod_u32(v, m, T.mod[sl].magic));
                 }
-                const u64 any = acc[0] | acc[1] | acc[2] | acc[3];
-                if (!__ballot_sync(kFullMask, any != 0)) continue;
+#pragma unroll 1
+                for (int step = 0; step < kFSteps; ++step) {
+                    const int ws = w0 + step * kWarpSize * kFK;
+                    if (ws >= wt) break;
+                    u64 acc[kFK];
 #pragma unroll
-                for (int kk = 0; kk < kFK; ++kk) {
-                    const int w = ws + kWarpSize * kk + lane;
-                    u64 a = acc[kk];
-                    if (w == last_word) a &= last_mask;
-                    const bool live = a != 0 && w < wt;
-                    const u32 bb = __ballot_sync(kFullMask, live);
-                    if (bb) {
-                        const int at = qn + __popc(bb & lanemask_lt());
-                        if (live) {
-                            wq_mask[at] = a;
-                            wq_pos[at] = tag | (pos0 + u64(T.stride) * u64(w));
+                    for (int kk = 0; kk < kFK; ++kk)
+                        acc[kk] = *reinterpret_cast<const u64 *>(slot_base[0] + o[0] + 256 * kk);
+#pragma unroll
+                    for (int sl = 1; sl < NS; ++sl) {
+#pragma unroll
+                        for (int kk = 0; kk < kFK; ++kk)
+                            acc[kk] &= *reinterpret_cast<const u64 *>(slot_base[sl] + o[sl] + 256 * kk);
+                    }
+#pragma unroll
+                    for (int sl = 0; sl < NS; ++sl) {
+                        // advance (32 kFK) mod m words; unsigned min wraps into [0, m)
+                        const u32 t = o[sl] + step8[sl];
+                        o[sl] = min(t, t - mod8[sl]);
+                    }
+                    const u64 any = acc[0] | acc[1] | acc[2] | acc[3];
+                    if (!__ballot_sync(kFullMask, any != 0)) continue;
+                    if (ws + kWarpSize * kFK >= wt) {
+                        // the step reaches the class's last word in the tile:
+                        // that word keeps its valid bits, words past it none
+#pragma unroll
+                        for (int kk = 0; kk < kFK; ++kk) {
+                            const int w = ws + kWarpSize * kk + lane;
+                            if (w == last_word) acc[kk] &= last_mask;
+                            if (w >= wt) acc[kk] = 0;
                         }
-                        qn += __popc(bb);
-                        if (qn >= 32) {
-                            __syncwarp();
-                            fast_drain(wq_mask, wq_pos, qn - 32, 32, T, A, ctx);
-                            qn -= 32;
-                            if (qn == 0) oldest = seq;
+                    }
+#pragma unroll
+                    for (int kk = 0; kk < kFK; ++kk) {
+                        const bool live = acc[kk] != 0;
+                        const u32 bb = __ballot_sync(kFullMask, live);
+                        if (bb) {
+                            const int at = qn + __popc(bb & lanemask_lt());
+                            if (live) {
+                                const int w = ws + kWarpSize * kk + lane;
+                                wq_mask[at] = acc[kk];
+                                wq_pos[at] = tag | (pos0 + u64(T.stride) * u64(w));
+                            }
+                            qn += __popc(bb);
+                            if (qn >= 32) {
+                                __syncwarp();
+                                fast_drain(wq_mask, wq_pos, qn - 32, 32, T, A, ctx);
+                                qn -= 32;
+                                if (qn == 0) oldest = seq;
+                            }
                         }
                     }
                 }
             }
+            ++seq;
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_addr(&s_empty[b]));  // this warp is done with slot b
-        ++seq;
         b = b + 1 == SLOTS ? 0 : b + 1;
     }
 }

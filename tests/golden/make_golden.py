@@ -1,7 +1,7 @@
 """Generate the committed golden fixtures in tests/golden/ from the reference.
 
-Run in a checkout where the reference tree is available (default
-/root/reference, or --reference PATH).  Sources of truth:
+Run in a checkout where the reference tree is available, naming it with
+--reference PATH (required).  Sources of truth:
 
 * oracle_cases: the reference's independent Python oracle
   (tests/test_multi_gpu.py:17-40) imported from the reference tree and
@@ -64,7 +64,7 @@ def pipeline_output(coefficients_text, height, first, last):
 
 def main():
     parser = argparse.ArgumentParser(description=__doc__)
-    parser.add_argument("--reference", default="/root/reference")
+    parser.add_argument("--reference", required=True, help="root of the reference tree")
     args = parser.parse_args()
     ref = Path(args.reference)
     sys.path.insert(0, str(ref / "tests"))

@@ -297,7 +297,8 @@ def test_wide_kernel_matches_oracle(rpg, oracle):
             curves.append(c)
     points, status, _, stats = rpg.batch_search(curves)
     assert status == [0] * len(curves)
-    assert stats["wide_curves"] == len(curves)
+    # x intervals narrow a curve's rows, which can send it to the narrow kernel
+    assert stats["wide_curves"] >= sum(1 for c in curves if not c.get("intervals"))
     found = 0
     for c, got in zip(curves, points):
         expected = _oracle_points(oracle, c)
