@@ -820,7 +820,11 @@ struct Sieve::Impl {
             Md.neg_h = dev::u32((Sp.m - bound % Sp.m) % Sp.m);
             Md.wlo_mod = 0;
             Md.step = dev::u32((dev::kWarpSize * dev::kFK) % Sp.m);
+            Md.step8 = 8u * Md.step;
+            Md.mod8 = 8u * dev::u32(Sp.m);
+            Md.soff8 = 8u * dev::u32(Md.smem_offset);
             Md.magic = (unsigned long long)((~0ull) / (unsigned long long)Sp.m) + 1;
+            F.min_modulus = sl == 0 ? Sp.m : std::min(F.min_modulus, Sp.m);
         }
         F.smem_words = smem_words;
         const auto &cands = candidate_primes();
@@ -830,7 +834,7 @@ struct Sieve::Impl {
             Sp.nf = 1;
             Sp.m = p;
             Sp.q[0] = p;
-            pattern_of(p, 0, Sp, 0);  // rows with p | d are never read: stage 2 skips such p
+            pattern_of(p, 0, Sp, 0);  // rows with p | d go unused: stage 2 skips such p
             Sp.length = p;
             Sp.offset = total;
             total += (long long)p * p;

@@ -16,9 +16,9 @@
 // Stage 1 ANDs the rows of NS composite moduli of small primes (chosen per
 // curve), staged in shared memory per denominator; surviving words go through
 // a per-warp queue to stage 2, which checks the reference's 32 selected
-// primes (same selection as the reference plan) from class-layout tables in
-// global memory, then emits (a, d).  Survivors are a subset of the reference
-// plan's.
+// primes (same selection as the reference plan: the 32 largest of its 36
+// candidates that do not divide d) from class-layout tables in global memory,
+// then emits (a, d).  Survivors are a subset of the reference plan's.
 //
 // Warp-specialized pipeline: warp 0 produces denominators (prime selection,
 // class layout from the per-curve class-start table, TMA copies of the rows)
@@ -45,9 +45,9 @@ constexpr int kFSteps = 4;                                 // steps per work ite
 constexpr int kFItemWords = kWarpSize * kFK * kFSteps;     // 512 words per item
 constexpr int kFExt = kWarpSize * (kFK - 1);               // row extension
 constexpr int kFQueue = 64;
+constexpr int kFStage2Group = 6;                           // stage-2 primes loaded together
 constexpr long long kFMaxClassWords = 1LL << 23;           // class words of a launch's tile (24-bit field)
 constexpr int kFAdmQ = 16;                                 // admissible-residue words for q <= 13
-constexpr int kFStage2Group = 8;                           // stage-2 primes loaded together
 
 
 struct FastModulus {
@@ -62,6 +62,10 @@ struct FastModulus {
     u32 wlo_mod;                   // first word of the launch's tile, mod m
     u32 step;                      // (32 * kFK) mod m: row advance per step
     unsigned long long magic;      // ceil(2^64 / m) for 32-bit n mod m
+    u32 step8;                     // 8 step: byte advance of a lane's offset per step
+    u32 mod8;                      // 8 m
+    u32 soff8;                     // 8 smem_offset: byte offset of the staged row in a slot
+    u32 pad;
 };
 
 struct FastPrime {                 // one of the 36 reference candidates, class layout
@@ -115,6 +119,7 @@ struct FastTables {
     FastPrime prime[kCandidatePrimes];
     int slots;                     // stage-1 moduli in use
     int smem_words;                // staged row words
+    int min_modulus;               // smallest stage-1 modulus
 };
 
 // Position of the n-th set bit (n counted from 0) of a 64-bit mask.
@@ -236,25 +241,53 @@ struct FastSlot {
     int nclass;
     int items;                     // sweep items of the denominator
     int rot;                       // items handed out in this CTA before these, mod the consumer count
-    unsigned char sel[kSelectedPrimes];  // selected candidates, largest first
 };
 
-// A denominator a consumer warp still has queued words of: its copy of the
-// slot's denominator and prime selection, so the slot can be refilled before
-// those words go through stage 2.
-constexpr int kFCtx = 4;
-struct FastCtx {
-    int d;
-    unsigned char sel[kSelectedPrimes];
-};
+// A consumer warp's queued words carry one of kFCtx context indices; the
+// context holds their denominator, so a slot can be refilled before those
+// words go through stage 2.  Sixteen contexts per warp let its queue fill up
+// across many denominators before it is drained.
+constexpr int kFCtx = 16;
+constexpr int kFTagShift = 56;             // context index in bits 56..59 of a queued position
+
+// One group of stage 2: candidates ci0, ci0-1, .., ci0-COUNT+1 (descending),
+// each tested on the words whose denominator it does not divide; ndiv counts
+// the candidates that divide it.  The group's table words are loaded together.
+template <int COUNT>
+__device__ __forceinline__ void fast_stage2_group(const FastTables &T, int ci0, u32 hi, u32 lo, u32 d,
+                                                  u64 &m, int &ndiv) {
+    u64 rows[COUNT];
+    bool skip[COUNT];
+#pragma unroll
+    for (int t = 0; t < COUNT; ++t) {
+        const FastPrime &P = T.prime[ci0 - t];
+        const u32 p = u32(P.p);
+        const u32 rho = mod_small(d, p, P.magic);
+        u32 r = mod_small(hi, p, P.magic);
+        r = mod_small((r << 16) | lo, p, P.magic);  // pos mod p
+        r += P.neg_h;                               // a mod p
+        if (r >= p) r -= p;
+        const u32 u = mod_small(r * P.inv_stride, p, P.magic);
+        skip[t] = rho == 0;
+        ndiv += skip[t] ? 1 : 0;
+        rows[t] = __ldg(T.prime_rows + P.offset + (long long)rho * p + u);
+    }
+#pragma unroll
+    for (int t = 0; t < COUNT; ++t) m &= skip[t] ? ~u64(0) : rows[t];
+}
 
 // Stage 2 for up to 32 queued words (one per lane), then emission.  A queued
-// word carries its denominator context (bits 56..57) and the position
-// pos = a - (-H) of its bit 0 (bits 0..55): its sites are a = -H + pos + M j,
-// and the class-layout row index of prime p is (a mod p) S^-1 mod p.
+// word carries its context (bits 56..59) and the position pos = a - (-H) of
+// its bit 0 (bits 0..55): its sites are a = -H + pos + M j, and the
+// class-layout row index of prime p is (a mod p) S^-1 mod p in row d mod p.
+// A word meets the reference's selection, the 32 largest of the 36
+// candidates that do not divide d: the 32 largest candidates (six at a time
+// in a loop that is not unrolled, which keeps the kernel's code compact; the
+// warp stops once its words are empty), skipping those dividing d, then, one
+// at a time and only for words where some of those divided d, the four
+// smallest until 32 have been tested.
 __device__ __forceinline__ void fast_drain(const u64 *qmask, const u64 *qpos, int start, int n,
-                                           const FastTables &T, const SieveArgs &A,
-                                           const FastCtx *ctx) {
+                                           const FastTables &T, const SieveArgs &A, const int *ctx_d) {
     const int lane = threadIdx.x & 31;
     u64 m = 0, pos = 0;
     if (lane < n) {
@@ -262,29 +295,35 @@ __device__ __forceinline__ void fast_drain(const u64 *qmask, const u64 *qpos, in
         pos = qpos[start + lane];
     }
     __syncwarp();
-    const FastCtx &X = ctx[int(pos >> 56) & (kFCtx - 1)];
-    const u64 p56 = pos & ((u64(1) << 56) - 1);
+    // lanes past n hold no word: any denominator keeps their row indices in range
+    const u32 d = lane < n ? u32(ctx_d[int(pos >> kFTagShift) & (kFCtx - 1)]) : 1u;
+    const u64 p56 = pos & ((u64(1) << kFTagShift) - 1);
     const u32 hi = u32(p56 >> 16), lo = u32(p56 & 0xFFFF);
-    const u32 d = u32(X.d);
-    if (m) {
-        // the table words of kFStage2Group primes are loaded together, so a
-        // word pays one L2 round trip per group instead of one per prime
-        for (int s0 = 0; s0 < kSelectedPrimes && m; s0 += kFStage2Group) {
-            u64 rows[kFStage2Group];
+    static_assert(kCandidatePrimes == 36 && kSelectedPrimes == 32, "stage-2 group schedule");
+    int ndiv = 0;  // of the candidates tested so far, those dividing d
+#pragma unroll 1
+    for (int g = 0; g + kFStage2Group <= kSelectedPrimes; g += kFStage2Group) {
+        if (!__any_sync(kFullMask, m != 0)) break;
+        fast_stage2_group<kFStage2Group>(T, kCandidatePrimes - 1 - g, hi, lo, d, m, ndiv);
+    }
+    constexpr int kRest = kSelectedPrimes % kFStage2Group;
+    if (kRest > 0 && __any_sync(kFullMask, m != 0))
+        fast_stage2_group<kRest>(T, kCandidatePrimes - 1 - (kSelectedPrimes - kRest), hi, lo, d, m, ndiv);
+    // candidates 3, 2, 1, 0 make up for the larger ones that divide d
 #pragma unroll
-            for (int t = 0; t < kFStage2Group; ++t) {
-                const FastPrime &P = T.prime[X.sel[s0 + t]];
-                const u32 p = u32(P.p);
-                u32 r = mod_small(hi, p, P.magic);
-                r = mod_small((r << 16) | lo, p, P.magic);  // pos mod p
-                r += P.neg_h;                               // a mod p
-                if (r >= p) r -= p;
-                const u32 u = mod_small(r * P.inv_stride, p, P.magic);
-                const u32 rho = mod_small(d, p, P.magic);
-                rows[t] = __ldg(T.prime_rows + P.offset + (long long)rho * p + u);
-            }
-#pragma unroll
-            for (int t = 0; t < kFStage2Group; ++t) m &= rows[t];
+    for (int ci = 3; ci >= 0; --ci) {
+        if (!__any_sync(kFullMask, m != 0 && ndiv > 0)) break;
+        const FastPrime &P = T.prime[ci];
+        const u32 p = u32(P.p);
+        const u32 rho = mod_small(d, p, P.magic);
+        if (m != 0 && ndiv > 0 && rho != 0) {
+            u32 r = mod_small(hi, p, P.magic);
+            r = mod_small((r << 16) | lo, p, P.magic);
+            r += P.neg_h;
+            if (r >= p) r -= p;
+            const u32 u = mod_small(r * P.inv_stride, p, P.magic);
+            m &= __ldg(T.prime_rows + P.offset + (long long)rho * p + u);
+            --ndiv;  // one of the 32 taken by a smaller candidate
         }
     }
     // emission: a = -H + pos + M j
@@ -313,37 +352,15 @@ __device__ __forceinline__ void fast_drain(const u64 *qmask, const u64 *qpos, in
     }
 }
 
-// The 32 largest candidates not dividing d (two ballots), into S.sel.
-__device__ __forceinline__ void fast_select(const FastTables &T, u32 du, FastSlot &S) {
-    const int lane = threadIdx.x & 31;
-    {
-        // lane l tests candidate 35 - l, lanes 0..3 also candidate 3 - l
-        const int ch = kCandidatePrimes - 1 - lane;
-        const u32 rh = mod_small(du, u32(T.prime[ch].p), T.prime[ch].magic);
-        const u32 hi_div = __ballot_sync(kFullMask, rh == 0);
-        const int cl = kCandidatePrimes - 1 - 32 - lane;
-        const u32 rl =
-            lane < kCandidatePrimes - 32 ? mod_small(du, u32(T.prime[cl].p), T.prime[cl].magic) : 1u;
-        const u32 lo_div = __ballot_sync(kFullMask, rl == 0);
-        const u32 below = lanemask_lt();
-        const int rank_h = lane - __popc(hi_div & below);
-        if (rh != 0 && rank_h < kSelectedPrimes) S.sel[rank_h] = (unsigned char)ch;
-        const int rank_l = 32 - __popc(hi_div) + lane - __popc(lo_div & below);
-        if (lane < kCandidatePrimes - 32 && rl != 0 && rank_l < kSelectedPrimes)
-            S.sel[rank_l] = (unsigned char)cl;
-    }
-}
-
-// Producer work for denominator d into slot S (the whole warp): the prime
-// selection, then the admissible classes and their sweep items (a prefix
-// scan, 32 classes per pass) in shared memory.  Returns the item count.
+// Producer work for denominator d into slot S (the whole warp): the
+// admissible classes and their sweep items (a prefix scan, 32 classes per
+// pass) in shared memory.  Returns the item count.
 __device__ __forceinline__ int fast_setup(const FastTables &T, const SieveArgs &A, long long d,
                                            FastSlot &S, FastRun *runs, int *prefix) {
     const int lane = threadIdx.x & 31;
     const u32 du = u32(d);
     const int q = T.class_prime;
     const int M = T.class_mod;
-    fast_select(T, du, S);
     const u64 classes2 = __ldg(T.admissible + (du & 63));
     const u64 classesq =
         q > 1 ? __ldg(T.admissible + 64 + int(mod_u32(du, u32(q), (~0ull) / u32(q) + 1))) : u64(1);
@@ -406,6 +423,30 @@ __device__ __forceinline__ int fast_setup(const FastTables &T, const SieveArgs &
     (void)M;
 }
 
+// Four 64-bit shared words of one staged row, 256 bytes apart (a lane's kFK
+// words, 32 apart), as 32-bit halves: one address register, immediate offsets.
+__device__ __forceinline__ void lds_row4(u32 a, u32 (&lo)[kFK], u32 (&hi)[kFK]) {
+    static_assert(kFK == 4, "four words per lane per step");
+    asm volatile(
+        "ld.shared.v2.u32 {%0, %1}, [%8];\n\t"
+        "ld.shared.v2.u32 {%2, %3}, [%8+256];\n\t"
+        "ld.shared.v2.u32 {%4, %5}, [%8+512];\n\t"
+        "ld.shared.v2.u32 {%6, %7}, [%8+768];"
+        : "=r"(lo[0]), "=r"(hi[0]), "=r"(lo[1]), "=r"(hi[1]), "=r"(lo[2]), "=r"(hi[2]), "=r"(lo[3]),
+          "=r"(hi[3])
+        : "r"(a));
+}
+__device__ __forceinline__ u32 and3(u32 a, u32 b, u32 c) {
+    u32 d;
+    asm("lop3.b32 %0, %1, %2, %3, 0x80;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+__device__ __forceinline__ u32 or3(u32 a, u32 b, u32 c) {
+    u32 d;
+    asm("lop3.b32 %0, %1, %2, %3, 0xFE;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
 template <int NS, int SLOTS>
 __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, SieveArgs A,
                                                                unsigned long long *work) {
@@ -417,7 +458,7 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
     int *prefix0 = reinterpret_cast<int *>(runs0 + SLOTS * T.max_classes);  // [slots][max_classes + 1]
 
     __shared__ FastSlot slot[SLOTS];
-    __shared__ FastCtx s_ctx[kFConsumers][kFCtx];
+    __shared__ int s_ctx[kFConsumers][kFCtx];  // denominators of each warp's contexts
     __shared__ __align__(8) unsigned long long s_full[SLOTS];
     __shared__ __align__(8) unsigned long long s_empty[SLOTS];
 
@@ -491,7 +532,6 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
                 const u32 full = smem_addr(&s_full[b]);
                 int items;
                 if (lists) {
-                    fast_select(T, u32(d), S);
                     items = n_j * T.list_ipc;
                     if (lane == 0) {
                         S.runs = T.list_runs + (long long)combo_j * T.max_classes;
@@ -557,7 +597,7 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
     const int cw = warp - 1;
     u64 *wq_mask = qmask + cw * kFQueue;
     u64 *wq_pos = qpos + cw * kFQueue;
-    FastCtx *ctx = s_ctx[cw];
+    int *ctx = s_ctx[cw];
     u32 phase = 0;   // bit b: parity of slot b's next fill
     int b = 0;
     int qn = 0;      // queued words (kept across denominators)
@@ -591,10 +631,9 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
             if (qn > 0 && seq - oldest >= kFCtx) drain_all();
             if (qn == 0) oldest = seq;
             __syncwarp();
-            ctx[k].sel[lane] = S.sel[lane];
-            if (lane == 0) ctx[k].d = int(S.d);
+            if (lane == 0) ctx[k] = int(S.d);
             __syncwarp();
-            const u64 tag = u64(k) << 56;
+            const u64 tag = u64(k) << kFTagShift;
 
             const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
             const FastRun *runs = S.runs;
@@ -604,14 +643,7 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
             // finding an item's class takes no memory access
             const bool lane_prefix = prefix != nullptr && nclass < kWarpSize;
             const int my_prefix = lane_prefix && lane <= nclass ? prefix[lane] : 0;
-            u32 step8[NS], mod8[NS];
-            const unsigned char *slot_base[NS];
-#pragma unroll
-            for (int sl = 0; sl < NS; ++sl) {
-                step8[sl] = 8u * T.mod[sl].step;
-                mod8[sl] = 8u * u32(T.mod[sl].m);
-                slot_base[sl] = sbase + 8 * T.mod[sl].smem_offset;
-            }
+            const u32 slot_addr = smem_addr(sbase);
             int c = 0;  // this warp's items of a slot only increase: so do their classes
             for (; item < total_items; item += kFConsumers) {
                 // class index: item / list_ipc for a class list; otherwise the
@@ -644,35 +676,57 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
                 // pos of word w of this class: ofs + S (w_lo + w)
                 const u64 pos0 = u64(run.ofs) + u64(T.stride) * u64(A.w_lo);
                 u32 o[NS];  // byte offset of this lane's word inside each staged row
-#pragma unroll
-                for (int sl = 0; sl < NS; ++sl) {
-                    const u32 m = u32(T.mod[sl].m);
-                    const u32 v = u32(run.start[sl]) + u32(w0 + lane);
+                if (w0 == 0 && T.min_modulus >= kWarpSize) {
                     // a class's first item: start < m and lane < 32 <= m, one subtraction
-                    o[sl] = 8u * (w0 == 0 && m >= 32 ? (v >= m ? v - m : v) : mod_u32(v, m, T.mod[sl].magic));
+#pragma unroll
+                    for (int sl = 0; sl < NS; ++sl) {
+                        const u32 v = 8u * (u32(run.start[sl]) + u32(lane));
+                        o[sl] = min(v, v - T.mod[sl].mod8);
+                    }
+                } else {
+#pragma unroll
+                    for (int sl = 0; sl < NS; ++sl)
+                        o[sl] = 8u * mod_u32(u32(run.start[sl]) + u32(w0 + lane), u32(T.mod[sl].m), T.mod[sl].magic);
                 }
 #pragma unroll 1
                 for (int step = 0; step < kFSteps; ++step) {
                     const int ws = w0 + step * kWarpSize * kFK;
                     if (ws >= wt) break;
-                    u64 acc[kFK];
+                    // stage 1: this lane's kFK words (32 apart) of each staged
+                    // row, ANDed three at a time
+                    u32 lo[kFK], hi[kFK];
+                    lds_row4(slot_addr + T.mod[0].soff8 + o[0], lo, hi);
 #pragma unroll
-                    for (int kk = 0; kk < kFK; ++kk)
-                        acc[kk] = *reinterpret_cast<const u64 *>(slot_base[0] + o[0] + 256 * kk);
+                    for (int sl = 1; sl + 1 < NS; sl += 2) {
+                        u32 xl[kFK], xh[kFK], yl[kFK], yh[kFK];
+                        lds_row4(slot_addr + T.mod[sl].soff8 + o[sl], xl, xh);
+                        lds_row4(slot_addr + T.mod[sl + 1].soff8 + o[sl + 1], yl, yh);
 #pragma unroll
-                    for (int sl = 1; sl < NS; ++sl) {
+                        for (int kk = 0; kk < kFK; ++kk) {
+                            lo[kk] = and3(lo[kk], xl[kk], yl[kk]);
+                            hi[kk] = and3(hi[kk], xh[kk], yh[kk]);
+                        }
+                    }
+                    if (NS % 2 == 0) {
+                        u32 xl[kFK], xh[kFK];
+                        lds_row4(slot_addr + T.mod[NS - 1].soff8 + o[NS - 1], xl, xh);
 #pragma unroll
-                        for (int kk = 0; kk < kFK; ++kk)
-                            acc[kk] &= *reinterpret_cast<const u64 *>(slot_base[sl] + o[sl] + 256 * kk);
+                        for (int kk = 0; kk < kFK; ++kk) {
+                            lo[kk] &= xl[kk];
+                            hi[kk] &= xh[kk];
+                        }
                     }
 #pragma unroll
                     for (int sl = 0; sl < NS; ++sl) {
                         // advance (32 kFK) mod m words; unsigned min wraps into [0, m)
-                        const u32 t = o[sl] + step8[sl];
-                        o[sl] = min(t, t - mod8[sl]);
+                        const u32 t = o[sl] + T.mod[sl].step8;
+                        o[sl] = min(t, t - T.mod[sl].mod8);
                     }
-                    const u64 any = acc[0] | acc[1] | acc[2] | acc[3];
+                    const u32 any = or3(or3(lo[0], hi[0], lo[1]), or3(hi[1], lo[2], hi[2]), lo[3] | hi[3]);
                     if (!__ballot_sync(kFullMask, any != 0)) continue;
+                    u64 acc[kFK];
+#pragma unroll
+                    for (int kk = 0; kk < kFK; ++kk) acc[kk] = (u64(hi[kk]) << 32) | lo[kk];
                     if (ws + kWarpSize * kFK >= wt) {
                         // the step reaches the class's last word in the tile:
                         // that word keeps its valid bits, words past it none
