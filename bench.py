@@ -592,6 +592,9 @@ def summary(line):
     rs = line.get("restricted") or {}
     if rs:
         out["restricted_identical"] = all(v.get("points_identical") for v in rs.values())
+    at = line.get("autotune") or {}
+    if at:
+        out["autotune"] = {name: t["chosen"] for name, t in at.items()}
     cb = line.get("cpu_baseline") or {}
     if cb:
         out["cpu_baseline"] = {"value": r(cb.get("value")), "kind": cb.get("kind"),
@@ -630,6 +633,8 @@ def main():
                         help="untimed searches through rpg_point_search before them")
     parser.add_argument("--cpu-seconds", type=float, default=12.0)
     parser.add_argument("--no-cpu-baseline", action="store_true")
+    parser.add_argument("--tune", action=argparse.BooleanOptionalAction, default=True,
+                        help="time the fast plan's candidate shapes first and use the fastest")
     parser.add_argument("--batch-curves", type=int, default=4096,
                         help="curves of the mixed batch (0: skip the batch measurement)")
     parser.add_argument("--batch-plain-curves", type=int, default=4096,
@@ -668,6 +673,18 @@ def main():
     rpg.load()
     coeffs = c2_curve()
     last = args.denominators
+    tuning = None
+    if args.tune:
+        # the measured autotuner: candidate shapes of the fast plan timed on a
+        # sample of this workload, the fastest kept in a tuning cache that the
+        # sessions and searches below read (untimed)
+        cache = Path(tempfile.mkdtemp(prefix="rpg_tune_")) / "fast_plan_shapes.json"
+        os.environ["RPG_TUNE_CACHE"] = str(cache)
+        tuning = {"c2": rpg.tune_fast_plan(coeffs, HEIGHT, 1, last, device=local, sample=1 << 17)}
+        if args.record_denominators > 0 or args.dense_height > 0:
+            import workloads
+            tuning["record_curve"] = rpg.tune_fast_plan(workloads.RECORD_CURVE.split(), 10 ** 7, 1, 10 ** 7,
+                                                        device=local, sample=20_000)
     # weak scaling: rank r sieves its own block of `last` denominators
     first_b, last_b = rank_block(rank, last)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
@@ -773,6 +790,12 @@ def main():
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clock,
     }
+    if tuning:
+        line["autotune"] = {name: {"key": t["key"], "chosen": f"{t['rows']} rows x {t['slots']} slots",
+                                   "sample_denominators": t["sample"],
+                                   "candidates_ms": {f"{c['rows']}x{c['slots']}": round(c["ms"], 4)
+                                                     for c in t["candidates"]}}
+                            for name, t in tuning.items()}
     if args.reference_gpu_denominators > 0:
         line["reference_gpu"] = reference_gpu(coeffs, args.reference_gpu_denominators, rpg,
                                               args.reference_gpu_steps)

@@ -159,6 +159,41 @@ typedef struct rpg_fast_plan_info {
 rpg_status rpg_fast_plan(const char *const *coefficients, int32_t coefficient_count, int64_t numerator_bound,
                          rpg_fast_plan_info *plan);
 
+/*
+ * Measured choice of the fast plan's shape: the number of stage-1 rows and
+ * the row slots (2 or 3) per CTA of the single-curve kernel.  Builds the sieve
+ * with the cost model's shape and its neighbours (the other slot count, one
+ * and two rows fewer or more), times each with CUDA events on parameters
+ * [first, first + sample) (clipped to last; flags: RPG_SIEVE_SQUARE_DENOMINATORS),
+ * and reports them with the fastest.  When the environment variable
+ * RPG_TUNE_CACHE names a file, the choice is stored there as JSON, keyed by
+ * the kind of curve (degree, class prime, row length, small- or large-prime
+ * rows), and every later fast-plan sieve of a curve of that kind in a process
+ * with that variable uses it.  No counterpart in the reference, whose kernel
+ * shape is fixed (its tests/tune_cuda.py times build variants).
+ */
+#define RPG_TUNE_MAX_CANDIDATES 8
+typedef struct rpg_tune_report {
+    int32_t rows;                          /* the chosen shape */
+    int32_t slots;
+    int32_t candidates;                    /* shapes timed */
+    int32_t candidate_rows[RPG_TUNE_MAX_CANDIDATES];
+    int32_t candidate_slots[RPG_TUNE_MAX_CANDIDATES];
+    double candidate_ms[RPG_TUNE_MAX_CANDIDATES];
+    double candidate_bits[RPG_TUNE_MAX_CANDIDATES];
+    int64_t sample_denominators;
+    int32_t stored;                        /* 1: written to the RPG_TUNE_CACHE file */
+    char key[96];                          /* the kind of curve, NUL-terminated */
+} rpg_tune_report;
+rpg_status rpg_tune_fast_plan(const char *const *coefficients, int32_t coefficient_count,
+                              int64_t numerator_bound, int32_t first, int32_t last, uint32_t flags,
+                              int32_t device, int64_t sample, rpg_tune_report *report);
+/* The shape a fast-plan sieve of this curve would use (host only): *rows and
+ * *slots of its plan, *from_cache 1 when a stored tuning result decides it
+ * (see rpg_tune_fast_plan), 0 when the cost model does. */
+rpg_status rpg_fast_shape(const char *const *coefficients, int32_t coefficient_count, int64_t numerator_bound,
+                          int32_t *rows, int32_t *slots, int32_t *from_cache);
+
 /* The device pre-verification test of one site, evaluated on the host:
  * *may_be_point = 0 iff gcd(a, d) != 1 or F(a, d) fails a residue test that
  * every square passes (mod 2^64, the primes 3..97, four primes below 2^31).

@@ -31,7 +31,7 @@ EXECUTABLE = BIN_DIR / "ratpoints_gpu"
 
 CUDA_SOURCES = ["sieve.cu", "noalloc.cu", "batch.cu", "preverify.cu", "selftest.cu", "probe.cu"]
 CXX_SOURCES = ["bigint.cpp", "exact.cpp", "plan.cpp", "search.cpp", "cli.cpp", "point_format.cpp", "capi.cpp",
-               "serve.cpp", "compat_sieve.cpp"]
+               "serve.cpp", "compat_sieve.cpp", "tune.cpp"]
 MAIN_SOURCE = "ratpoints_gpu_main.cpp"
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -1,6 +1,8 @@
 // extern "C" entry points of librpgpu (include/ratpoints_gb300.h).
 #include "ratpoints_gb300.h"
 
+#include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -17,6 +19,7 @@
 #include "serve.hpp"
 #include "session.hpp"
 #include "sieve.hpp"
+#include "tune.hpp"
 
 namespace {
 
@@ -237,6 +240,55 @@ rpg_status rpg_fast_plan(const char *const *coefficients, int32_t coefficient_co
         }
         plan->bits = p.bits;
         plan->slots = p.row_slots;
+        return RPG_OK;
+    });
+}
+
+rpg_status rpg_tune_fast_plan(const char *const *coefficients, int32_t coefficient_count,
+                              int64_t numerator_bound, int32_t first, int32_t last, uint32_t flags,
+                              int32_t device, int64_t sample, rpg_tune_report *report) {
+    return guarded([&]() -> rpg_status {
+        std::vector<std::string> coeffs;
+        std::string error;
+        if (!coefficients_from(coefficients, coefficient_count, coeffs, error)) return fail(RPG_E_ARG, error);
+        if (!report) return fail(RPG_E_ARG, "report must not be NULL");
+        if (numerator_bound < 1) return fail(RPG_E_ARG, "maximum height must be positive");
+        if (first < 1 || last < first || sample < 1) return fail(RPG_E_ARG, "invalid denominator range");
+        if ((flags & RPG_SIEVE_SQUARE_DENOMINATORS) && last > 46340)
+            return fail(RPG_E_ARG, "invalid denominator range");
+        const rpg::TuneResult r = rpg::tune_fast_shape(coeffs, numerator_bound, first, last,
+                                                       (flags & RPG_SIEVE_SQUARE_DENOMINATORS) != 0, device,
+                                                       sample);
+        std::memset(report, 0, sizeof *report);
+        report->rows = r.chosen.rows;
+        report->slots = r.chosen.slots;
+        report->candidates = int32_t(std::min<std::size_t>(r.candidates.size(), RPG_TUNE_MAX_CANDIDATES));
+        for (int i = 0; i < report->candidates; ++i) {
+            report->candidate_rows[i] = r.candidates[i].shape.rows;
+            report->candidate_slots[i] = r.candidates[i].shape.slots;
+            report->candidate_ms[i] = r.candidates[i].ms;
+            report->candidate_bits[i] = r.candidates[i].bits;
+        }
+        report->sample_denominators = r.sample;
+        report->stored = r.stored ? 1 : 0;
+        std::snprintf(report->key, sizeof report->key, "%s", r.key.c_str());
+        return RPG_OK;
+    });
+}
+
+rpg_status rpg_fast_shape(const char *const *coefficients, int32_t coefficient_count, int64_t numerator_bound,
+                          int32_t *rows, int32_t *slots, int32_t *from_cache) {
+    return guarded([&]() -> rpg_status {
+        std::vector<std::string> coeffs;
+        std::string error;
+        if (!coefficients_from(coefficients, coefficient_count, coeffs, error)) return fail(RPG_E_ARG, error);
+        if (!rows || !slots || !from_cache) return fail(RPG_E_ARG, "outputs must not be NULL");
+        if (numerator_bound < 1) return fail(RPG_E_ARG, "maximum height must be positive");
+        const rpg::FastShape stored = rpg::tuned_fast_shape(coeffs, numerator_bound);
+        const rpg::FastPlan p = rpg::single_curve_plan(coeffs, numerator_bound, nullptr, stored);
+        *rows = int32_t(p.moduli.size());
+        *slots = p.row_slots;
+        *from_cache = stored.rows > 0 ? 1 : 0;
         return RPG_OK;
     });
 }

@@ -16,6 +16,7 @@
 // survivors into a per-warp queue that a full warp then checks against the
 // remaining 22 primes from L2-resident tables before warp-aggregated emission.
 #include "sieve.hpp"
+#include "tune.hpp"
 
 #include <algorithm>
 #include <chrono>
@@ -329,7 +330,8 @@ long long fast_row_budget(int max_classes, int slots) {
     return (per_cta - (long long)fast_dynamic_smem(0, max_classes, slots)) / (8LL * slots);
 }
 
-FastPlan single_curve_plan(const std::vector<std::string> &coefficients, long long bound, int *max_classes) {
+FastPlan single_curve_plan(const std::vector<std::string> &coefficients, long long bound, int *max_classes,
+                           FastShape shape) {
     // the staged row sets of a CTA, its queues and its slots' class runs must
     // fit shared memory at 2 CTAs/SM.  Three slots stage a denominator ahead
     // further with less shared memory per row set: they pay when sweeping a
@@ -344,7 +346,8 @@ FastPlan single_curve_plan(const std::vector<std::string> &coefficients, long lo
         const long long row_budget = fast_row_budget(classes, slots);
         FastPlan plan;
         for (int cap = kMaxModulus;;) {
-            plan = planner.plan(cap, kMaxFastSlots, row_budget);
+            plan = shape.rows > 0 ? planner.plan(cap, std::min(shape.rows, kMaxFastSlots), row_budget, false)
+                                  : planner.plan(cap, kMaxFastSlots, row_budget);
             int row_words = 0;
             for (int m : plan.moduli) row_words += (m + dev::kFExt + 1) & ~1;
             if (row_words <= row_budget || cap <= 64) break;
@@ -353,6 +356,7 @@ FastPlan single_curve_plan(const std::vector<std::string> &coefficients, long lo
         plan.row_slots = slots;
         return plan;
     };
+    if (shape.rows > 0) return plan_for(shape.slots == dev::kFMaxSlotCount ? dev::kFMaxSlotCount : 2);
     const FastPlan two = plan_for(2);
     if (word_count64(bound) > (1LL << 20)) return two;
     const FastPlan three = plan_for(dev::kFMaxSlotCount);
@@ -647,9 +651,11 @@ struct Sieve::Impl {
         // on a host thread while the streams and buffers are created.
         PlannedRows planned;
         if (opt.plan == PlanKind::fast)
-            planned = std::async(std::launch::async, [&coefficients, h = bound] {
+            planned = std::async(std::launch::async, [&coefficients, h = bound, forced = opt.fast_shape] {
                 int max_classes = 0;
-                FastPlan p = single_curve_plan(coefficients, h, &max_classes);
+                FastShape shape = forced;
+                if (shape.rows <= 0) shape = tuned_fast_shape(coefficients, h);
+                FastPlan p = single_curve_plan(coefficients, h, &max_classes, shape);
                 return std::make_pair(std::move(p), max_classes);
             });
         if (opt.device >= 0) check_cuda(cudaSetDevice(opt.device), "cudaSetDevice");

@@ -33,6 +33,13 @@ public:
 
 void check_cuda(cudaError_t status, const char *what);
 
+// Shape of a fast plan: the number of stage-1 rows and the row slots (2 or 3)
+// each CTA of the single-curve kernel stages.  rows 0: the cost model's choice.
+struct FastShape {
+    int rows = 0;
+    int slots = 0;
+};
+
 struct SieveOptions {
     PlanKind plan = PlanKind::reference;
     bool square = false;            // parameters k give denominators k*k
@@ -42,6 +49,10 @@ struct SieveOptions {
     // (gcd and residue tests; see preverify.hpp).  Deliveries then hold a
     // subset of the modular survivors that still contains every point.
     bool preverify = false;
+    // Fast plan only: a forced shape (rows > 0); otherwise a shape measured
+    // earlier for curves of this kind (tune.hpp), when the tuning cache is
+    // enabled and holds one, else the cost model's.
+    FastShape fast_shape;
 };
 
 // One delivery of survivors.  Pointers stay valid until the next call to
@@ -77,8 +88,11 @@ void release_pooled_pipelines(int device);
 // The fast plan a single-curve sieve uses for a curve and numerator bound
 // (host only): the autotuner's choice under the fast kernel's shared-memory
 // budget; *max_classes (optional) receives the most classes of one denominator.
+// A shape with rows > 0 fixes the row count (the rows filtering most) and the
+// row slots instead of the cost model.
 struct FastPlan;
-FastPlan single_curve_plan(const std::vector<std::string> &coefficients, long long bound, int *max_classes);
+FastPlan single_curve_plan(const std::vector<std::string> &coefficients, long long bound, int *max_classes,
+                           FastShape shape = FastShape{});
 
 // The fast plan a sieve chose for its curve (empty for the reference plan).
 struct FastPlanInfo {

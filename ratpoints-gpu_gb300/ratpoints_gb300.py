@@ -82,6 +82,14 @@ class FastPlanInfo(ctypes.Structure):
                 ("bits", ctypes.c_double), ("slots", ctypes.c_int32)]
 
 
+class TuneReport(ctypes.Structure):
+    _fields_ = [("rows", ctypes.c_int32), ("slots", ctypes.c_int32), ("candidates", ctypes.c_int32),
+                ("candidate_rows", ctypes.c_int32 * 8), ("candidate_slots", ctypes.c_int32 * 8),
+                ("candidate_ms", ctypes.c_double * 8), ("candidate_bits", ctypes.c_double * 8),
+                ("sample_denominators", ctypes.c_int64), ("stored", ctypes.c_int32),
+                ("key", ctypes.c_char * 96)]
+
+
 class BatchStats(ctypes.Structure):
     _fields_ = ([(name, ctypes.c_uint64) for name in
                  ("curves", "wide_curves", "denominators", "survivors", "points", "launches",
@@ -163,6 +171,13 @@ def load():
                                     ctypes.POINTER(ctypes.c_int32)]
     lib.rpg_fast_plan.restype = S
     lib.rpg_fast_plan.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.POINTER(FastPlanInfo)]
+    lib.rpg_tune_fast_plan.restype = S
+    lib.rpg_tune_fast_plan.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.c_uint32, ctypes.c_int32, ctypes.c_int64,
+                                       ctypes.POINTER(TuneReport)]
+    lib.rpg_fast_shape.restype = S
+    lib.rpg_fast_shape.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32),
+                                   ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
     lib.rpg_preverify.restype = S
     lib.rpg_preverify.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
                                   ctypes.POINTER(ctypes.c_int32)]
@@ -404,6 +419,33 @@ def fast_plan(coefficients, bound):
     return {"class_prime": info.class_prime, "moduli": list(info.moduli[:n]),
             "factors": [[f for f in info.factors[i] if f] for i in range(n)], "bits": info.bits,
             "slots": info.slots}
+
+
+def tune_fast_plan(coefficients, bound, first, last, square=False, device=-1, sample=1 << 17):
+    """Times the fast plan's candidate shapes (rpg_tune_fast_plan) and returns
+    {"rows", "slots", "key", "stored", "sample", "candidates": [{"rows",
+    "slots", "ms", "bits"}, ...]}; the choice is kept in the RPG_TUNE_CACHE file
+    when that environment variable is set."""
+    coeffs = coefficients_of(coefficients)
+    r = TuneReport()
+    flags = RPG_SIEVE_SQUARE_DENOMINATORS if square else 0
+    _check(load().rpg_tune_fast_plan(_strings(coeffs), len(coeffs), int(bound), int(first), int(last), flags,
+                                     int(device), int(sample), ctypes.byref(r)))
+    return {"rows": r.rows, "slots": r.slots, "key": r.key.decode(), "stored": bool(r.stored),
+            "sample": r.sample_denominators,
+            "candidates": [{"rows": r.candidate_rows[i], "slots": r.candidate_slots[i],
+                            "ms": r.candidate_ms[i], "bits": r.candidate_bits[i]}
+                           for i in range(r.candidates)]}
+
+
+def fast_shape(coefficients, bound):
+    """(rows, slots, from_cache) of the fast plan a sieve of this curve uses
+    (host only): from_cache is True when a stored tuning result decides it."""
+    coeffs = coefficients_of(coefficients)
+    rows, slots, cached = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
+    _check(load().rpg_fast_shape(_strings(coeffs), len(coeffs), int(bound), ctypes.byref(rows),
+                                 ctypes.byref(slots), ctypes.byref(cached)))
+    return rows.value, slots.value, bool(cached.value)
 
 
 def preverify(coefficients, a, b):
