@@ -94,7 +94,8 @@ struct FastTables {
     int max_classes;               // most admissible classes of any denominator
     // Class lists by denominator class k = (d mod 64) q + (d mod q), for
     // launches over whole class rows (null otherwise): list_count[k] classes
-    // and their runs list_runs[k max_classes ..].  A denominator's classes
+    // and their runs list_runs[k max_classes ..], copied into a slot with its
+    // rows.  A denominator's classes
     // depend on k alone, so the producer looks them up instead of laying them
     // out.  Every class of a whole row has list_ipc sweep items (its words
     // differ from another class's by at most one, and a class with fewer
@@ -534,7 +535,7 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
                 if (lists) {
                     items = n_j * T.list_ipc;
                     if (lane == 0) {
-                        S.runs = T.list_runs + (long long)combo_j * T.max_classes;
+                        S.runs = runs0 + b * T.max_classes;
                         S.prefix = nullptr;
                         S.nclass = n_j;
                         S.items = items;
@@ -546,9 +547,10 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
                 if (lane == 0) S.rot = rot;
                 rot = int((rot + (unsigned)items) % unsigned(kFConsumers));
                 __syncwarp();
+                const u32 run_bytes = lists ? u32(n_j) * u32(sizeof(FastRun)) : 0u;
                 if (lane == 0) {
                     __threadfence_block();
-                    mbar_arrive_expect_tx(full, u32(T.smem_words) * 8u);
+                    mbar_arrive_expect_tx(full, u32(T.smem_words) * 8u + run_bytes);
                 }
                 __syncwarp();
                 if (lane < NS) {
@@ -560,6 +562,13 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
                     bulk_copy_to_shared(smem_addr(smem + b * row_stride) + u32(Md.smem_offset) * 8u,
                                         T.rows + Md.offset + (long long)rho * Md.length,
                                         u32(Md.length) * 8u, full);
+                }
+                if (lists && lane == 31) {
+                    // the class list's runs go next to the slot with the rows, so
+                    // the consumers read them from shared memory
+                    fence_proxy_async_shared();
+                    bulk_copy_to_shared(smem_addr(runs0 + b * T.max_classes),
+                                        T.list_runs + (long long)combo_j * T.max_classes, run_bytes, full);
                 }
 #pragma unroll
                 for (int t = 0; t < SLOTS; ++t) uses[t] += t == b ? 1 : 0;
