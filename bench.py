@@ -233,6 +233,40 @@ def cpu_baseline(coeffs, seconds=12.0):
                       f"{survivors} modular survivors), {elapsed:.2f} s on {threads} threads"}
 
 
+def reference_host_mock(threads=None):
+    """The reference's own CPU path on the C1 configuration: its host program
+    with the CPU mock backend (every site checked exactly with GMP), built from
+    its unchanged sources by oracle/ref_cpu/build_mock.py where the reference
+    tree exists; None elsewhere.  One mock device per thread."""
+    import hashlib
+    import statistics
+
+    mock = ROOT / "oracle" / "_ref" / "mock_ratpoints_gpu"
+    if not mock.exists():
+        return None
+    golden = json.loads((ROOT / "tests" / "golden" / "golden.json").read_text())["c1"]
+    threads = threads or os.cpu_count() or 1
+    env = dict(os.environ, RATPOINTS_TEST_DEVICE_COUNT=str(threads))
+    env.pop("CUDA_VISIBLE_DEVICES", None)
+    # at most 2,000,000 sites per mock worker (tests/mock_backend.cpp:106-108)
+    batch = max(1, min(499, 2_000_000 // (2 * golden["height"] + 1)))
+    cmd = [str(mock), golden["coefficients"], str(golden["height"]), "-du", str(golden["last"]),
+           "--devices", "all", "--batch-size", str(batch)]
+    times, same = [], True
+    for _ in range(3):
+        t0 = time.perf_counter()
+        r = subprocess.run(cmd, capture_output=True, env=env, timeout=600)
+        times.append(time.perf_counter() - t0)
+        same = same and r.returncode == 0 and hashlib.sha256(r.stdout).hexdigest() == golden["sha256"]
+    wall = statistics.median(times)
+    reduced = reduced_sites(golden["height"], golden["last"])
+    return {"value": reduced / wall / 1e9, "unit": UNIT, "seconds": wall, "threads": threads,
+            "stdout_matches_golden": same,
+            "workload": f"C1: degree-6 curve, coefficients in [-50, 50], a in [-{golden['height']}, "
+                        f"{golden['height']}], b in [1, {golden['last']}], default output; process "
+                        "wall time, median of 3"}
+
+
 def run_reference(args):
     coeffs = c2_curve()
     rank = int(os.environ.get("RANK", "0"))
@@ -251,6 +285,9 @@ def run_reference(args):
             "cpu_baseline": {**values[-1], "value": value},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    mock = reference_host_mock()
+    if mock is not None:
+        line["reference_host_mock"] = mock
     print(json.dumps(line))
 
 
