@@ -294,8 +294,9 @@ __global__ void composite_kernel(const CompositeSpec *specs, int nspecs, const u
 // ---------------------------------------------------------------------------
 // Stage 2 and emission
 
-// The 32 largest candidates not dividing d with 1/d mod p, by one warp: lane l
-// tests candidate 35 - l, lanes 0..3 also candidate 3 - l.
+// The 32 largest candidates not dividing d with 1/d mod p (s_dinv null: the
+// candidates only), by one warp: lane l tests candidate 35 - l, lanes 0..3
+// also candidate 3 - l.
 template <typename Index, typename Inverse>
 __device__ __forceinline__ void select_warp(u32 du, const Candidates &cand,
                                             const unsigned short *inv_table, Index *s_ci,
@@ -311,12 +312,12 @@ __device__ __forceinline__ void select_warp(u32 du, const Candidates &cand,
     const int rank_h = lane - __popc(hi_div & below);
     if (rh != 0 && rank_h < kSelectedPrimes) {
         s_ci[rank_h] = static_cast<Index>(ch);
-        s_dinv[rank_h] = static_cast<Inverse>(__ldg(inv_table + cand.p[ch] * kMaximumPrime + rh));
+        if (s_dinv) s_dinv[rank_h] = static_cast<Inverse>(__ldg(inv_table + cand.p[ch] * kMaximumPrime + rh));
     }
     const int rank_l = 32 - __popc(hi_div) + lane - __popc(lo_div & below);
     if (lane < kCandidatePrimes - 32 && rl != 0 && rank_l < kSelectedPrimes) {
         s_ci[rank_l] = static_cast<Index>(cl);
-        s_dinv[rank_l] = static_cast<Inverse>(__ldg(inv_table + cand.p[cl] * kMaximumPrime + rl));
+        if (s_dinv) s_dinv[rank_l] = static_cast<Inverse>(__ldg(inv_table + cand.p[cl] * kMaximumPrime + rl));
     }
     __syncwarp();
 }
@@ -399,8 +400,13 @@ struct WideRun {
     unsigned char first;
     unsigned char last;            // 1..64
     unsigned short start[kWideSlots];
+    unsigned int pad[2];           // 32 bytes: class lists are copied by TMA in whole 16-byte units
 };
-static_assert(sizeof(WideRun) == 24, "packed class run");
+static_assert(sizeof(WideRun) == 32, "packed class run");
+
+// Item prefixes of a class list are stored at a stride of whole 16-byte
+// units, so that a list's prefix row starts 16-byte aligned.
+__host__ __device__ inline int wide_prefix_stride(int max_classes) { return (max_classes + 1 + 3) & ~3; }
 
 // Per curve and class residue r mod M (precomputed on the host): the row
 // index of class word 0 for each modulus, (a0 S^-1) mod m with a0 = -H + ofs.
@@ -425,7 +431,6 @@ struct WideSlot {
     int next;                      // sweep-item counter
     int steps;                     // > 0: items are groups of kWK short classes, this many steps
     unsigned char sel[kSelectedPrimes];
-    unsigned short dinv[kSelectedPrimes];
 };
 
 // A denominator a consumer warp still has queued words of.
@@ -434,7 +439,6 @@ struct WideCtx {
     int d;
     int curve;
     unsigned char sel[kSelectedPrimes];
-    unsigned short dinv[kSelectedPrimes];
 };
 
 // Stage 2 and emission for up to 32 queued words.  A queued word carries its
@@ -443,8 +447,8 @@ struct WideCtx {
 // bitmasks are read through the read-only cache.
 __device__ __forceinline__ void wide_drain(const u64 *qmask, const u64 *qpos, int start, int n,
                                            const WideCurve *curves, const u64 *affine,
-                                           const Candidates &cand, const WideCtx *ctx,
-                                           const BatchOut &out) {
+                                           const Candidates &cand, const unsigned short *inv_table,
+                                           const WideCtx *ctx, const BatchOut &out) {
     const int lane = threadIdx.x & 31;
     u64 m = 0, pos = 0;
     if (lane < n) {
@@ -461,7 +465,9 @@ __device__ __forceinline__ void wide_drain(const u64 *qmask, const u64 *qpos, in
         for (int s = 0; s < kSelectedPrimes && m; ++s) {
             const int ci = X.sel[s];
             const u32 p = u32(cand.p[ci]), magic = cand.magic[ci];
-            const u32 dinv = X.dinv[s];
+            // 1/d mod p (stage 2 is rare enough to look it up here rather
+            // than in the producer's path)
+            const u32 dinv = __ldg(inv_table + p * kMaximumPrime + mod_small(u32(X.d), p, magic));
             u32 r = mod_small(hi, p, magic);
             r = mod_small((r << 16) | lo, p, magic);  // pos mod p
             r += __ldg(&Cg->neg_h[ci]);               // a mod p
@@ -562,7 +568,8 @@ __global__ void __launch_bounds__(kWThreads, 2)
     u64 *qmask = smem + kWSlotCount * row_stride;
     u64 *qpos = qmask + kWConsumers * kQueue;
     WideRun *runs0 = reinterpret_cast<WideRun *>(qpos + kWConsumers * kQueue);  // [slots][max_classes]
-    int *prefix0 = reinterpret_cast<int *>(runs0 + kWSlotCount * max_classes);  // [slots][max_classes + 1]
+    int *prefix0 = reinterpret_cast<int *>(runs0 + kWSlotCount * max_classes);  // [slots][prefix stride]
+    const int pstride = wide_prefix_stride(max_classes);
     __shared__ WideSlot slot[kWSlotCount];
     __shared__ WideCtx s_ctx[kWConsumers][kWCtx];
     __shared__ __align__(8) unsigned long long s_full[kWSlotCount];
@@ -651,7 +658,7 @@ __global__ void __launch_bounds__(kWThreads, 2)
             }
             const u32 du = u32(d);
             const WideCurve &C = curves[item.curve];
-            select_warp(du, cand, inv_table, S.sel, S.dinv);
+            select_warp(du, cand, inv_table, S.sel, static_cast<unsigned short *>(nullptr));
             if (lane < kWideSlots) {
                 const Modulus &Md = C.mod[lane];
                 S.magic[lane] = Md.magic;
@@ -659,17 +666,18 @@ __global__ void __launch_bounds__(kWThreads, 2)
                 S.step8[lane] = 8u * Md.step;
                 S.soff[lane] = 8u * u32(Md.smem_offset);
             }
+            // a class list goes next to the slot by TMA with the rows
+            const WideRun *list_src = nullptr;
+            const int *prefix_src = nullptr;
+            u32 list_bytes = 0, prefix_bytes = 0;
             if (lists >= 0) {
-                // the class list of d's class, copied next to the slot
                 const int lm = C.list_max;
-                const u32 *src = reinterpret_cast<const u32 *>(list_runs + C.list_runs + (long long)combo * lm);
                 WideRun *runs = runs0 + b * max_classes;
-                int *prefix = prefix0 + b * (max_classes + 1);
-                u32 *dst = reinterpret_cast<u32 *>(runs);
-                const int nwords = nlist * int(sizeof(WideRun) / 4);
-                for (int t = lane; t < nwords; t += kWarpSize) dst[t] = __ldg(src + t);
-                const int *psrc = list_prefix + C.list_prefix + (long long)combo * (lm + 1);
-                for (int t = lane; t <= nlist; t += kWarpSize) prefix[t] = __ldg(psrc + t);
+                int *prefix = prefix0 + b * pstride;
+                list_src = list_runs + C.list_runs + (long long)combo * lm;
+                prefix_src = list_prefix + C.list_prefix + (long long)combo * wide_prefix_stride(lm);
+                list_bytes = u32(nlist) * u32(sizeof(WideRun));
+                prefix_bytes = u32(wide_prefix_stride(nlist)) * 4u;  // within the list's stride
                 if (lane == 0) {
                     S.runs = runs;
                     S.prefix = prefix;
@@ -678,7 +686,7 @@ __global__ void __launch_bounds__(kWThreads, 2)
                 }
             } else {
                 WideRun *runs = runs0 + b * max_classes;
-                int *prefix = prefix0 + b * (max_classes + 1);
+                int *prefix = prefix0 + b * pstride;
                 const int nclass = wide_layout(C, class_starts + C.cls, du, d, item.range, runs, prefix);
                 if (lane == 0) {
                     S.runs = runs;
@@ -694,7 +702,7 @@ __global__ void __launch_bounds__(kWThreads, 2)
                 S.next = 0;
                 __threadfence_block();
                 fence_proxy_async_shared();
-                mbar_arrive_expect_tx(full, u32(C.smem_words) * 8u);
+                mbar_arrive_expect_tx(full, u32(C.smem_words) * 8u + list_bytes + prefix_bytes);
                 const u32 dst = smem_addr(smem + b * row_stride);
 #pragma unroll
                 for (int sl = 0; sl < kWideSlots; ++sl) {
@@ -703,6 +711,10 @@ __global__ void __launch_bounds__(kWThreads, 2)
                     bulk_copy_to_shared(dst + u32(Md.smem_offset) * 8u,
                                         pool + Md.offset + (long long)rho * Md.length,
                                         u32(Md.length) * 8u, full);
+                }
+                if (list_bytes) {
+                    bulk_copy_to_shared(smem_addr(runs0 + b * max_classes), list_src, list_bytes, full);
+                    bulk_copy_to_shared(smem_addr(prefix0 + b * pstride), prefix_src, prefix_bytes, full);
                 }
             }
             __syncwarp();
@@ -734,7 +746,7 @@ __global__ void __launch_bounds__(kWThreads, 2)
         while (qn > 0) {
             const int nd = qn < 32 ? qn : 32;
             __syncwarp();
-            wide_drain(wq_mask, wq_pos, qn - nd, nd, curves, affine, cand, ctx, out);
+            wide_drain(wq_mask, wq_pos, qn - nd, nd, curves, affine, cand, inv_table, ctx, out);
             qn -= nd;
         }
     };
@@ -755,7 +767,6 @@ __global__ void __launch_bounds__(kWThreads, 2)
         if (qn == 0) oldest = seq;
         __syncwarp();
         ctx[kc].sel[lane] = S.sel[lane];
-        ctx[kc].dinv[lane] = S.dinv[lane];
         if (lane == 0) {
             ctx[kc].d = int(S.d);
             ctx[kc].curve = S.curve;
@@ -836,7 +847,7 @@ __global__ void __launch_bounds__(kWThreads, 2)
                             qn += __popc(bb);
                             if (qn >= 32) {
                                 __syncwarp();
-                                wide_drain(wq_mask, wq_pos, qn - 32, 32, curves, affine, cand, ctx, out);
+                                wide_drain(wq_mask, wq_pos, qn - 32, 32, curves, affine, cand, inv_table, ctx, out);
                                 qn -= 32;
                                 if (qn == 0) oldest = seq;
                             }
@@ -920,7 +931,7 @@ __global__ void __launch_bounds__(kWThreads, 2)
                             qn += __popc(bb);
                             if (qn >= 32) {
                                 __syncwarp();
-                                wide_drain(wq_mask, wq_pos, qn - 32, 32, curves, affine, cand, ctx, out);
+                                wide_drain(wq_mask, wq_pos, qn - 32, 32, curves, affine, cand, inv_table, ctx, out);
                                 qn -= 32;
                                 if (qn == 0) oldest = seq;
                             }
@@ -1373,7 +1384,7 @@ long long wide_row_budget(int max_classes) {
     const long long fixed = 6 * 1024 +  // static shared memory of the kernel (5 KB) and slack
                             (long long)dev::kWConsumers * dev::kQueue * 16 +
                             (long long)dev::kWSlotCount * max_classes * (long long)sizeof(dev::WideRun) +
-                            (long long)dev::kWSlotCount * (max_classes + 1) * 4;
+                            (long long)dev::kWSlotCount * dev::wide_prefix_stride(max_classes) * 4;
     return std::max(2LL * 64, (per_cta - fixed) / 8);
 }
 
@@ -1695,10 +1706,10 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 const std::size_t ncombo = std::size_t(64) * std::size_t(q);
                 C.list_count = list_count_total;
                 C.list_runs = list_runs_total;
-                C.list_prefix = list_prefix_total;
+                C.list_prefix = list_prefix_total;  // a multiple of 4: rows start 16-byte aligned
                 list_count_total += (long long)ncombo;
                 list_runs_total += (long long)ncombo * lm;
-                list_prefix_total += (long long)ncombo * (lm + 1);
+                list_prefix_total += (long long)ncombo * dev::wide_prefix_stride(lm);
                 list_curves.push_back({P.wide.size(), i});  // filled below, in parallel
                 // classes of at most 128 words are swept kWK at a time
                 const long long max_words = (C.count_q + 1 + 63) >> 6;
@@ -1824,7 +1835,7 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 const int nclass = __builtin_popcountll(classes2) * nq;
                 if (nclass > lm) throw std::logic_error("class list longer than its stride");
                 dev::WideRun *runs = P.list_runs.data() + C.list_runs + k * std::size_t(lm);
-                int *prefix = P.list_prefix.data() + C.list_prefix + k * std::size_t(lm + 1);
+                int *prefix = P.list_prefix.data() + C.list_prefix + k * std::size_t(dev::wide_prefix_stride(lm));
                 int items = 0;
                 for (int cidx = 0; cidx < nclass; ++cidx) {
                     const int r64 = nth_bit_host(classes2, cidx / nq);
@@ -2046,7 +2057,7 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
                                       std::size_t(dev::kWConsumers) * dev::kQueue * 16 +
                                       std::size_t(dev::kWSlotCount) * std::size_t(wide_max_classes) *
                                           sizeof(dev::WideRun) +
-                                      std::size_t(dev::kWSlotCount) * std::size_t(wide_max_classes + 1) * 4;
+                                      std::size_t(dev::kWSlotCount) * std::size_t(dev::wide_prefix_stride(wide_max_classes)) * 4;
         const std::size_t narrow_smem = std::size_t(dev::kNarrowTableWords + dev::kAffWords) * 8 +
                                         std::size_t(dev::kNWarps) * dev::kQueue * 12;
         int wide_grid = 0, narrow_grid = 0;
