@@ -592,135 +592,131 @@ __global__ void __launch_bounds__(kWThreads, 2)
 
     if (warp == 0) {
         // ---- producer ----
+        // Work items come from the device queue with the next item's index
+        // fetched ahead; lane j classifies parameter j of each 32 of an item,
+        // and the live denominators go to the slots in order.  Lanes
+        // 0 .. kWideSlots-1 copy one row each, lanes 30 and 31 the class list.
         int b = 0;
         int uses[kWSlotCount] = {};  // fills of each slot so far
         bool failed = false;
-        BatchItem item{};
-        int i = 0, count = 0;
-        int q = 1, square = 0, nint = 0;
-        long long lists = -1;  // the item's curve's class-list offset (-1: laid out here)
-        unsigned long long magic_q = 0;
-        for (;;) {
-            long long d = -1;
-            int combo = 0, nlist = 0;
-            for (;;) {
-                if (i >= count) {
-                    int nxt = 0;
-                    if (lane == 0) nxt = int(atomicAdd(work, 1ull));
-                    nxt = __shfl_sync(kFullMask, nxt, 0);
-                    if (nxt >= nitems) break;
-                    item = items[nxt];
-                    i = 0;
-                    count = item.count;
-                    const WideCurve &C = curves[item.curve];
-                    q = C.class_prime;
-                    square = C.square;
-                    nint = C.nint;
-                    lists = C.list_count;
-                    magic_q = (~0ull) / u32(q) + 1;
-                    continue;
-                }
-                const long long k = item.first + i++;
-                const long long dd = square ? k * k : k;
-                const u32 du = u32(dd);
-                const int dq = q > 1 ? int(mod_u32(du, u32(q), magic_q)) : 0;
-                if (lists >= 0) {
-                    combo = int(du & 63) * q + dq;
-                    nlist = __ldg(list_count + lists + combo);
-                    if (nlist == 0) continue;
-                } else {
-                    const WideCurve &C = curves[item.curve];
-                    if (C.admissible[du & 63] == 0 || (q > 1 && C.admissible[64 + dq] == 0)) continue;
-                    long long L, U;
-                    if (nint > 0 && !x_range(C.lo, C.hi, nint, C.bound, dd, item.range, L, U)) continue;
-                }
-                d = dd;
-                break;
-            }
-            // slot b must be released by every consumer before it is refilled
+        int next_item = 0;
+        if (lane == 0) next_item = int(atomicAdd(work, 1ull));
+        auto acquire_slot = [&]() -> bool {
             int used = 0;
 #pragma unroll
             for (int t = 0; t < kWSlotCount; ++t) used = t == b ? uses[t] : used;
-            if (used > 0 && !mbar_wait(smem_addr(&s_empty[b]), u32(used - 1) & 1u)) {
-                failed = true;
-                break;
-            }
-            WideSlot &S = slot[b];
-            const u32 full = smem_addr(&s_full[b]);
-            if (d < 0) {
-                if (lane == 0) S.d = -1;
-                __syncwarp();
-                if (lane == 0) {
-                    __threadfence_block();
-                    mbar_arrive(full);
-                }
-                break;
-            }
-            const u32 du = u32(d);
+            return used == 0 || mbar_wait(smem_addr(&s_empty[b]), u32(used - 1) & 1u);
+        };
+        for (;;) {
+            const int idx = __shfl_sync(kFullMask, next_item, 0);
+            if (idx >= nitems) break;
+            if (lane == 0) next_item = int(atomicAdd(work, 1ull));
+            const BatchItem item = items[idx];
             const WideCurve &C = curves[item.curve];
-            select_warp(du, cand, inv_table, S.sel, static_cast<unsigned short *>(nullptr));
-            if (lane < kWideSlots) {
-                const Modulus &Md = C.mod[lane];
-                S.magic[lane] = Md.magic;
-                S.m[lane] = u32(Md.m);
-                S.step8[lane] = 8u * Md.step;
-                S.soff[lane] = 8u * u32(Md.smem_offset);
+            const int q = C.class_prime;
+            const long long lists = C.list_count;  // -1: classes laid out here
+            const unsigned long long magic_q = (~0ull) / u32(q) + 1;
+            for (int base = 0; base < item.count && !failed; base += kWarpSize) {
+                const bool valid = base + lane < item.count;
+                const long long k = item.first + base + (valid ? lane : 0);
+                const long long dd = C.square ? k * k : k;
+                const u32 dv = u32(dd);
+                const int dq = q > 1 ? int(mod_u32(dv, u32(q), magic_q)) : 0;
+                const int combo = int(dv & 63) * q + dq;
+                int nlist = 0;
+                bool live = false;
+                if (valid) {
+                    if (lists >= 0) {
+                        nlist = __ldg(list_count + lists + combo);
+                        live = nlist > 0;
+                    } else {
+                        long long L, U;
+                        live = C.admissible[dv & 63] != 0 && (q == 1 || C.admissible[64 + dq] != 0) &&
+                               (C.nint == 0 || x_range(C.lo, C.hi, C.nint, C.bound, dd, item.range, L, U));
+                    }
+                }
+                for (u32 todo = __ballot_sync(kFullMask, live); todo; todo &= todo - 1) {
+                    const int j = __ffs(todo) - 1;
+                    const long long d = __shfl_sync(kFullMask, dd, j);
+                    const int combo_j = __shfl_sync(kFullMask, combo, j);
+                    const int nlist_j = __shfl_sync(kFullMask, nlist, j);
+                    if (!acquire_slot()) {
+                        failed = true;
+                        break;
+                    }
+                    WideSlot &S = slot[b];
+                    const u32 full = smem_addr(&s_full[b]);
+                    const u32 du = u32(d);
+                    select_warp(du, cand, inv_table, S.sel, static_cast<unsigned short *>(nullptr));
+                    if (lane < kWideSlots) {
+                        const Modulus &Md = C.mod[lane];
+                        S.magic[lane] = Md.magic;
+                        S.m[lane] = u32(Md.m);
+                        S.step8[lane] = 8u * Md.step;
+                        S.soff[lane] = 8u * u32(Md.smem_offset);
+                    }
+                    WideRun *runs = runs0 + b * max_classes;
+                    int *prefix = prefix0 + b * pstride;
+                    // a class list goes next to the slot by TMA with the rows
+                    u32 list_bytes = 0, prefix_bytes = 0;
+                    int nclass = nlist_j;
+                    if (lists >= 0) {
+                        list_bytes = u32(nlist_j) * u32(sizeof(WideRun));
+                        prefix_bytes = u32(wide_prefix_stride(nlist_j)) * 4u;  // within the list's stride
+                    } else {
+                        nclass = wide_layout(C, class_starts + C.cls, du, d, item.range, runs, prefix);
+                    }
+                    __syncwarp();
+                    if (lane == 0) {
+                        S.runs = runs;
+                        S.prefix = prefix;
+                        S.nclass = nclass;
+                        S.steps = lists >= 0 ? C.list_steps : 0;
+                        S.d = d;
+                        S.curve = item.curve;
+                        S.next = 0;
+                        __threadfence_block();
+                        mbar_arrive_expect_tx(full, u32(C.smem_words) * 8u + list_bytes + prefix_bytes);
+                    }
+                    __syncwarp();
+                    if (lane < kWideSlots) {
+                        // the consumers' reads of this slot's previous contents are
+                        // ordered before the asynchronous copies that overwrite them
+                        fence_proxy_async_shared();
+                        const Modulus &Md = C.mod[lane];
+                        const u32 rho = mod_u32(du, u32(Md.m), Md.magic);
+                        bulk_copy_to_shared(smem_addr(smem + b * row_stride) + u32(Md.smem_offset) * 8u,
+                                            pool + Md.offset + (long long)rho * Md.length,
+                                            u32(Md.length) * 8u, full);
+                    } else if (list_bytes && lane >= kWarpSize - 2) {
+                        fence_proxy_async_shared();
+                        const int lm = C.list_max;
+                        if (lane == kWarpSize - 2)
+                            bulk_copy_to_shared(smem_addr(runs), list_runs + C.list_runs + (long long)combo_j * lm,
+                                                list_bytes, full);
+                        else
+                            bulk_copy_to_shared(smem_addr(prefix),
+                                                list_prefix + C.list_prefix + (long long)combo_j * wide_prefix_stride(lm),
+                                                prefix_bytes, full);
+                    }
+#pragma unroll
+                    for (int t = 0; t < kWSlotCount; ++t) uses[t] += t == b ? 1 : 0;
+                    b = b + 1 == kWSlotCount ? 0 : b + 1;
+                }
             }
-            // a class list goes next to the slot by TMA with the rows
-            const WideRun *list_src = nullptr;
-            const int *prefix_src = nullptr;
-            u32 list_bytes = 0, prefix_bytes = 0;
-            if (lists >= 0) {
-                const int lm = C.list_max;
-                WideRun *runs = runs0 + b * max_classes;
-                int *prefix = prefix0 + b * pstride;
-                list_src = list_runs + C.list_runs + (long long)combo * lm;
-                prefix_src = list_prefix + C.list_prefix + (long long)combo * wide_prefix_stride(lm);
-                list_bytes = u32(nlist) * u32(sizeof(WideRun));
-                prefix_bytes = u32(wide_prefix_stride(nlist)) * 4u;  // within the list's stride
+            if (failed) break;
+        }
+        if (!failed) {
+            // no more work: an empty slot fill tells the consumers to finish
+            if (acquire_slot()) {
                 if (lane == 0) {
-                    S.runs = runs;
-                    S.prefix = prefix;
-                    S.nclass = nlist;
-                    S.steps = C.list_steps;
+                    slot[b].d = -1;
+                    __threadfence_block();
+                    mbar_arrive(smem_addr(&s_full[b]));
                 }
             } else {
-                WideRun *runs = runs0 + b * max_classes;
-                int *prefix = prefix0 + b * pstride;
-                const int nclass = wide_layout(C, class_starts + C.cls, du, d, item.range, runs, prefix);
-                if (lane == 0) {
-                    S.runs = runs;
-                    S.prefix = prefix;
-                    S.nclass = nclass;
-                    S.steps = 0;
-                }
+                failed = true;
             }
-            __syncwarp();
-            if (lane == 0) {
-                S.d = d;
-                S.curve = item.curve;
-                S.next = 0;
-                __threadfence_block();
-                fence_proxy_async_shared();
-                mbar_arrive_expect_tx(full, u32(C.smem_words) * 8u + list_bytes + prefix_bytes);
-                const u32 dst = smem_addr(smem + b * row_stride);
-#pragma unroll
-                for (int sl = 0; sl < kWideSlots; ++sl) {
-                    const Modulus &Md = C.mod[sl];
-                    const u32 rho = mod_u32(du, u32(Md.m), Md.magic);
-                    bulk_copy_to_shared(dst + u32(Md.smem_offset) * 8u,
-                                        pool + Md.offset + (long long)rho * Md.length,
-                                        u32(Md.length) * 8u, full);
-                }
-                if (list_bytes) {
-                    bulk_copy_to_shared(smem_addr(runs0 + b * max_classes), list_src, list_bytes, full);
-                    bulk_copy_to_shared(smem_addr(prefix0 + b * pstride), prefix_src, prefix_bytes, full);
-                }
-            }
-            __syncwarp();
-#pragma unroll
-            for (int t = 0; t < kWSlotCount; ++t) uses[t] += t == b ? 1 : 0;
-            b = b + 1 == kWSlotCount ? 0 : b + 1;
         }
         if (failed) {
             if (out.error && lane == 0) atomicOr(out.error, 1ull);
