@@ -87,3 +87,39 @@ def test_record_curve_at_full_height(rpg, oracle):
     # the record curve at its published height 10^7 (a dense curve: the
     # reference's fast launch overflows and its streaming rerun runs)
     compare(rpg, oracle, RECORD, 10_000_000, 1, 6000, batch=3000)
+
+
+def planted_c2_curve(rpg, seed=77):
+    """A squarefree curve of the benchmark's shape (degree 6, coefficients in
+    [-2^32, 2^32)) with c0 chosen so that F(1, 1) = sum(c) is a square y^2:
+    (1 : y : 1) is a point."""
+    import math
+    rng = random.Random(seed)
+    while True:
+        c = [rng.randrange(-(2**32), 2**32) for _ in range(7)]
+        rest = sum(c[1:])
+        y = math.isqrt(max(0, rest + 2**31))
+        c[0] = y * y - rest
+        if -(2**32) <= c[0] < 2**32 and c[6] != 0 and rpg.is_squarefree([str(v) for v in c]):
+            return [str(v) for v in c], y
+
+
+def test_c2_shape_with_points_full_box(rpg, oracle):
+    """A curve of the benchmark's shape that has points, over the benchmark's
+    whole box: the reference kernels' survivor multiset equals the reference
+    plan's, both plans print the same non-empty stdout, and every printed
+    point satisfies y^2 = F(a, b) exactly."""
+    coeffs, y1 = planted_c2_curve(rpg)
+    ref = compare(rpg, oracle, coeffs, 5_000_000, 1, 5_000_000)
+    text = " ".join(coeffs)
+    runs = {plan: rpg.cli([text, "5000000", "--sieve-plan", plan, "-i"]) for plan in ("reference", "fast")}
+    assert runs["fast"].returncode == 0 and runs["reference"].returncode == 0
+    assert runs["fast"].stdout == runs["reference"].stdout
+    lines = runs["fast"].stdout.decode().splitlines()
+    assert f"(1 : {y1} : 1)" in lines
+    c = [int(v) for v in coeffs]
+    for line in lines:
+        a, y, b = (int(t) for t in line.strip("()").split(" : "))
+        F = sum(ci * a**i * b**(6 - i) for i, ci in enumerate(c))
+        assert y * y == F
+    assert ref["survivors"] >= len(lines) // 2
