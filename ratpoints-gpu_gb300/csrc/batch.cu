@@ -1101,12 +1101,14 @@ __global__ void __launch_bounds__(kNThreads, 3)
                         at[s] = min(t, t - mods[s]);
                     }
                     const int wl = w0 + kNK * lane;
+                    if (w0 == w_lo || w0 + kWarpSize * kNK - 1 > w_hi) {  // the range's first or last step
 #pragma unroll
-                    for (int k = 0; k < kNK; ++k) {
-                        const int w = wl + k;
-                        if (w > w_hi) acc[k] = 0;
-                        if (w == w_lo) acc[k] &= first_mask;
-                        if (w == w_hi) acc[k] &= last_mask;
+                        for (int k = 0; k < kNK; ++k) {
+                            const int w = wl + k;
+                            if (w > w_hi) acc[k] = 0;
+                            if (w == w_lo) acc[k] &= first_mask;
+                            if (w == w_hi) acc[k] &= last_mask;
+                        }
                     }
                     if (!__ballot_sync(kFullMask, (acc[0] | acc[1] | acc[2] | acc[3]) != 0)) continue;
 #pragma unroll

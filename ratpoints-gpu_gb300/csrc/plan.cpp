@@ -162,11 +162,15 @@ FastPlanner::FastPlanner(const std::vector<std::string> &coefficients, long long
         }
     };
     add_primes(3, prime_limit_);
-    // Class prime: the strongest of 3..13 whose classes stay long enough
-    // (at least 256 words of 64 sites per class) and few enough: admissible
-    // 2-adic classes times admissible residues mod q (q | d admits every
-    // r != 0 at most), over all d.
+    // Class prime: of 3..13 whose classes stay long enough (at least 256
+    // words of 64 sites per class) and few enough (admissible 2-adic classes
+    // times admissible residues mod q, over all d), the one whose class
+    // layout sweeps the smallest share of the (d, r) residue pairs mod q:
+    // A = q x pass rate residues for each of the q - 1 classes of d prime to
+    // q, and for q | d every r != 0 when F(r, d) = c_n r^n is a square mod q
+    // (c_n a square or zero, or n odd, where F vanishes), none otherwise.
     const long double sites = 2.0L * bound + 1.0L;
+    const int degree = int(coefficients.size()) - 1;
     double best = 0.45;  // below ~0.45 bits a class prime does not pay for its classes
     int worst2 = -1;
     for (const auto &s : strength_) {
@@ -180,9 +184,13 @@ FastPlanner::FastPlanner(const std::vector<std::string> &coefficients, long long
             for (auto m : adm2) worst2 = std::max(worst2, __builtin_popcountll(m));
         }
         const int admissible = int(std::lround(std::exp2(-s.first) * q));
-        if (worst2 * std::max(admissible, q - 1) > kMaxFastClasses) continue;
-        if (s.first > best) {
-            best = s.first;
+        const bool lead = degree % 2 == 1 || square_mod(decimal_mod(coefficients.back(), q), q);
+        const int divides = lead ? q - 1 : 0;
+        if (worst2 * std::max(admissible, divides) > kMaxFastClasses) continue;
+        const int swept = (q - 1) * admissible + divides;
+        const double bits = swept > 0 ? std::log2(double(q) * q / swept) : 16.0;
+        if (bits > best) {
+            best = bits;
             class_prime_ = q;
         }
     }

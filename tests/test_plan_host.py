@@ -32,9 +32,12 @@ def test_c2_plan(rpg):
     import bench
     plan = rpg.fast_plan(bench.c2_curve(), 5_000_000)
     well_formed(plan)
-    # rows of small-prime products, class prime 5 (f mod 3 is always a square);
-    # three staged denominators per CTA cost it no filtering (13.2 bits)
-    assert plan["class_prime"] == 5
+    # rows of small-prime products; class prime 7: its classes sweep 18 of
+    # the 49 residue pairs (d, r) mod 7 (3 residues for each d prime to 7,
+    # none for 7 | d: c_6 is not a square mod 7), against 12 of 25 mod 5
+    # (f mod 3 is always a square); three staged denominators per CTA cost
+    # it no filtering (13.3 bits)
+    assert plan["class_prime"] == 7
     assert 6 <= len(plan["moduli"]) <= 8 and plan["bits"] > 13
     assert plan["slots"] == 3
     assert all(q < 128 for f in plan["factors"] for q in f)
