@@ -392,6 +392,7 @@ struct Sieve::Impl {
     int fast_max_classes = 1;
     std::size_t fast_smem = 0;
     std::vector<dev::u64> fast_adm_host;
+    std::vector<int> fast_bad_primes;      // denominator primes (see FastTables::nbad)
     FastPlan fast_plan;
     long long max_tile = dev::kMaxTileWords;
     long long capacity = 0;       // most survivors a buffer may grow to hold
@@ -896,6 +897,25 @@ struct Sieve::Impl {
                 }
             }
         }
+        // Denominator primes: p < 512 (p != q, which the class residues
+        // already cover) with c_n not a square mod p, for even degree.  A
+        // denominator divisible by one holds no points: p !| a (gcd) gives
+        // F(a, d) = c_n a^n (mod p), a non-square.  The producer skips such
+        // denominators (pairs p, ceil(2^64 / p) after the class residues).
+        fast_bad_primes.clear();
+        if (n % 2 == 0) {
+            for (int p = 3; p < kMaximumPrime; p += 2) {
+                bool prime = true;
+                for (int f = 3; f * f <= p && prime; f += 2) prime = p % f != 0;
+                if (!prime || p == q) continue;
+                const int lc = decimal_mod(coefficients.back(), p);
+                if (lc == 0 || square_mod(lc, p)) continue;
+                fast_bad_primes.push_back(p);
+                adm.push_back(dev::u64(p));
+                adm.push_back((~0ull) / dev::u64(p) + 1);
+            }
+        }
+        F.nbad = int(fast_bad_primes.size());
         fast_adm_host = adm;
         // class starts for every residue r mod M: ofs = (r + H) mod M and, per
         // modulus, the row index ((-H + ofs) S^-1) mod m of class word 0
@@ -1420,11 +1440,28 @@ unsigned long long Sieve::swept_words(long long first, long long last) const {
     const int q = I.F.class_prime;
     const long long M = I.F.class_mod;
     std::vector<unsigned long long> per_residue(M, 0);
-    for (long long t = 0; t < M; ++t) {
-        const long long lo = first + ((t - first % M) % M + M) % M;  // first k >= first, k = t (mod M)
-        const unsigned long long n = lo > last ? 0 : (unsigned long long)((last - lo) / M + 1);
-        const long long dres = I.opt.square ? (t * t) % M : t;
-        per_residue[dres] += n;
+    if (I.fast_bad_primes.empty()) {
+        for (long long t = 0; t < M; ++t) {
+            const long long lo = first + ((t - first % M) % M + M) % M;  // first k >= first, k = t (mod M)
+            const unsigned long long n = lo > last ? 0 : (unsigned long long)((last - lo) / M + 1);
+            const long long dres = I.opt.square ? (t * t) % M : t;
+            per_residue[dres] += n;
+        }
+    } else {
+        // parameters k without a denominator prime factor, by segments
+        constexpr long long kSegment = 1LL << 22;
+        std::vector<unsigned char> skip;
+        for (long long lo = first; lo <= last; lo += kSegment) {
+            const long long hi = std::min(last, lo + kSegment - 1);
+            skip.assign(std::size_t(hi - lo + 1), 0);
+            for (int p : I.fast_bad_primes)
+                for (long long k = lo + ((p - lo % p) % p); k <= hi; k += p) skip[std::size_t(k - lo)] = 1;
+            for (long long k = lo; k <= hi; ++k) {
+                if (skip[std::size_t(k - lo)]) continue;
+                const long long t = k % M;
+                per_residue[I.opt.square ? (t * t) % M : t] += 1;
+            }
+        }
     }
     const long long sites = 2 * I.bound + 1;
     unsigned long long total = 0;

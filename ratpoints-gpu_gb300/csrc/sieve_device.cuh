@@ -52,6 +52,18 @@ __device__ __forceinline__ u32 mod_u32(u32 n, u32 m, unsigned long long magic) {
     return r >= m ? r - m : r;
 }
 
+// Three-input AND and OR (one lop3 each).
+__device__ __forceinline__ u32 and3(u32 a, u32 b, u32 c) {
+    u32 d;
+    asm("lop3.b32 %0, %1, %2, %3, 0x80;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+__device__ __forceinline__ u32 or3(u32 a, u32 b, u32 c) {
+    u32 d;
+    asm("lop3.b32 %0, %1, %2, %3, 0xFE;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
 // Shared-memory address, mbarrier and bulk-copy (TMA, non-tensor) helpers.
 __device__ __forceinline__ u32 smem_addr(const void *p) {
     return u32(__cvta_generic_to_shared(p));

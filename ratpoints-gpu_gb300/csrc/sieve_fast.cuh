@@ -48,6 +48,7 @@ constexpr int kFQueue = 64;
 constexpr int kFStage2Group = 6;                           // stage-2 primes loaded together
 constexpr long long kFMaxClassWords = 1LL << 23;           // class words of a launch's tile (24-bit field)
 constexpr int kFAdmQ = 16;                                 // admissible-residue words for q <= 13
+constexpr int kFBadBase = 64 + kFAdmQ;                     // first denominator-prime word of admissible
 
 
 struct FastModulus {
@@ -106,7 +107,9 @@ struct FastTables {
     int list_ipc;
     const u64 *rows;               // stage-1 modulus tables
     const u64 *prime_rows;         // reference candidate tables (class layout)
-    const u64 *admissible;         // [64] 2-adic classes by d mod 64, then [kFAdmQ] residues by d mod q
+    const u64 *admissible;         // [64] 2-adic classes by d mod 64, then [kFAdmQ] residues by d mod q,
+                                   // then nbad pairs (p, ceil(2^64 / p)): the denominator primes
+    int nbad;                      // denominator primes: p < 512, p != q, c_n not a square mod p (even degree)
     int class_prime;               // q (1: none)
     int class_mod;                 // M = 64 q
     int h_mod_m;                   // H mod M
@@ -437,16 +440,6 @@ __device__ __forceinline__ void lds_row4(u32 a, u32 (&lo)[kFK], u32 (&hi)[kFK]) 
           "=r"(hi[3])
         : "r"(a));
 }
-__device__ __forceinline__ u32 and3(u32 a, u32 b, u32 c) {
-    u32 d;
-    asm("lop3.b32 %0, %1, %2, %3, 0x80;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-    return d;
-}
-__device__ __forceinline__ u32 or3(u32 a, u32 b, u32 c) {
-    u32 d;
-    asm("lop3.b32 %0, %1, %2, %3, 0xFE;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-    return d;
-}
 
 template <int NS, int SLOTS>
 __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, SieveArgs A,
@@ -502,9 +495,11 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
             const long long chunk = (long long)__shfl_sync(kFullMask, next_chunk, 0);
             if (chunk >= A.k_count) break;
             if (lane == 0) next_chunk = atomicAdd(work, (unsigned long long)kFChunk);
-            const long long idx = chunk + lane;
-            const bool valid = lane < kFChunk && idx < A.k_count;
-            const long long k = A.k_first + (valid ? idx : 0);
+            static_assert(2 * kFChunk == kWarpSize, "lanes 16..31 mirror the chunk's parameters");
+            const long long idx = chunk + (lane & (kFChunk - 1));
+            const bool in_range = idx < A.k_count;
+            const bool valid = lane < kFChunk && in_range;
+            const long long k = A.k_first + (in_range ? idx : 0);
             const long long dd = A.square ? k * k : k;
             const u32 du = u32(dd);
             const int combo = int(du & 63) * q + (q > 1 ? int(mod_u32(du, u32(q), magic_q)) : 0);
@@ -517,6 +512,21 @@ __global__ void __launch_bounds__(kFThreads, 2) fast_sieve_kernel(FastTables T, 
                                      (q == 1 || __ldg(T.admissible + 64 + int(mod_u32(du, u32(q), magic_q))) != 0);
                     list_n = adm ? 1 : 0;
                 }
+            }
+            if (T.nbad > 0) {
+                // Denominator primes: for p | d and p !| a, F(a, d) = c_n a^n
+                // (mod p), which is not a square when c_n is not and n is
+                // even, so d holds no points.  p | k^2 iff p | k; the two
+                // half-warps test a parameter against alternate primes.
+                const u32 ku = u32(k);
+                int hit = 0;
+                for (int i = lane >> 4; i < T.nbad; i += 2) {
+                    const u32 p = u32(__ldg(T.admissible + kFBadBase + 2 * i));
+                    const unsigned long long mg = __ldg(T.admissible + kFBadBase + 2 * i + 1);
+                    hit |= mod_u32(ku, p, mg) == 0 ? 1 : 0;
+                }
+                hit |= __shfl_xor_sync(kFullMask, hit, kFChunk);
+                if (hit) list_n = 0;
             }
             u32 live = __ballot_sync(kFullMask, list_n > 0);
             while (live) {

@@ -1,9 +1,10 @@
 """Fast plan parity: its survivor set is exactly the reference plan's survivor
 set intersected with the extra filters the fast plan documents (2-adic
-classes mod 64 with gcd parity, and f(a/d) a square mod each small prime the
+classes mod 64 with gcd parity; f(a/d) a square mod each small prime the
 per-curve plan chose, or gcd and the leading-coefficient test when the prime
-divides d).  Every extra filter holds for every point, so the point sets are
-equal."""
+divides d; and, for even degree, no denominator divisible by a prime p < 512
+mod which the leading coefficient is not a square).  Every extra filter holds
+for every point, so the point sets are equal."""
 
 import math
 import random
@@ -24,6 +25,10 @@ def fast_filter(coeffs, small_primes):
     squares64 = {v * v % 64 for v in range(64)}
     sq = {q: {v * v % q for v in range(q)} for q in small_primes}
     lead_ok = {q: (n % 2 == 1) or (c[-1] % q in sq[q]) for q in small_primes}
+    # denominator primes: c_n a nonzero non-square mod p, even degree
+    odd_primes = [p for p in range(3, 512, 2) if all(p % f for f in range(3, int(p ** 0.5) + 1, 2))]
+    denominator_primes = [] if n % 2 else [
+        p for p in odd_primes if c[-1] % p and pow(c[-1] % p, (p - 1) // 2, p) == p - 1]
 
     def F_mod(a, d, m):
         value = sum(ci * pow(a, i, m) * pow(d, n - i, m) for i, ci in enumerate(c)) % m
@@ -31,6 +36,8 @@ def fast_filter(coeffs, small_primes):
 
     def passes(a, d):
         if d % 2 == 0 and a % 2 == 0:
+            return False
+        if any(d % p == 0 for p in denominator_primes):
             return False
         if F_mod(a % 64, d % 64, 64) not in squares64:
             return False
@@ -94,6 +101,17 @@ def test_fast_plan_divisible_denominators(rpg, oracle):
     coeffs = ["9", "1", "0", "-3", "0", "1", "4"]
     for d in (105, 3 * 5 * 7 * 11 * 13, 17 * 19 * 23, 509 * 3, 64 * 105):
         check(rpg, oracle, coeffs, 2000, d, d + 3)
+
+
+def test_fast_plan_denominator_primes(rpg, oracle):
+    # c_6 = 3 is not a square mod 5, 7 or 17: no denominator divisible by
+    # one of them keeps a survivor, and the rest match the reference plan
+    coeffs = ["9", "1", "0", "-3", "0", "1", "3"]
+    got = check(rpg, oracle, coeffs, 2000, 1, 140)
+    assert got and all(d % 5 and d % 7 and d % 17 for _, d in got)
+    assert {d for _, d in got} & {1, 2, 3, 4, 11, 13}
+    got = check(rpg, oracle, coeffs, 3000, 1, 60, square=True)
+    assert got and all(d % 5 and d % 7 for _, d in got)
 
 
 def test_fast_plan_small_buffers(rpg, oracle, golden, monkeypatch):
