@@ -47,6 +47,15 @@ constexpr int kMaxFactors = 4;
 constexpr int kMaxIntervals = 8;                        // more: sweep the whole row
 
 
+// The odd primes below 512 with ceil(2^64 / p) (mod_u32): a curve's
+// denominator primes are a bit mask over this table.
+constexpr int kOddPrimes = 96;
+struct OddPrime {
+    u32 p;
+    u32 pad;
+    unsigned long long magic;
+};
+
 struct Modulus {                   // one stage-1 modulus of a wide curve (class layout)
     long long offset;              // word offset of row 0 in the table pool
     unsigned long long magic;      // mod_u32 constant (all ones for m = 1)
@@ -82,6 +91,9 @@ struct WideCurve {
                                    // (their items are kWK classes swept side by side); else 0
     int square;
     int index;                     // position in the caller's curve list
+    int rows;                      // stage-1 moduli in use (the others are padding)
+    int pad0;
+    u64 denom_primes[2];           // bit i: odd prime i of the OddPrime table is a denominator prime
     unsigned short neg_h[kCandidatePrimes];   // (-H) mod p
     unsigned short s_mod[kCandidatePrimes];   // S mod p
     unsigned short m_mod[kCandidatePrimes];   // M mod p
@@ -102,6 +114,8 @@ struct NarrowCurve {
     int table_words;               // even
     int square;
     int index;
+    int rows;                      // stage-1 moduli in use (the others are padding)
+    u64 denom_primes[2];           // bit i: odd prime i of the OddPrime table is a denominator prime
     int m[kNarrowSlots];           // moduli (1: padding)
     int off[kNarrowSlots];         // word offset of each table inside the block
     int len[kNarrowSlots];         // row length m + kNK - 1 (rows repeat their first words)
@@ -376,6 +390,20 @@ __device__ __forceinline__ void emit(u64 m, long long base, long long step, long
     }
 }
 
+// Denominator primes: for p | d and p !| a, F(a, d) = c_n a^n (mod p), not a
+// square when c_n is not and n is even, so a denominator with such a prime
+// factor holds no points.  True if k (d = k or k^2: p | k^2 iff p | k) has a
+// prime factor in the curve's mask (the loop is uniform over the warp).
+__device__ __forceinline__ bool has_denominator_prime(u32 k, u64 mask0, u64 mask1, const OddPrime *odd) {
+    bool hit = false;
+    for (int w = 0; w < 2; ++w)
+        for (u64 m = w ? mask1 : mask0; m; m &= m - 1) {
+            const int i = 64 * w + __ffsll((long long)m) - 1;
+            hit |= mod_u32(k, __ldg(&odd[i].p), __ldg(&odd[i].magic)) == 0;
+        }
+    return hit;
+}
+
 // ---------------------------------------------------------------------------
 // Wide rows: class layout, warp-specialized like the single-curve fast
 // kernel.  Warp 0 produces denominators into two slots: it takes work items
@@ -562,8 +590,9 @@ __global__ void __launch_bounds__(kWThreads, 2)
                 int nitems, const u64 *__restrict__ pool, const u64 *__restrict__ affine,
                 const ClassStart *__restrict__ class_starts, const WideRun *__restrict__ list_runs,
                 const int *__restrict__ list_prefix, const int *__restrict__ list_count,
-                const unsigned short *__restrict__ inv_table, Candidates cand, BatchOut out,
-                int row_stride, int max_classes, unsigned long long *work) {
+                const unsigned short *__restrict__ inv_table, const OddPrime *__restrict__ odd,
+                Candidates cand, BatchOut out, int row_stride, int max_classes, unsigned long long *work,
+                unsigned long long *swept) {
     extern __shared__ __align__(16) u64 smem[];
     u64 *qmask = smem + kWSlotCount * row_stride;
     u64 *qpos = qmask + kWConsumers * kQueue;
@@ -572,6 +601,7 @@ __global__ void __launch_bounds__(kWThreads, 2)
     const int pstride = wide_prefix_stride(max_classes);
     __shared__ WideSlot slot[kWSlotCount];
     __shared__ WideCtx s_ctx[kWConsumers][kWCtx];
+    __shared__ unsigned long long s_swept[kWConsumers][2];
     __shared__ __align__(8) unsigned long long s_full[kWSlotCount];
     __shared__ __align__(8) unsigned long long s_empty[kWSlotCount];
 
@@ -616,6 +646,7 @@ __global__ void __launch_bounds__(kWThreads, 2)
             const int q = C.class_prime;
             const long long lists = C.list_count;  // -1: classes laid out here
             const unsigned long long magic_q = (~0ull) / u32(q) + 1;
+            const u64 bad0 = C.denom_primes[0], bad1 = C.denom_primes[1];
             for (int base = 0; base < item.count && !failed; base += kWarpSize) {
                 const bool valid = base + lane < item.count;
                 const long long k = item.first + base + (valid ? lane : 0);
@@ -635,6 +666,7 @@ __global__ void __launch_bounds__(kWThreads, 2)
                                (C.nint == 0 || x_range(C.lo, C.hi, C.nint, C.bound, dd, item.range, L, U));
                     }
                 }
+                if (bad0 | bad1) live = live && !has_denominator_prime(u32(k), bad0, bad1, odd);
                 for (u32 todo = __ballot_sync(kFullMask, live); todo; todo &= todo - 1) {
                     const int j = __ffs(todo) - 1;
                     const long long d = __shfl_sync(kFullMask, dd, j);
@@ -746,6 +778,10 @@ __global__ void __launch_bounds__(kWThreads, 2)
             qn -= nd;
         }
     };
+    // class words this warp sweeps, and the stage-1 shared-memory bytes
+    // they read (8 per word and row of the curve), kept in shared memory
+    unsigned long long *my_swept = s_swept[cw];
+    if (lane == 0) my_swept[0] = my_swept[1] = 0;
     for (;;) {
         if (!mbar_wait(smem_addr(&s_full[b]), (phase >> b) & 1u)) {  // bounded wait
             if (out.error && lane == 0) atomicOr(out.error, 1ull);
@@ -755,6 +791,10 @@ __global__ void __launch_bounds__(kWThreads, 2)
         const WideSlot &S = slot[b];
         if (S.d < 0) {
             drain_all();
+            if (lane == 0) {
+                atomicAdd(swept, my_swept[0]);
+                atomicAdd(swept + 1, my_swept[1]);
+            }
             return;
         }
         // context kc replaces the one taken kWCtx fills ago: its queued words go first
@@ -772,6 +812,7 @@ __global__ void __launch_bounds__(kWThreads, 2)
         const WideCurve &C = curves[S.curve];
         const unsigned char *sbase = reinterpret_cast<const unsigned char *>(smem + b * row_stride);
         const u64 stride = u64(C.stride);
+        const u32 rows = u32(__ldg(&C.rows));
         const WideRun *runs = S.runs;
         const int *prefix = S.prefix;
         const int nclass = S.nclass;
@@ -805,6 +846,11 @@ __global__ void __launch_bounds__(kWThreads, 2)
                             o[sl][kk] += 8u * (m >= 32 ? (v >= m ? v - m : v) : mod_u32(v, m, S.magic[sl]));
                         }
                     }
+                }
+                if (lane == 0) {
+                    const u32 words = (meta[0] & 0xFFu) + (meta[1] & 0xFFu) + (meta[2] & 0xFFu) + (meta[3] & 0xFFu);
+                    my_swept[0] += words;
+                    my_swept[1] += 8ull * words * rows;
                 }
 #pragma unroll 1
                 for (int step = 0; step < nsteps; ++step) {
@@ -877,6 +923,11 @@ __global__ void __launch_bounds__(kWThreads, 2)
                 const int w0 = (sweep - prefix[c]) * kWItemWords;
                 const WideRun run = runs[c];
                 const int wt = run.words;
+                if (lane == 0) {
+                    const u32 words = u32(min(kWItemWords, wt - w0));
+                    my_swept[0] += words;
+                    my_swept[1] += 8ull * words * rows;
+                }
                 const u64 first_mask = ~u64(0) << run.first;
                 const u64 last_mask = run.last >= 64 ? ~u64(0) : ((u64(1) << run.last) - 1);
                 const u64 pos0 = u64(run.ofs) + stride * u64(run.wbase);
@@ -973,8 +1024,8 @@ __device__ __forceinline__ void narrow_drain(const u64 *qmask, const u32 *qword,
 __global__ void __launch_bounds__(kNThreads, 3)
     narrow_kernel(const NarrowCurve *__restrict__ curves, const BatchItem *__restrict__ items,
                   int nitems, const u64 *__restrict__ pool, const u64 *__restrict__ affine,
-                  const unsigned short *__restrict__ inv_table, Candidates cand, BatchOut out,
-                  unsigned long long *work) {
+                  const unsigned short *__restrict__ inv_table, const OddPrime *__restrict__ odd,
+                  Candidates cand, BatchOut out, unsigned long long *work, unsigned long long *swept) {
     extern __shared__ __align__(16) u64 smem[];
     __shared__ NarrowCurve C;
     __shared__ int s_item;
@@ -995,6 +1046,8 @@ __global__ void __launch_bounds__(kNThreads, 3)
     const u32 bar = smem_addr(&s_bar);
     u32 phase = 0;
     int cur = -1;
+    // row words this warp sweeps and the stage-1 shared-memory bytes they read
+    unsigned long long swept_words = 0, swept_bytes = 0;
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
         s_abort = 0;
@@ -1066,10 +1119,18 @@ __global__ void __launch_bounds__(kNThreads, 3)
                 }
                 const u64 mask2 = C.dense2[du & 63];
                 if (!mask2) continue;
+                // denominator primes (see has_denominator_prime), split over the lanes
+                bool hit = false;
+                for (int i = lane; i < kOddPrimes; i += kWarpSize)
+                    if ((C.denom_primes[i >> 6] >> (i & 63)) & 1)
+                        hit |= mod_u32(u32(k), __ldg(&odd[i].p), __ldg(&odd[i].magic)) == 0;
+                if (__any_sync(kFullMask, hit)) continue;
                 // words [w_lo, w_hi] hold the numerator range of this item: a in [L, U]
                 long long L = -C.bound, U = C.bound;
                 if (C.nint > 0 && !x_range(C.lo, C.hi, C.nint, C.bound, d, item.range, L, U)) continue;
                 const int w_lo = int((L + C.bound) >> 6), w_hi = int((U + C.bound) >> 6);
+                swept_words += u32(w_hi - w_lo + 1);
+                swept_bytes += 8ull * u32(C.rows) * u32(w_hi - w_lo + 1);
                 const u64 first_mask = ~u64(0) << ((L + C.bound) & 63);
                 const int last_bits = int((U + C.bound) & 63) + 1;
                 const u64 last_mask = last_bits >= 64 ? ~u64(0) : ((u64(1) << last_bits) - 1);
@@ -1141,6 +1202,10 @@ __global__ void __launch_bounds__(kNThreads, 3)
             }
         }
         __syncthreads();
+    }
+    if (lane == 0) {
+        atomicAdd(swept, swept_words);
+        atomicAdd(swept + 1, swept_bytes);
     }
 }
 
@@ -1233,6 +1298,28 @@ unsigned long long host_magic(int m) {
     return m == 1 ? ~0ull : (~0ull) / (unsigned long long)m + 1;
 }
 
+// Position of the odd prime p in the list of odd primes (3 -> 0, 5 -> 1, ...).
+int odd_prime_index(int p) {
+    int i = 0;
+    for (int f = 3; f < p; f += 2) i += is_small_prime(f) ? 1 : 0;
+    return i;
+}
+
+// Bit i set iff the i-th odd prime p below 512 (p != skip) is a denominator
+// prime of the curve: even degree and c_n a nonzero non-square mod p (a
+// denominator divisible by one holds no points).
+void denominator_prime_mask(const std::vector<std::string> &coefficients, int skip, dev::u64 out[2]) {
+    out[0] = out[1] = 0;
+    if ((coefficients.size() - 1) % 2) return;
+    int i = 0;
+    for (int p = 3; p < kMaximumPrime; p += 2) {
+        if (!is_small_prime(p)) continue;
+        const int lc = decimal_mod(coefficients.back(), p);
+        if (p != skip && lc != 0 && !square_mod(lc, p)) out[i >> 6] |= dev::u64(1) << (i & 63);
+        ++i;
+    }
+}
+
 // Position of the k-th set bit (k counted from 0) of a 64-bit mask.
 int nth_bit_host(dev::u64 mask, int k) {
     for (int i = 0; i < k; ++i) mask &= mask - 1;
@@ -1304,6 +1391,7 @@ struct CurveWork {
     int classes = 1;           // wide curves: most numerator classes of one denominator
     std::unique_ptr<FastPlanner> planner;  // wide curves, until planned
     std::vector<unsigned short> cand_residues;  // c_i mod p for the 36 candidates, candidate-major
+    dev::u64 denom_primes[2] = {};             // the curve's denominator primes (no class prime removed)
 };
 
 // Words of one denominator's row that the sieve sweeps: the whole row, or with
@@ -1491,6 +1579,7 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             } else {
                 cw.plan = narrow_plan(c.coefficients);
             }
+            denominator_prime_mask(c.coefficients, 1, cw.denom_primes);
             {
                 const auto &cps = candidate_primes();
                 cw.cand_residues.reserve(kCandidatePrimes * c.coefficients.size());
@@ -1648,6 +1737,10 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             C.inv64_q = q > 1 ? int(mod_inverse(64 % q, q)) : 0;
             C.square = c.square ? 1 : 0;
             C.index = int(i);
+            C.rows = int(plan.moduli.size());
+            // the class prime's classes already leave q | d without sites
+            C.denom_primes[0] = cw.denom_primes[0] & ~(q > 1 ? dev::u64(1) << odd_prime_index(q) : 0);
+            C.denom_primes[1] = cw.denom_primes[1];
             C.aff = aff_base;
             if (C.count_q / 64 + 2 >= dev::kMaxClassWords)
                 throw std::invalid_argument("numerator bound too large for the batched search");
@@ -1722,32 +1815,6 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 for (long long f = c.first; f <= c.last; f += chunk)
                     P.wide_items.push_back({f, int(P.wide.size()), int(std::min(chunk, c.last - f + 1)),
                                             range, 0});
-            {
-                // class words swept: admissible classes of each d (by d mod 64 and
-                // d mod q), each of about 2H / (64 M) words
-                const long long per_class = (2 * H / M + 64) / 64;
-                long double classes = 0;
-                const long long qq = q > 1 ? q : 1;
-                const long long period = 64 * qq;
-                for (long long res = 0; res < period; ++res) {
-                    // parameters k in [first, last] with d(k) = res (mod 64 q)
-                    long long n = 0;
-                    if (!c.square) {
-                        const long long lo = c.first, hi = c.last;
-                        const long long base = (res - lo % period + period) % period + lo;
-                        n = base > hi ? 0 : (hi - base) / period + 1;
-                    } else {
-                        for (long long k = c.first; k <= std::min(c.last, c.first + period - 1); ++k)
-                            if ((k * k) % period == res) n += (c.last - k) / period + 1;
-                    }
-                    if (!n) continue;
-                    const int c2 = __builtin_popcountll(C.admissible[res & 63]);
-                    const int cq = q > 1 ? __builtin_popcountll(C.admissible[64 + res % q]) : 1;
-                    classes += (long double)n * c2 * cq;
-                }
-                stats.swept_words += (unsigned long long)(classes * per_class);
-                stats.smem_bytes += (unsigned long long)(classes * per_class) * 8ull * plan.moduli.size();
-            }
             P.wide.push_back(C);
             stats.wide_curves += 1;
         } else {
@@ -1756,6 +1823,9 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
             C.words = cw.words;
             C.square = c.square ? 1 : 0;
             C.index = int(i);
+            C.rows = int(plan.moduli.size());
+            C.denom_primes[0] = cw.denom_primes[0];
+            C.denom_primes[1] = cw.denom_primes[1];
             C.aff = aff_base;
             if (P.row_words % 2) P.row_words += 1;  // 16-byte aligned bulk copy
             C.tables = P.row_words;
@@ -1793,23 +1863,6 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
                 for (long long f = c.first; f <= c.last; f += chunk)
                     P.narrow_items.push_back({f, int(P.narrow.size()),
                                               int(std::min(chunk, c.last - f + 1)), range, 0});
-            {
-                long double live = 0;  // parameters whose d mod 64 admits a class
-                for (int res = 0; res < 64; ++res) {
-                    if (!C.dense2[res]) continue;
-                    long long n = 0;
-                    if (!c.square) {
-                        const long long base = (res - c.first % 64 + 64) % 64 + c.first;
-                        n = base > c.last ? 0 : (c.last - base) / 64 + 1;
-                    } else {
-                        for (long long k = c.first; k <= std::min(c.last, c.first + 63); ++k)
-                            if ((k * k) % 64 == res) n += (c.last - k) / 64 + 1;
-                    }
-                    live += n;
-                }
-                stats.swept_words += (unsigned long long)(live * cw.words);
-                stats.smem_bytes += (unsigned long long)(live * cw.words) * 8ull * plan.moduli.size();
-            }
             P.narrow.push_back(C);
         }
         stats.curves += 1;
@@ -1869,6 +1922,10 @@ struct BatchEngine::Impl {
     cudaStream_t stream = nullptr, side = nullptr;
     cudaEvent_t ev[6] = {};    // tables, wide kernel, narrow kernel (start, end)
     cudaEvent_t fork = nullptr, join = nullptr;
+    // device counters of a run: survivors, wide and narrow work items, error
+    // word, survivors kept by pre-verification, words swept, stage-1
+    // shared-memory bytes read
+    static constexpr int kCounters = 7;
     unsigned long long *h_counters = nullptr;
     unsigned long long capacity = 1ull << 20;
     dev::Candidates cand{};
@@ -1883,6 +1940,7 @@ struct BatchEngine::Impl {
     DeviceArray<int> d_lprefix, d_lcount;
     DeviceArray<unsigned short> d_res, d_inv;
     DeviceArray<dev::u64> d_sq, d_aff, d_patterns, d_rows;
+    DeviceArray<dev::OddPrime> d_odd;
     // [0] survivors [1] wide work [2] narrow work [3] error [4] pre-verified survivors
     DeviceArray<unsigned long long> d_counters;
     DeviceArray<long long> d_a, d_pa;        // survivors, and those kept by pre-verification
@@ -1922,10 +1980,15 @@ struct BatchEngine::Impl {
                 square_masks[std::size_t(p) * dev::kRefWords + sq / 64] |= dev::u64(1) << (sq % 64);
             }
         }
+        std::vector<dev::OddPrime> odd;
+        for (int p = 3; p < kMaximumPrime; p += 2)
+            if (is_small_prime(p)) odd.push_back({dev::u32(p), 0, host_magic(p)});
+        if (odd.size() != std::size_t(dev::kOddPrimes)) throw std::logic_error("odd prime table");
         unsigned long long bytes = 0;
         d_inv.upload(inv_table, stream, bytes, "upload inverses");
         d_sq.upload(square_masks, stream, bytes, "upload squares");
-        d_counters.ensure(5, "cudaMalloc(batch counters)");
+        d_odd.upload(odd, stream, bytes, "upload odd primes");
+        d_counters.ensure(kCounters, "cudaMalloc(batch counters)");
         ensure_output(capacity);
         check_cuda(cudaStreamSynchronize(stream), "batch engine setup");
     }
@@ -2089,7 +2152,7 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
         };
         auto enqueue_sieve = [&]() {
             const dev::BatchOut out{d_a.p, d_d.p, d_c.p, d_counters.p, capacity, d_counters.p + 3};
-            check_cuda(cudaMemsetAsync(d_counters.p, 0, 5 * sizeof(unsigned long long), stream),
+            check_cuda(cudaMemsetAsync(d_counters.p, 0, kCounters * sizeof(unsigned long long), stream),
                        "cudaMemsetAsync");
             if (preverify)
                 check_cuda(cudaMemsetAsync(d_curve_modular.p, 0, curves.size() * sizeof(unsigned long long), stream),
@@ -2100,8 +2163,8 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
             if (wide_grid) {
                 dev::wide_kernel<<<wide_grid, dev::kWThreads, wide_smem, stream>>>(
                     d_wide.p, d_witems.p, int(P.wide_items.size()), d_rows.p, d_aff.p, d_cls.p, d_lruns.p,
-                    d_lprefix.p, d_lcount.p, d_inv.p, cand, out, wide_smem_words, wide_max_classes,
-                    d_counters.p + 1);
+                    d_lprefix.p, d_lcount.p, d_inv.p, d_odd.p, cand, out, wide_smem_words, wide_max_classes,
+                    d_counters.p + 1, d_counters.p + 5);
                 check_cuda(cudaGetLastError(), "wide_kernel launch");
             }
             record(ev[3], stream);
@@ -2109,7 +2172,7 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
             if (narrow_grid) {
                 dev::narrow_kernel<<<narrow_grid, dev::kNThreads, narrow_smem, side>>>(
                     d_narrow.p, d_nitems.p, int(P.narrow_items.size()), d_rows.p, d_aff.p, d_inv.p,
-                    cand, out, d_counters.p + 2);
+                    d_odd.p, cand, out, d_counters.p + 2, d_counters.p + 5);
                 check_cuda(cudaGetLastError(), "narrow_kernel launch");
             }
             record(ev[5], side);
@@ -2118,7 +2181,7 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
             if (preverify)
                 pre.launch(d_a.p, d_d.p, d_c.p, d_counters.p, capacity, d_pa.p, d_pd.p, d_pc.p, d_counters.p + 4,
                            d_curve_modular.p, stream);
-            check_cuda(cudaMemcpyAsync(h_counters, d_counters.p, 5 * sizeof(unsigned long long),
+            check_cuda(cudaMemcpyAsync(h_counters, d_counters.p, kCounters * sizeof(unsigned long long),
                                        cudaMemcpyDeviceToHost, stream),
                        "download batch counters");
         };
@@ -2198,6 +2261,8 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
             if (h_counters[3]) throw DeviceTimeout("batched sieve: a bounded wait timed out");
         }
         stats.survivors = h_counters[0];
+        stats.swept_words = h_counters[5];
+        stats.smem_bytes = h_counters[6];
         // survivors for the host: those kept by pre-verification, or all
         const std::size_t n = std::size_t(preverify ? h_counters[4] : h_counters[0]);
         stats.host_candidates = n;
@@ -2221,7 +2286,7 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
                                        stream),
                        "download batch survivor counts");
         check_cuda(cudaStreamSynchronize(stream), "download batch survivors");
-        stats.d2h_bytes += n * (sizeof(long long) + 2 * sizeof(int)) + 5 * sizeof(unsigned long long) +
+        stats.d2h_bytes += n * (sizeof(long long) + 2 * sizeof(int)) + kCounters * sizeof(unsigned long long) +
                            curve_modular.size() * sizeof(unsigned long long);
 
         // ---- exact verification per curve, in single-search order ----

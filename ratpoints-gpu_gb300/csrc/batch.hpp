@@ -61,7 +61,7 @@ struct BatchStats {
     unsigned long long solo_curves = 0;       // curves with huge rows searched alone
     unsigned long long wide_items = 0, narrow_items = 0, launches = 0, words = 0;
     unsigned long long table_words = 0;
-    unsigned long long swept_words = 0;       // 64-site words the sieve kernels sweep (no intervals)
+    unsigned long long swept_words = 0;       // 64-site words the sieve kernels sweep (counted by them)
     unsigned long long smem_bytes = 0;        // stage-1 shared-memory bytes those sweeps read
     long double rectangle_sites = 0;
     double plan_ms = 0, table_ms = 0, sieve_ms = 0, verify_ms = 0, wall_ms = 0;

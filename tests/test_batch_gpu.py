@@ -305,3 +305,26 @@ def test_wide_kernel_matches_oracle(rpg, oracle):
         assert got == expected, c
         found += len(expected)
     assert found >= 20
+
+
+def test_denominator_primes_batch(rpg, oracle):
+    """Even-degree curves whose leading coefficient is a non-square mod some
+    small primes (c_6 = 3: 5, 7, 17; c_4 = -1: 3, 7, 11, 19): both batch
+    kernels skip the denominators divisible by one, which hold no points;
+    every curve's points equal the oracle's restatement of the reference
+    pipeline."""
+    sextic = ["9", "1", "0", "-3", "0", "1", "3"]
+    quartic = ["4", "0", "-5", "0", "-1"]
+    curves = [
+        {"coefficients": sextic, "bound": 70000, "first": 1, "last": 40},
+        {"coefficients": sextic, "bound": 3000, "first": 1, "last": 400},
+        {"coefficients": quartic, "bound": 5000, "first": 1, "last": 300},
+        {"coefficients": quartic, "bound": 80000, "first": 1, "last": 30, "square": True},
+    ]
+    assert all(rpg.is_squarefree(c["coefficients"]) for c in curves)
+    points, status, _, stats = rpg.batch_search(curves)
+    assert status == [0] * len(curves)
+    assert stats["wide_curves"] == 2
+    for c, got in zip(curves, points):
+        assert got == _oracle_points(oracle, c), c
+        assert all(d % 7 for _, _, d in got if d)
