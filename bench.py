@@ -51,8 +51,8 @@ NOMINAL_SMEM_BYTES_PER_CLK = 128   # LDS bandwidth per SM, for comparison with t
 # (dram__bytes_read.sum + dram__bytes_write.sum) and the ALU-pipe share.  ncu
 # runs every pass with a cold L2, so the DRAM figure is an upper bound for the
 # timed launches, whose class tables stay in L2 between launches.
-FAST_LAUNCH_PROFILE = {"dram_bytes": 45_854_464 + 140_032, "alu_pipe_frac": 0.535,
-                       "issue_active_frac": 0.637,
+FAST_LAUNCH_PROFILE = {"dram_bytes": 43_845_120 + 71_424, "alu_pipe_frac": 0.554,
+                       "issue_active_frac": 0.658,
                        "source": "profiles/fast_sieve_kernel_c2.md (ncu --set full, "
                                  "fast_sieve_kernel<7,3>, one launch)"}
 
