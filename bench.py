@@ -366,13 +366,16 @@ def record_curve_kernels(rpg, torch, flush, height=10 ** 7, denominators=10 ** 6
     return out
 
 
-def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2, shape="all", smem_peak_gbs=None):
+def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2, shape="all", smem_peak_gbs=None,
+                    tune=False):
     """Mixed many-curve batch: one batched pass against the plain per-curve
     loop of single-curve searches, same curves, points compared curve by curve.
     Both are timed end to end through the C ABI (coefficient strings in,
     verified points out).  shape "wide" / "narrow" keeps only the curves whose
     rows have at least / fewer than 2,048 words of 64 numerators (the two
-    batch kernels), for per-kernel measurements."""
+    batch kernels), for per-kernel measurements.  With tune the batch's work
+    items per kernel are tuned first (rpg_tune_batch, untimed, kept in the
+    run's tuning cache)."""
     import workloads
 
     curves = workloads.mixed_batch(count)
@@ -383,6 +386,7 @@ def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2, shape="all", sm
     mu = workloads.mobius(max(c["last"] for c in curves))
     reduced = [workloads.reduced_sites(c["bound"], c["first"], c["last"], mu) for c in curves]
     rect = [(2 * c["bound"] + 1) * (c["last"] - c["first"] + 1) for c in curves]
+    tuning = rpg.tune_batch(curves) if tune else None
     rpg.batch_search(curves[:32])  # warm-up: module load, graph instantiation paths
     runs = []
     for _ in range(steps):
@@ -415,7 +419,12 @@ def batch_benchmark(rpg, count=4096, plain_curves=4096, steps=2, shape="all", sm
                     "wide_curves": stats["wide_curves"], "survivors": stats["survivors"],
                     "points": stats["points"], "table_bytes": stats["table_words"] * 8,
                     "h2d_bytes": stats["h2d_bytes"], "d2h_bytes": stats["d2h_bytes"],
-                    "graph": bool(stats["graph"]), "launches": stats["launches"]},
+                    "graph": bool(stats["graph"]), "launches": stats["launches"],
+                    "items_per_kernel": stats["items_per_kernel"],
+                    "items_from_cache": bool(stats["items_from_cache"])},
+        "items_tuning": None if tuning is None else {
+            "key": tuning["key"], "chosen": tuning["items"],
+            "candidates_ms": {str(c["items"]): round(c["ms"], 2) for c in tuning["candidates"]}},
         "plain_loop": {"value": plain_value, "unit": UNIT, "wall_s": plain_wall,
                        "curves": n_plain,
                        "note": "rpg_point_search (single-curve fast plan) called once per curve"},
@@ -615,7 +624,8 @@ def summary(line):
     if b:
         out["batch"] = {"speedup_vs_plain": r(b.get("speedup_vs_plain"), 2),
                         "points_identical": b.get("points_identical"),
-                        "roofline_frac": r((b.get("roofline") or {}).get("frac"))}
+                        "roofline_frac": r((b.get("roofline") or {}).get("frac")),
+                        "items_per_kernel": (b.get("batched") or {}).get("items_per_kernel")}
     sv = line.get("serving") or {}
     if sv:
         out["serving"] = {"p50_ms": r(sv.get("p50_ms")), "p99_ms": r(sv.get("p99_ms")),
@@ -847,7 +857,7 @@ def main():
                                                             denominators=args.record_denominators)
     if args.batch_curves > 0:
         line["batch"] = batch_benchmark(rpg, args.batch_curves, args.batch_plain_curves,
-                                        shape=args.batch_shape, smem_peak_gbs=peak)
+                                        shape=args.batch_shape, smem_peak_gbs=peak, tune=args.tune)
     if args.restricted > 0:
         line["restricted"] = restricted_benchmark(rpg, args.restricted, args.square_cubics)
     if args.serving_requests > 0:

@@ -291,7 +291,7 @@ typedef struct rpg_batch_stats {
     uint64_t launches;         /* kernel launches (table build and sieve) */
     uint64_t words;            /* 64-site row words of all denominators */
     uint64_t table_words;      /* stage-1 table words resident on the device */
-    uint64_t swept_words;      /* 64-site words the sieve kernels sweep (whole rows) */
+    uint64_t swept_words;      /* 64-site words the sieve kernels sweep (counted by them) */
     uint64_t smem_bytes;       /* stage-1 shared-memory bytes those sweeps read */
     double rectangle_sites;    /* sum over curves of (2H + 1) x denominators */
     double plan_ms;            /* host: validation, plans, descriptors */
@@ -305,6 +305,8 @@ typedef struct rpg_batch_stats {
     uint64_t d2h_bytes;
     int32_t graph;             /* nonzero if the kernels ran as a CUDA graph */
     uint64_t host_candidates;  /* survivors given to the host's exact check */
+    int32_t items_per_kernel;  /* work-item target of the batched kernels */
+    int32_t items_from_cache;  /* 1: a stored rpg_tune_batch result chose it */
 } rpg_batch_stats;
 
 typedef int (*rpg_batch_point_cb)(int32_t curve, int64_t numerator, const char *ordinate,
@@ -314,6 +316,32 @@ rpg_status rpg_batch_search(const rpg_search_options *curves, int32_t curve_coun
                             uint32_t flags, rpg_batch_point_cb callback, void *user,
                             int32_t *curve_status, uint64_t *curve_survivors,
                             rpg_batch_stats *stats);
+
+/*
+ * Measured tuning of rpg_batch_search's work items: the batched kernels take
+ * (curve, denominator range) items from device queues, each kernel's work cut
+ * into about N items.  rpg_tune_batch runs these curves with N = 2,048, 8,192
+ * and 32,768 on one engine (after a warm-up run) and keeps the N with the
+ * least batched sieve time (CUDA events) in the RPG_TUNE_CACHE file, under the
+ * kind of batch (curve count, median row length, median degree; see
+ * rpg_tune_fast_plan for the file).  Later batches of that kind use it; without
+ * a stored value N is 8,192.  Curves that fail validation are left out.  No
+ * counterpart in the reference, which searches one curve per process.
+ */
+typedef struct rpg_batch_tune_report {
+    int32_t items;                         /* the chosen items per kernel */
+    int32_t candidates;
+    int32_t candidate_items[RPG_TUNE_MAX_CANDIDATES];
+    double candidate_ms[RPG_TUNE_MAX_CANDIDATES];  /* batched sieve time of each */
+    int32_t stored;                        /* 1: written to the RPG_TUNE_CACHE file */
+    char key[96];                          /* the kind of batch, NUL-terminated */
+} rpg_batch_tune_report;
+rpg_status rpg_tune_batch(const rpg_search_options *curves, int32_t curve_count, int32_t device,
+                          rpg_batch_tune_report *report);
+/* The work items per kernel an rpg_batch_search of these curves would use
+ * (host only): *from_cache 1 when a stored rpg_tune_batch result decides it. */
+rpg_status rpg_batch_items(const rpg_search_options *curves, int32_t curve_count, int32_t *items,
+                           int32_t *from_cache);
 
 /*
  * Serving: searches submitted at any time, answered in batches that overlap

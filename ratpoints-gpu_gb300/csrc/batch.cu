@@ -17,6 +17,7 @@
 #include "preverify.hpp"
 #include "sieve.hpp"
 #include "sieve_device.cuh"
+#include "tune.hpp"
 
 namespace rpg {
 namespace dev {
@@ -1548,7 +1549,7 @@ struct BatchPlan {
 // Validation and per-curve plans (one curve per task), then descriptors,
 // table specs and work items in the order the kernels take them.
 void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurveResult> &results,
-                BatchPlan &P, BatchStats &stats) {
+                BatchPlan &P, BatchStats &stats, int items_per_kernel) {
     P.work.resize(curves.size());
     parallel_for(curves.size(), [&](std::size_t i) {
         const BatchCurveSpec &c = curves[i];
@@ -1632,18 +1633,19 @@ void build_plan(const std::vector<BatchCurveSpec> &curves, std::vector<BatchCurv
     });
     std::vector<std::pair<std::size_t, std::size_t>> list_curves;  // (descriptor, curve) with class lists
     // items: large enough that building and fetching them stays cheap, small
-    // enough that a small batch still spreads over the device (about 8,192
-    // items per kernel): up to 2^21 row words (wide) and 2^18 swept words
-    // (narrow), at least one denominator per warp; one set per numerator range
+    // enough that a small batch still spreads over the device (about
+    // items_per_kernel items per kernel): up to 2^21 row words (wide) and 2^18
+    // swept words (narrow), at least one denominator per warp; one set per
+    // numerator range
     long double wide_work = 0, narrow_work = 0;
     for (std::size_t i : order) {
         const CurveWork &cw = P.work[i];
         (cw.wide ? wide_work : narrow_work) += (long double)(cw.wide ? cw.words : cw.swept) * cw.count;
     }
     const long long wide_item =
-        (long long)std::min<long double>(1LL << 21, std::max<long double>(1LL << 14, wide_work / 8192));
+        (long long)std::min<long double>(1LL << 21, std::max<long double>(1LL << 14, wide_work / items_per_kernel));
     const long long narrow_item =
-        (long long)std::min<long double>(1LL << 18, std::max<long double>(1LL << 12, narrow_work / 8192));
+        (long long)std::min<long double>(1LL << 18, std::max<long double>(1LL << 12, narrow_work / items_per_kernel));
     auto item_chunk = [&](const CurveWork &cw) -> long long {
         return cw.wide ? std::max(1LL, std::min<long long>(1 << 16, wide_item / cw.words))
                        : std::max<long long>(dev::kNWarps,
@@ -2015,13 +2017,20 @@ struct BatchEngine::Impl {
     }
 
     std::vector<BatchCurveResult> run(const std::vector<BatchCurveSpec> &curves, BatchStats *stats_out,
-                                      bool use_graph, bool preverify);
+                                      bool use_graph, bool preverify, int items_per_kernel);
 };
 
 std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurveSpec> &curves,
-                                                     BatchStats *stats_out, bool use_graph, bool preverify) {
+                                                     BatchStats *stats_out, bool use_graph, bool preverify,
+                                                     int items_per_kernel) {
     const auto started = Clock::now();
     BatchStats stats;
+    if (items_per_kernel <= 0) {
+        items_per_kernel = tuned_batch_items(curves);
+        stats.items_from_cache = items_per_kernel > 0;
+        if (items_per_kernel <= 0) items_per_kernel = kDefaultBatchItems;
+    }
+    stats.items_per_kernel = items_per_kernel;
     std::vector<BatchCurveResult> results(curves.size());
     check_cuda(cudaSetDevice(device), "cudaSetDevice");
     // Curves with huge rows fill the device on their own: batching gains them
@@ -2042,7 +2051,7 @@ std::vector<BatchCurveResult> BatchEngine::Impl::run(const std::vector<BatchCurv
         }
     BatchPlan P;
     const auto t_plan = Clock::now();
-    build_plan(batched, results, P, stats);
+    build_plan(batched, results, P, stats, items_per_kernel);
     stats.plan_ms = ms_since(t_plan);
     const std::vector<CurveWork> &work = P.work;
     std::exception_ptr solo_error;
@@ -2353,8 +2362,9 @@ BatchEngine::BatchEngine(int device) : impl_(new Impl(device)) {}
 BatchEngine::~BatchEngine() = default;
 
 std::vector<BatchCurveResult> BatchEngine::run(const std::vector<BatchCurveSpec> &curves,
-                                               BatchStats *stats, bool use_graph, bool preverify) {
-    return impl_->run(curves, stats, use_graph, preverify);
+                                               BatchStats *stats, bool use_graph, bool preverify,
+                                               int items_per_kernel) {
+    return impl_->run(curves, stats, use_graph, preverify, items_per_kernel);
 }
 
 int BatchEngine::device() const { return impl_->device; }

@@ -34,6 +34,9 @@ constexpr long long kBatchWideWords = 2048;
 // the single-curve kernel, beside its batched kernels.
 constexpr long long kBatchSoloWords = 1LL << 17;
 constexpr int kBatchNarrowModulus = 34;
+// Work items per batched kernel: enough that a small batch spreads over the
+// device, few enough that building and fetching them stays cheap.
+constexpr int kDefaultBatchItems = 8192;
 
 struct BatchCurveSpec {
     std::vector<std::string> coefficients;
@@ -68,6 +71,8 @@ struct BatchStats {
     double wide_ms = 0, narrow_ms = 0;
     unsigned long long h2d_bytes = 0, d2h_bytes = 0;
     bool graph = false;
+    int items_per_kernel = 0;                 // the work-item target the run used
+    bool items_from_cache = false;            // a stored tuning result chose it
 };
 
 // Device resources of batched runs kept across runs: streams, events, the
@@ -86,9 +91,12 @@ public:
     // together.  The table build and sieve launches are captured in one CUDA
     // graph when use_graph is set.  With preverify a kernel drops the
     // survivors that cannot be points before the copy to the host
-    // (preverify.hpp); the points are the same either way.
+    // (preverify.hpp); the points are the same either way.  Each kernel's
+    // work is cut into about items_per_kernel (curve, denominator range)
+    // items; 0 takes the tuned value for this kind of batch (tune.hpp), else
+    // kDefaultBatchItems.
     std::vector<BatchCurveResult> run(const std::vector<BatchCurveSpec> &curves, BatchStats *stats,
-                                      bool use_graph = true, bool preverify = true);
+                                      bool use_graph = true, bool preverify = true, int items_per_kernel = 0);
     int device() const;
 
     // Upper estimate of the device bytes a curve adds to a run (admission).

@@ -411,6 +411,32 @@ rpg_status rpg_session_plan(rpg_session *session, int32_t *class_prime, int32_t 
 
 void rpg_session_destroy(rpg_session *session) { delete session; }
 
+// The batch specs of the curves that pass the option checks (their indices
+// in valid); status[i] is RPG_E_ARG for the others.
+void batch_specs_from(const rpg_search_options *curves, int32_t curve_count, std::vector<int32_t> &status,
+                      std::vector<std::size_t> &valid, std::vector<rpg::BatchCurveSpec> &run) {
+    const std::size_t count = static_cast<std::size_t>(curve_count);
+    status.assign(count, RPG_OK);
+    for (int32_t i = 0; i < curve_count; ++i) {
+        rpg::SearchOptions s;
+        std::string error;
+        if (!options_from(curves[i], s, error)) {
+            status[std::size_t(i)] = RPG_E_ARG;
+            continue;
+        }
+        rpg::BatchCurveSpec b;
+        b.coefficients = s.coefficients;
+        b.bound = s.numerator_bound;
+        b.first = s.first;
+        b.last = s.last;
+        b.square = s.square;
+        b.include_infinity = s.include_infinity;
+        b.intervals = s.intervals;
+        valid.push_back(std::size_t(i));
+        run.push_back(std::move(b));
+    }
+}
+
 rpg_status rpg_batch_search(const rpg_search_options *curves, int32_t curve_count, int32_t device,
                             uint32_t flags, rpg_batch_point_cb callback, void *user,
                             int32_t *curve_status, uint64_t *curve_survivors,
@@ -419,33 +445,10 @@ rpg_status rpg_batch_search(const rpg_search_options *curves, int32_t curve_coun
         if (curve_count < 0 || (curve_count > 0 && !curves) || !callback)
             return fail(RPG_E_ARG, "curves and callback must not be NULL");
         const std::size_t count = static_cast<std::size_t>(curve_count);
-        std::vector<rpg::BatchCurveSpec> specs(count);
-        std::vector<int32_t> status(count, RPG_OK);
-        std::vector<std::string> errors(count);
-        for (int32_t i = 0; i < curve_count; ++i) {
-            rpg::SearchOptions s;
-            rpg::BatchCurveSpec &b = specs[std::size_t(i)];
-            if (!options_from(curves[i], s, errors[std::size_t(i)])) {
-                status[std::size_t(i)] = RPG_E_ARG;
-                b.first = 1;
-                b.last = 0;  // no work; the curve is reported as failed
-                continue;
-            }
-            b.coefficients = s.coefficients;
-            b.bound = s.numerator_bound;
-            b.first = s.first;
-            b.last = s.last;
-            b.square = s.square;
-            b.include_infinity = s.include_infinity;
-            b.intervals = s.intervals;
-        }
+        std::vector<int32_t> status;
         std::vector<std::size_t> valid;
         std::vector<rpg::BatchCurveSpec> run;
-        for (int32_t i = 0; i < curve_count; ++i)
-            if (status[std::size_t(i)] == RPG_OK) {
-                valid.push_back(std::size_t(i));
-                run.push_back(std::move(specs[std::size_t(i)]));
-            }
+        batch_specs_from(curves, curve_count, status, valid, run);
         rpg::BatchStats st;
         std::vector<rpg::BatchCurveResult> results =
             rpg::batch_search(run, device, &st, (flags & RPG_BATCH_NO_GRAPH) == 0,
@@ -488,7 +491,48 @@ rpg_status rpg_batch_search(const rpg_search_options *curves, int32_t curve_coun
             stats->h2d_bytes = st.h2d_bytes;
             stats->d2h_bytes = st.d2h_bytes;
             stats->graph = st.graph ? 1 : 0;
+            stats->items_per_kernel = st.items_per_kernel;
+            stats->items_from_cache = st.items_from_cache ? 1 : 0;
         }
+        return RPG_OK;
+    });
+}
+
+rpg_status rpg_tune_batch(const rpg_search_options *curves, int32_t curve_count, int32_t device,
+                          rpg_batch_tune_report *report) {
+    return guarded([&]() -> rpg_status {
+        if (curve_count < 1 || !curves || !report) return fail(RPG_E_ARG, "curves and report must not be NULL");
+        std::vector<int32_t> status;
+        std::vector<std::size_t> valid;
+        std::vector<rpg::BatchCurveSpec> run;
+        batch_specs_from(curves, curve_count, status, valid, run);
+        if (run.empty()) return fail(RPG_E_ARG, "no valid curve to tune on");
+        const rpg::BatchTuneResult r = rpg::tune_batch_items(run, device);
+        std::memset(report, 0, sizeof *report);
+        report->items = r.items;
+        report->candidates = int32_t(std::min<std::size_t>(r.candidates.size(), RPG_TUNE_MAX_CANDIDATES));
+        for (int i = 0; i < report->candidates; ++i) {
+            report->candidate_items[i] = r.candidates[std::size_t(i)].first;
+            report->candidate_ms[i] = r.candidates[std::size_t(i)].second;
+        }
+        report->stored = r.stored ? 1 : 0;
+        std::snprintf(report->key, sizeof report->key, "%s", r.key.c_str());
+        return RPG_OK;
+    });
+}
+
+rpg_status rpg_batch_items(const rpg_search_options *curves, int32_t curve_count, int32_t *items,
+                           int32_t *from_cache) {
+    return guarded([&]() -> rpg_status {
+        if (curve_count < 0 || (curve_count > 0 && !curves) || !items || !from_cache)
+            return fail(RPG_E_ARG, "curves and outputs must not be NULL");
+        std::vector<int32_t> status;
+        std::vector<std::size_t> valid;
+        std::vector<rpg::BatchCurveSpec> run;
+        batch_specs_from(curves, curve_count, status, valid, run);
+        const int stored = rpg::tuned_batch_items(run);
+        *items = stored > 0 ? stored : rpg::kDefaultBatchItems;
+        *from_cache = stored > 0 ? 1 : 0;
         return RPG_OK;
     });
 }

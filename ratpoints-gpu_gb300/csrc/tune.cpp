@@ -21,12 +21,23 @@ namespace {
 
 // ---------------------------------------------------------------------------
 // The cache file: {"fast_plan_shapes": {key: {"rows": R, "slots": S,
-// "sample_denominators": N, "measured_ms": {"RxS": ms, ...}}, ...}}
+// "sample_denominators": N, "measured_ms": {"RxS": ms, ...}}, ...},
+// "batch_items": {key: {"items": N, "measured_ms": {"N": ms, ...}}, ...}}
 
 struct Entry {
     FastShape shape;
     long long sample = 0;
     std::map<std::string, double> measured;
+};
+
+struct BatchEntry {
+    int items = 0;
+    std::map<std::string, double> measured;
+};
+
+struct CacheContents {
+    std::map<std::string, Entry> shapes;
+    std::map<std::string, BatchEntry> batches;
 };
 
 // A small JSON reader for the cache file: objects, strings, numbers (other
@@ -35,7 +46,7 @@ class JsonReader {
 public:
     explicit JsonReader(const std::string &text) : t_(text) {}
 
-    bool shapes(std::map<std::string, Entry> &out) {
+    bool contents(CacheContents &out) {
         try {
             skip();
             expect('{');
@@ -48,7 +59,16 @@ public:
                         const std::string key = string();
                         expect(':');
                         Entry e;
-                        if (entry(e)) out[key] = e;
+                        if (entry(e)) out.shapes[key] = e;
+                        take(',');
+                    }
+                } else if (name == "batch_items") {
+                    expect('{');
+                    while (!take('}')) {
+                        const std::string key = string();
+                        expect(':');
+                        BatchEntry e;
+                        if (batch_entry(e)) out.batches[key] = e;
                         take(',');
                     }
                 } else {
@@ -58,12 +78,33 @@ public:
             }
             return true;
         } catch (const std::exception &) {
-            out.clear();
+            out = CacheContents{};
             return false;
         }
     }
 
 private:
+    bool batch_entry(BatchEntry &e) {
+        expect('{');
+        while (!take('}')) {
+            const std::string name = string();
+            expect(':');
+            if (name == "items") e.items = int(number());
+            else if (name == "measured_ms") measured(e.measured);
+            else value();
+            take(',');
+        }
+        return e.items >= 64 && e.items <= (1 << 20);
+    }
+    void measured(std::map<std::string, double> &out) {
+        expect('{');
+        while (!take('}')) {
+            const std::string k = string();
+            expect(':');
+            out[k] = number();
+            take(',');
+        }
+    }
     bool entry(Entry &e) {
         expect('{');
         while (!take('}')) {
@@ -73,13 +114,7 @@ private:
             else if (name == "slots") e.shape.slots = int(number());
             else if (name == "sample_denominators") e.sample = (long long)number();
             else if (name == "measured_ms") {
-                expect('{');
-                while (!take('}')) {
-                    const std::string k = string();
-                    expect(':');
-                    e.measured[k] = number();
-                    take(',');
-                }
+                measured(e.measured);
             } else {
                 value();
             }
@@ -170,31 +205,65 @@ public:
     bool lookup(const std::string &path, const std::string &key, FastShape &out) {
         std::lock_guard<std::mutex> lock(mutex_);
         load(path);
-        auto it = entries_.find(key);
-        if (it == entries_.end()) return false;
+        auto it = contents_.shapes.find(key);
+        if (it == contents_.shapes.end()) return false;
         out = it->second.shape;
         return true;
+    }
+
+    int lookup_items(const std::string &path, const std::string &key) {
+        std::lock_guard<std::mutex> lock(mutex_);
+        load(path);
+        auto it = contents_.batches.find(key);
+        return it == contents_.batches.end() ? 0 : it->second.items;
     }
 
     bool store(const std::string &path, const std::string &key, const Entry &e) {
         std::lock_guard<std::mutex> lock(mutex_);
         load(path);
-        entries_[key] = e;
+        contents_.shapes[key] = e;
+        return write(path);
+    }
+
+    bool store_items(const std::string &path, const std::string &key, const BatchEntry &e) {
+        std::lock_guard<std::mutex> lock(mutex_);
+        load(path);
+        contents_.batches[key] = e;
+        return write(path);
+    }
+
+private:
+    static void write_measured(std::ostringstream &o, const std::map<std::string, double> &measured) {
+        o << "\"measured_ms\": {";
+        bool first = true;
+        for (const auto &m : measured) {
+            char buf[64];
+            std::snprintf(buf, sizeof buf, "%.6f", m.second);
+            o << (first ? "" : ", ") << json_string(m.first) << ": " << buf;
+            first = false;
+        }
+        o << "}";
+    }
+
+    bool write(const std::string &path) {
         std::ostringstream o;
         o << "{\n  \"fast_plan_shapes\": {";
         bool first = true;
-        for (const auto &kv : entries_) {
+        for (const auto &kv : contents_.shapes) {
             o << (first ? "\n" : ",\n") << "    " << json_string(kv.first) << ": {\"rows\": "
               << kv.second.shape.rows << ", \"slots\": " << kv.second.shape.slots
-              << ", \"sample_denominators\": " << kv.second.sample << ", \"measured_ms\": {";
-            bool f2 = true;
-            for (const auto &m : kv.second.measured) {
-                char buf[64];
-                std::snprintf(buf, sizeof buf, "%.6f", m.second);
-                o << (f2 ? "" : ", ") << json_string(m.first) << ": " << buf;
-                f2 = false;
-            }
-            o << "}}";
+              << ", \"sample_denominators\": " << kv.second.sample << ", ";
+            write_measured(o, kv.second.measured);
+            o << "}";
+            first = false;
+        }
+        o << "\n  },\n  \"batch_items\": {";
+        first = true;
+        for (const auto &kv : contents_.batches) {
+            o << (first ? "\n" : ",\n") << "    " << json_string(kv.first) << ": {\"items\": " << kv.second.items
+              << ", ";
+            write_measured(o, kv.second.measured);
+            o << "}";
             first = false;
         }
         o << "\n  }\n}\n";
@@ -209,23 +278,22 @@ public:
         return std::rename(tmp.c_str(), path.c_str()) == 0;
     }
 
-private:
     void load(const std::string &path) {
         if (path == loaded_path_) return;
-        entries_.clear();
+        contents_ = CacheContents{};
         std::ifstream f(path);
         if (f) {
             std::stringstream buf;
             buf << f.rdbuf();
             const std::string text = buf.str();
-            JsonReader(text).shapes(entries_);
+            JsonReader(text).contents(contents_);
         }
         loaded_path_ = path;
     }
 
     std::mutex mutex_;
     std::string loaded_path_;
-    std::map<std::string, Entry> entries_;
+    CacheContents contents_;
 };
 
 ShapeCache &cache() {
@@ -324,6 +392,55 @@ TuneResult tune_fast_shape(const std::vector<std::string> &coefficients, long lo
         e.sample = result.sample;
         for (const auto &c : result.candidates) e.measured[shape_name(c.shape)] = c.ms;
         result.stored = cache().store(path, result.key, e);
+    }
+    return result;
+}
+
+std::string batch_items_key(const std::vector<BatchCurveSpec> &curves) {
+    std::vector<long long> words, degrees;
+    for (const auto &c : curves) {
+        words.push_back(word_count64(std::max(1LL, c.bound)));
+        degrees.push_back((long long)c.coefficients.size() - 1);
+    }
+    auto median = [](std::vector<long long> &v) -> long long {
+        if (v.empty()) return 1;
+        std::nth_element(v.begin(), v.begin() + long(v.size() / 2), v.end());
+        return v[v.size() / 2];
+    };
+    const int cbits = int(std::floor(std::log2(double(std::max<std::size_t>(1, curves.size())))));
+    const int wbits = int(std::floor(std::log2(double(std::max(1LL, median(words))))));
+    return "curves2^" + std::to_string(cbits) + "-words2^" + std::to_string(wbits) +
+           (median(degrees) <= 6 ? "-degree-low" : "-degree-high");
+}
+
+int tuned_batch_items(const std::vector<BatchCurveSpec> &curves) {
+    const std::string path = tune_cache_path();
+    if (path.empty()) return 0;
+    return cache().lookup_items(path, batch_items_key(curves));
+}
+
+BatchTuneResult tune_batch_items(const std::vector<BatchCurveSpec> &curves, int device) {
+    BatchTuneResult result;
+    result.key = batch_items_key(curves);
+    BatchEngine engine(device);
+    BatchStats warm;
+    engine.run(curves, &warm, true, true, kDefaultBatchItems);  // buffers sized, modules loaded
+    double best = 0;
+    for (int items : {2048, kDefaultBatchItems, 32768}) {
+        BatchStats st;
+        engine.run(curves, &st, true, true, items);
+        result.candidates.push_back({items, st.sieve_ms});
+        if (result.items == 0 || st.sieve_ms < best) {
+            best = st.sieve_ms;
+            result.items = items;
+        }
+    }
+    const std::string path = tune_cache_path();
+    if (!path.empty()) {
+        BatchEntry e;
+        e.items = result.items;
+        for (const auto &c : result.candidates) e.measured[std::to_string(c.first)] = c.second;
+        result.stored = cache().store_items(path, result.key, e);
     }
     return result;
 }

@@ -15,8 +15,10 @@
 #pragma once
 
 #include <string>
+#include <utility>
 #include <vector>
 
+#include "batch.hpp"
 #include "sieve.hpp"
 
 namespace rpg {
@@ -49,5 +51,26 @@ TuneResult tune_fast_shape(const std::vector<std::string> &coefficients, long lo
 
 // The cache file (RPG_TUNE_CACHE), empty when tuning results are not kept.
 std::string tune_cache_path();
+
+// Measured tuning of the batch engine's work items.  The batched kernels take
+// (curve, denominator range) items from device queues, each kernel's work cut
+// into about items_per_kernel items.  The tuner runs a batch with 2,048,
+// 8,192 and 32,768 items per kernel on one engine (after a warm-up run), keeps
+// the one with the least batched sieve time and stores it under the kind of
+// batch: its curve count, median row length and median degree (low: at most
+// 6), counts and lengths in powers of two.  Later batches of that kind use it.
+struct BatchTuneResult {
+    std::string key;
+    int items = 0;                                   // the chosen items per kernel
+    std::vector<std::pair<int, double>> candidates;  // (items per kernel, batched sieve ms)
+    bool stored = false;
+};
+
+std::string batch_items_key(const std::vector<BatchCurveSpec> &curves);
+
+// The stored items per kernel for this kind of batch (0: none, or no cache file).
+int tuned_batch_items(const std::vector<BatchCurveSpec> &curves);
+
+BatchTuneResult tune_batch_items(const std::vector<BatchCurveSpec> &curves, int device);
 
 }  // namespace rpg

@@ -98,10 +98,17 @@ class BatchStats(ctypes.Structure):
                  ("rectangle_sites", "plan_ms", "table_ms", "sieve_ms", "wide_ms", "narrow_ms",
                   "verify_ms", "wall_ms")] +
                 [("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
-                 ("graph", ctypes.c_int32), ("host_candidates", ctypes.c_uint64)])
+                 ("graph", ctypes.c_int32), ("host_candidates", ctypes.c_uint64),
+                 ("items_per_kernel", ctypes.c_int32), ("items_from_cache", ctypes.c_int32)])
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class BatchTuneReport(ctypes.Structure):
+    _fields_ = [("items", ctypes.c_int32), ("candidates", ctypes.c_int32),
+                ("candidate_items", ctypes.c_int32 * 8), ("candidate_ms", ctypes.c_double * 8),
+                ("stored", ctypes.c_int32), ("key", ctypes.c_char * 96)]
 
 
 class ServerOptions(ctypes.Structure):
@@ -175,6 +182,12 @@ def load():
     lib.rpg_tune_fast_plan.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                        ctypes.c_uint32, ctypes.c_int32, ctypes.c_int64,
                                        ctypes.POINTER(TuneReport)]
+    lib.rpg_tune_batch.restype = S
+    lib.rpg_tune_batch.argtypes = [ctypes.POINTER(SearchOptions), ctypes.c_int32, ctypes.c_int32,
+                                   ctypes.POINTER(BatchTuneReport)]
+    lib.rpg_batch_items.restype = S
+    lib.rpg_batch_items.argtypes = [ctypes.POINTER(SearchOptions), ctypes.c_int32,
+                                    ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
     lib.rpg_fast_shape.restype = S
     lib.rpg_fast_shape.argtypes = [pp, ctypes.c_int32, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32),
                                    ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
@@ -308,6 +321,41 @@ def _fill_options(opts, coeffs, bound, first, last, intervals=(), include_infini
     return (ivs, cstr)
 
 
+def _batch_options(curves):
+    """The curves as an rpg_search_options array (and the buffers it points to)."""
+    arr = (SearchOptions * max(1, len(curves)))()
+    keep = []
+    for i, c in enumerate(curves):
+        keep.append(_fill_options(arr[i], coefficients_of(c["coefficients"]), c["bound"],
+                                  c["first"], c["last"], c.get("intervals", ()),
+                                  c.get("include_infinity", True), square=c.get("square", False)))
+    return arr, keep
+
+
+def tune_batch(curves, device=-1):
+    """Times the batch with 2,048, 8,192 and 32,768 work items per kernel
+    (rpg_tune_batch) and returns {"items", "key", "stored", "candidates":
+    [{"items", "ms"}, ...]}; the choice is kept in the RPG_TUNE_CACHE file when
+    that environment variable is set."""
+    arr, keep = _batch_options(curves)
+    r = BatchTuneReport()
+    _check(load().rpg_tune_batch(arr, len(curves), int(device), ctypes.byref(r)))
+    del keep
+    return {"items": r.items, "key": r.key.decode(), "stored": bool(r.stored),
+            "candidates": [{"items": r.candidate_items[i], "ms": r.candidate_ms[i]}
+                           for i in range(r.candidates)]}
+
+
+def batch_items(curves):
+    """(items per kernel, from_cache) a batch_search of these curves uses
+    (host only)."""
+    arr, keep = _batch_options(curves)
+    items, cached = ctypes.c_int32(0), ctypes.c_int32(0)
+    _check(load().rpg_batch_items(arr, len(curves), ctypes.byref(items), ctypes.byref(cached)))
+    del keep
+    return items.value, bool(cached.value)
+
+
 def batch_search(curves, device=-1, graph=True, stop_after=None, preverify=True):
     """Search many curves in one batched pass.
 
@@ -318,12 +366,7 @@ def batch_search(curves, device=-1, graph=True, stop_after=None, preverify=True)
     """
     lib = load()
     n = len(curves)
-    arr = (SearchOptions * max(1, n))()
-    keep = []
-    for i, c in enumerate(curves):
-        keep.append(_fill_options(arr[i], coefficients_of(c["coefficients"]), c["bound"],
-                                  c["first"], c["last"], c.get("intervals", ()),
-                                  c.get("include_infinity", True), square=c.get("square", False)))
+    arr, keep = _batch_options(curves)
     points = [[] for _ in range(n)]
 
     @BATCH_POINT_CB

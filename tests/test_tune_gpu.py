@@ -46,3 +46,26 @@ def test_tuner_on_a_dense_curve_keeps_points(rpg, golden, monkeypatch, tmp_path)
     monkeypatch.delenv("RPG_TUNE_CACHE")
     plain, _ = rpg.point_search(rec, 100_000, 1, 3000)
     assert tuned == plain and plain
+
+
+def test_batch_tuner_measures_stores_and_is_used(rpg, monkeypatch, tmp_path):
+    # the batch engine's work items per kernel: three targets timed, the
+    # fastest stored under the kind of batch and used by the next batch of
+    # that kind, with the same points as the default
+    import workloads
+    curves = workloads.mixed_batch(96)
+    path = tmp_path / "tuning.json"
+    monkeypatch.setenv("RPG_TUNE_CACHE", str(path))
+    report = rpg.tune_batch(curves)
+    cands = report["candidates"]
+    assert [c["items"] for c in cands] == [2048, 8192, 32768] and all(c["ms"] > 0 for c in cands)
+    assert report["items"] == min(cands, key=lambda c: c["ms"])["items"] and report["stored"]
+    stored = json.loads(path.read_text())["batch_items"][report["key"]]
+    assert stored["items"] == report["items"] and len(stored["measured_ms"]) == 3
+    assert rpg.batch_items(curves) == (report["items"], True)
+    tuned, status, _, stats = rpg.batch_search(curves)
+    assert stats["items_per_kernel"] == report["items"] and stats["items_from_cache"] == 1
+    monkeypatch.delenv("RPG_TUNE_CACHE")
+    plain, status2, _, stats2 = rpg.batch_search(curves)
+    assert stats2["items_per_kernel"] == 8192 and not stats2["items_from_cache"]
+    assert tuned == plain and status == status2
