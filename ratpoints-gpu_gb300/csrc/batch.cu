@@ -409,13 +409,13 @@ __device__ __forceinline__ bool has_denominator_prime(u32 k, u64 mask0, u64 mask
 // Wide rows: class layout, warp-specialized like the single-curve fast
 // kernel.  Warp 0 produces denominators into two slots: it takes work items
 // (curve, parameter range, numerator range) from the device queue, skips
-// parameters without admissible classes, selects the 32 reference primes
-// with 1/d mod p, points the slot at the curve's class list for the
+// parameters without admissible classes or with a denominator prime, points
+// the slot at the curve's class list for the
 // denominator's class k = (d mod 64) q + (d mod q) (or, for curves with x
 // intervals, lays out the classes clipped to the numerator range in shared
 // memory), and copies the curve's stage-1 rows into the slot by TMA.  The
 // other warps sweep each filled slot's items and release it; queued words
-// carry a private context (curve, d, primes), so they wait past later
+// carry a private context (curve, d), so they wait past later
 // denominators and curves.  No barrier spans the CTA.
 
 // One class of one denominator in the numerator range being swept: class
@@ -459,7 +459,6 @@ struct WideSlot {
     int nclass;
     int next;                      // sweep-item counter
     int steps;                     // > 0: items are groups of kWK short classes, this many steps
-    unsigned char sel[kSelectedPrimes];
 };
 
 // A denominator a consumer warp still has queued words of.
@@ -467,13 +466,15 @@ constexpr int kWCtx = 4;
 struct WideCtx {
     int d;
     int curve;
-    unsigned char sel[kSelectedPrimes];
 };
 
 // Stage 2 and emission for up to 32 queued words.  A queued word carries its
 // context (bits 56..57) and the position pos = a + H of its bit 0 (bits
-// 0..55); its sites are a = -H + pos + M j.  The curve's descriptor and
-// bitmasks are read through the read-only cache.
+// 0..55); its sites are a = -H + pos + M j.  A word meets the reference's
+// selection, the 32 largest of the 36 candidates that do not divide its d:
+// the candidates go largest first, the same one for the whole warp, each
+// skipped where it divides d, until every word has met 32 or is empty.  The
+// curve's descriptor and bitmasks are read through the read-only cache.
 __device__ __forceinline__ void wide_drain(const u64 *qmask, const u64 *qpos, int start, int n,
                                            const WideCurve *curves, const u64 *affine,
                                            const Candidates &cand, const unsigned short *inv_table,
@@ -489,14 +490,17 @@ __device__ __forceinline__ void wide_drain(const u64 *qmask, const u64 *qpos, in
     const WideCurve *Cg = curves + (lane < n ? X.curve : 0);
     const u64 p56 = pos & ((u64(1) << 56) - 1);
     const u32 hi = u32(p56 >> 16), lo = u32(p56 & 0xFFFF);
-    if (m) {
-        const u64 *aff = affine + __ldg(&Cg->aff);
-        for (int s = 0; s < kSelectedPrimes && m; ++s) {
-            const int ci = X.sel[s];
-            const u32 p = u32(cand.p[ci]), magic = cand.magic[ci];
-            // 1/d mod p (stage 2 is rare enough to look it up here rather
-            // than in the producer's path)
-            const u32 dinv = __ldg(inv_table + p * kMaximumPrime + mod_small(u32(X.d), p, magic));
+    const u64 *aff = affine + __ldg(&Cg->aff);
+    const u32 d = lane < n ? u32(X.d) : 1u;
+    // the 32 largest candidates that do not divide d, largest first
+    int tested = 0;
+    for (int ci = kCandidatePrimes - 1; ci >= 0; --ci) {
+        if (!__any_sync(kFullMask, m != 0 && tested < kSelectedPrimes)) break;
+        const u32 p = u32(cand.p[ci]), magic = cand.magic[ci];
+        const u32 rho = mod_small(d, p, magic);
+        if (m != 0 && tested < kSelectedPrimes && rho != 0) {
+            ++tested;
+            const u32 dinv = __ldg(inv_table + p * kMaximumPrime + rho);
             u32 r = mod_small(hi, p, magic);
             r = mod_small((r << 16) | lo, p, magic);  // pos mod p
             r += __ldg(&Cg->neg_h[ci]);               // a mod p
@@ -680,7 +684,6 @@ __global__ void __launch_bounds__(kWThreads, 2)
                     WideSlot &S = slot[b];
                     const u32 full = smem_addr(&s_full[b]);
                     const u32 du = u32(d);
-                    select_warp(du, cand, inv_table, S.sel, static_cast<unsigned short *>(nullptr));
                     if (lane < kWideSlots) {
                         const Modulus &Md = C.mod[lane];
                         S.magic[lane] = Md.magic;
@@ -803,7 +806,6 @@ __global__ void __launch_bounds__(kWThreads, 2)
         if (qn > 0 && seq - oldest >= kWCtx) drain_all();
         if (qn == 0) oldest = seq;
         __syncwarp();
-        ctx[kc].sel[lane] = S.sel[lane];
         if (lane == 0) {
             ctx[kc].d = int(S.d);
             ctx[kc].curve = S.curve;
