@@ -102,3 +102,57 @@ def test_plans_match_the_regression_fixture(rpg):
         assert (plan["class_prime"], plan["moduli"], plan["factors"], plan["slots"]) == \
             (want["class_prime"], want["moduli"], want["factors"], want["slots"]), row
         assert plan["bits"] == pytest.approx(want["bits"], abs=1e-9)
+
+
+def test_class_prime_minimises_the_swept_share(rpg):
+    # the planner's class prime, checked by brute force: of the primes 3..13
+    # whose classes keep at least 256 words and at most 256 classes per
+    # denominator, the one whose classes sweep the smallest share of the
+    # residue pairs (d, r) mod q (q | d admits every r != 0 only when c_n is a
+    # square mod q or the degree is odd), if that share is below 2^-0.45
+    import random
+
+    rng = random.Random(99)
+    squares64 = {v * v % 64 for v in range(64)}
+    chosen = 0
+    for _ in range(40):
+        degree = rng.choice([3, 4, 5, 6, 8])
+        coeffs = [rng.randint(-10 ** 9, 10 ** 9) for _ in range(degree + 1)]
+        if coeffs[-1] == 0:
+            coeffs[-1] = 7
+        height = rng.choice([10 ** 6, 5 * 10 ** 6, 2 * 10 ** 7])
+        plan = rpg.fast_plan(" ".join(map(str, coeffs)), height)
+
+        def f_mod(x, q):
+            return sum(c * pow(x, i, q) for i, c in enumerate(coeffs)) % q
+
+        worst2 = 0
+        for dd in range(64):
+            count = 0
+            for r in range(64):
+                if dd % 2 == 0 and r % 2 == 0:
+                    continue
+                v = sum(c * pow(r, i, 64) * pow(dd, degree - i, 64) for i, c in enumerate(coeffs)) % 64
+                if degree % 2:
+                    v = v * dd % 64
+                count += v in squares64
+            worst2 = max(worst2, count)
+        shares = {}
+        for q in (3, 5, 7, 11, 13):
+            if (2 * height + 1) / (64 * 64 * q) < 256:
+                continue
+            sq = {v * v % q for v in range(q)}
+            admitted = sum(f_mod(x, q) in sq for x in range(q))
+            lead = degree % 2 == 1 or coeffs[-1] % q in sq
+            divides = q - 1 if lead else 0
+            if worst2 * max(admitted, divides) > 256:
+                continue
+            shares[q] = ((q - 1) * admitted + divides) / (q * q)
+        best = min(shares.values(), default=1.0)
+        if best < 2 ** -0.45:
+            assert plan["class_prime"] in shares and shares[plan["class_prime"]] == pytest.approx(best), \
+                (coeffs, height, shares, plan["class_prime"])
+            chosen += 1
+        else:
+            assert plan["class_prime"] == 1, (coeffs, height, shares)
+    assert chosen >= 10
