@@ -462,14 +462,14 @@ struct WideSlot {
 };
 
 // A denominator a consumer warp still has queued words of.
-constexpr int kWCtx = 4;
+constexpr int kWCtx = 8;
 struct WideCtx {
     int d;
     int curve;
 };
 
 // Stage 2 and emission for up to 32 queued words.  A queued word carries its
-// context (bits 56..57) and the position pos = a + H of its bit 0 (bits
+// context (bits 56..58) and the position pos = a + H of its bit 0 (bits
 // 0..55); its sites are a = -H + pos + M j.  A word meets the reference's
 // selection, the 32 largest of the 36 candidates that do not divide its d:
 // the candidates go largest first, the same one for the whole warp, each
