@@ -309,13 +309,10 @@ __global__ void composite_kernel(const CompositeSpec *specs, int nspecs, const u
 // ---------------------------------------------------------------------------
 // Stage 2 and emission
 
-// The 32 largest candidates not dividing d with 1/d mod p (s_dinv null: the
-// candidates only), by one warp: lane l tests candidate 35 - l, lanes 0..3
-// also candidate 3 - l.
-template <typename Index, typename Inverse>
+// The 32 largest candidates not dividing d with 1/d mod p, by one warp: lane
+// l tests candidate 35 - l, lanes 0..3 also candidate 3 - l.
 __device__ __forceinline__ void select_warp(u32 du, const Candidates &cand,
-                                            const unsigned short *inv_table, Index *s_ci,
-                                            Inverse *s_dinv) {
+                                            const unsigned short *inv_table, int *s_ci, u32 *s_dinv) {
     const int lane = threadIdx.x & 31;
     const int ch = kCandidatePrimes - 1 - lane;
     const u32 rh = mod_small(du, u32(cand.p[ch]), cand.magic[ch]);
@@ -326,13 +323,13 @@ __device__ __forceinline__ void select_warp(u32 du, const Candidates &cand,
     const u32 below = lanemask_lt();
     const int rank_h = lane - __popc(hi_div & below);
     if (rh != 0 && rank_h < kSelectedPrimes) {
-        s_ci[rank_h] = static_cast<Index>(ch);
-        if (s_dinv) s_dinv[rank_h] = static_cast<Inverse>(__ldg(inv_table + cand.p[ch] * kMaximumPrime + rh));
+        s_ci[rank_h] = ch;
+        s_dinv[rank_h] = __ldg(inv_table + cand.p[ch] * kMaximumPrime + rh);
     }
     const int rank_l = 32 - __popc(hi_div) + lane - __popc(lo_div & below);
     if (lane < kCandidatePrimes - 32 && rl != 0 && rank_l < kSelectedPrimes) {
-        s_ci[rank_l] = static_cast<Index>(cl);
-        if (s_dinv) s_dinv[rank_l] = static_cast<Inverse>(__ldg(inv_table + cand.p[cl] * kMaximumPrime + rl));
+        s_ci[rank_l] = cl;
+        s_dinv[rank_l] = __ldg(inv_table + cand.p[cl] * kMaximumPrime + rl);
     }
     __syncwarp();
 }
