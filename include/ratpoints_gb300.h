@@ -21,7 +21,9 @@
 extern "C" {
 #endif
 
-#define RPG_ABI_VERSION 2
+/* Raised when a structure layout or a signature changes (3: rpg_batch_stats
+ * gained items_per_kernel and items_from_cache). */
+#define RPG_ABI_VERSION 3
 
 typedef enum rpg_status {
     RPG_OK = 0,

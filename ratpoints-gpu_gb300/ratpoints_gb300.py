@@ -20,6 +20,7 @@ import numpy as np
 PACKAGE = Path(__file__).resolve().parent
 ROOT = PACKAGE.parent
 LIBRARY = PACKAGE / "lib" / "librpgpu.so"
+ABI_VERSION = 3  # RPG_ABI_VERSION of include/ratpoints_gb300.h that these structures follow
 EXECUTABLE = PACKAGE / "bin" / "ratpoints_gpu"
 HEADER = ROOT / "include" / "ratpoints_gb300.h"
 
@@ -223,6 +224,9 @@ def load():
     lib.rpg_device_count.restype = ctypes.c_int32
     lib.rpg_abi_version.restype = ctypes.c_int32
     lib.rpg_last_error.restype = ctypes.c_char_p
+    if lib.rpg_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{LIBRARY} has ABI version {lib.rpg_abi_version()}, this binding expects "
+                           f"{ABI_VERSION}: rebuild it (python ratpoints-gpu_gb300/build.py)")
     _lib = lib
     return lib
 

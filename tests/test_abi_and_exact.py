@@ -14,7 +14,7 @@ def test_library_exports_every_declared_function(rpg):
     assert len(names) >= 11
     for name in names:
         assert hasattr(lib, name), name
-    assert lib.rpg_abi_version() == 2
+    assert lib.rpg_abi_version() == 3
 
 
 def test_header_declares_the_sieve_boundary(rpg):
